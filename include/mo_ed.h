@@ -1,0 +1,214 @@
+/*
+ * mo_ed.h -- C-ABI of the GB300 exact-diagonalization impurity solver.
+ *
+ * Drop-in boundary for the ED hot path of MO-DMFT (sector basis, matrix-free
+ * H*v, Lanczos, continued-fraction G(i w_n), chi^2 bath fit).  Each entry
+ * point names the reference routine it replaces (file:line in the reference
+ * project).  A Fortran host binds these with ISO_C_BINDING (see
+ * mo-dmft_gb300/fortran/mo_ed_bind.f90); every Fortran array argument is
+ * passed as a plain pointer with the Fortran (column-major, 1-based) layout
+ * described per function.
+ *
+ * Conventions
+ *   - Every function returns an int status (MO_ED_OK == 0).  The reference
+ *     has no status codes: it calls die -> MPI_Abort or STOP; a Fortran shim
+ *     maps a nonzero status to die.  mo_ed_last_error() gives the message.
+ *   - One context per host thread; a context is not re-entrant.  All device
+ *     work of a context is issued on its stream (mo_ed_create).
+ *   - Sites: 1..nsite with impurity orbitals 1..norb first, then bath levels
+ *     norb+1..nsite.  ek[nsite] is ek(1:nsite); vk[norb*nbath] is Fortran
+ *     vk(1:norb, norb+1:nsite) column-major (norb fastest).
+ *   - State word: bit (ispin-1)*nsite + isite-1 is occupation of (isite,
+ *     ispin); row index of a sector vector = iup + (idown-1)*nup (1-based,
+ *     up-spin fastest), as in the reference.
+ *   - Complex arrays are interleaved (re, im) doubles, Fortran order
+ *     (norb, nw): element (iorb, iw) at 2*((iw-1)*norb + iorb-1).
+ *   - Host-pointer entry points copy in/out through the context's stream and
+ *     synchronize it; *_dev entry points take device pointers and do not
+ *     synchronize.
+ *   - There is no CPU fallback: without a usable CUDA device, mo_ed_create
+ *     fails with MO_ED_ERR_CUDA.
+ */
+#ifndef MO_ED_H
+#define MO_ED_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define MO_ED_OK 0
+#define MO_ED_ERR_ARG 1        /* invalid argument (null pointer, bad size, NaN input) */
+#define MO_ED_ERR_SECTOR 2     /* (ne_up, ne_down) outside [0, nsite] or nsite > 15 */
+#define MO_ED_ERR_CUDA 3       /* CUDA runtime error, or no device */
+#define MO_ED_ERR_NOMEM 4      /* device allocation failed */
+#define MO_ED_ERR_NOCONV 5     /* eigensolver did not converge within its limits */
+#define MO_ED_ERR_FIT 6        /* frprmn / brent iteration limit (reference: STOP) */
+#define MO_ED_ERR_STATE 7      /* call order: model, sectors or omega not set */
+#define MO_ED_ERR_CAPACITY 8   /* caller buffer smaller than required */
+
+/* ---- precision of the sector vectors --------------------------------- */
+#define MO_ED_FP64 0           /* plain FP64 device path */
+#define MO_ED_FP32 1           /* FP32 vectors and H*v, FP64 reductions / small solves */
+
+typedef struct mo_ed_ctx mo_ed_ctx;
+
+/* Solver options.  Defaults (mo_ed_default_options) follow ed_config.f90:116-126. */
+typedef struct {
+    int nstep;          /* Lanczos steps of the Green's function (DMFT.ContinuedFractionSteps, 50) */
+    int nev;            /* eigenpairs per sector (DMFT.Nev, 30) */
+    double beta;        /* inverse temperature (DMFT.beta, 100) */
+    int precision;      /* MO_ED_FP32 (default) or MO_ED_FP64 */
+    int fortran_cmplx;  /* 1 (default): round E and w_n to float inside CMPLX as the
+                           reference does (ed_green.F90:161,177); 0: exact doubles */
+    int gs_ncv;         /* Krylov basis size of the eigensolver per restart cycle (0: auto) */
+    int gs_maxcycles;   /* restart cycles before MO_ED_ERR_NOCONV (default 200) */
+    double gs_tol;      /* relative residual tolerance of converged Ritz pairs (0: auto) */
+    int green_reorth;   /* 0 (default): the reference recurrence without reorthogonalisation
+                           (ed_lanczos.F90:53-68); 1: full reorthogonalisation */
+    int reserved[8];
+} mo_ed_options;
+
+/* ---- context ----------------------------------------------------------- */
+/* stream: a cudaStream_t, or NULL to create a private non-blocking stream. */
+int mo_ed_create(mo_ed_ctx **ctx, int device, void *stream);
+int mo_ed_destroy(mo_ed_ctx *ctx);
+const char *mo_ed_last_error(const mo_ed_ctx *ctx);
+/* Library version string. */
+const char *mo_ed_version(void);
+int mo_ed_default_options(mo_ed_options *opt);
+int mo_ed_set_options(mo_ed_ctx *ctx, const mo_ed_options *opt);
+
+/* Model globals of ed_config.f90:11-36 (Norb, Nbath, U, Jex, ek, vk).
+ * Replaces ed_read_options' model part (ed_config.f90:53-114).  Invalidates
+ * cached sector tables. */
+int mo_ed_set_model(mo_ed_ctx *ctx, int norb, int nbath, double U, double Jex,
+                    const double *ek, const double *vk);
+/* Sector list (ed_config.f90:66-80: Nsector, Nelec(:), Nup(:)). */
+int mo_ed_set_sectors(mo_ed_ctx *ctx, int nsector, const int *nelec, const int *nup);
+/* Local Matsubara grid omega(1:nwloc) (ed_green.F90:41-52). */
+int mo_ed_set_omega(mo_ed_ctx *ctx, int nw, const double *omega);
+
+/* ---- a1: binomials (ed_utils.f90:54-69 iCom) --------------------------- */
+long long mo_ed_icom(int n, int m);
+
+/* ---- a2-a5: sector basis (ed_basis.F90) -------------------------------- */
+/* Sector dimensions (ed_basis.F90:44-46). */
+int mo_ed_sector_dims(mo_ed_ctx *ctx, int ne_up, int ne_down, int *nup, int *ndown,
+                      long long *ntot);
+/* generate_basis (ed_basis.F90:35-107), computed by the combinadic unrank /
+ * rank kernels.  Outputs (any may be NULL): up[nup], down[ndown] state words
+ * in ascending order; idx_up[2^nsite], idx_down[2^nsite] 1-based ranks, 0
+ * for words outside the sector (the reference allocates only
+ * [minrange, maxrange] and leaves other words undefined). */
+int mo_ed_generate_basis(mo_ed_ctx *ctx, int ne_up, int ne_down, int *up, int *down,
+                         int *idx_up, int *idx_down);
+/* ed_basis_get (ed_basis.F90:110-124) for n 1-based rows -> state words. */
+int mo_ed_basis_get(mo_ed_ctx *ctx, int ne_up, int ne_down, long long n, const long long *idx,
+                    unsigned int *state);
+/* ed_basis_idx (ed_basis.F90:127-139) for n state words -> 1-based rows
+ * (0 for a word outside the sector). */
+int mo_ed_basis_idx(mo_ed_ctx *ctx, int ne_up, int ne_down, long long n,
+                    const unsigned int *state, long long *idx);
+
+/* ---- a6-a10: matrix-free H*v (ed_hamiltonian.F90:88-191 multiply_H) ------ */
+/* B = H*A on host FP64 arrays of ntot entries, computed on the FP64 device path. */
+int mo_ed_multiply_h(mo_ed_ctx *ctx, int ne_up, int ne_down, const double *A, double *B);
+/* Host FP32 arrays, computed on the FP32 device path. */
+int mo_ed_multiply_h_f32(mo_ed_ctx *ctx, int ne_up, int ne_down, const float *A, float *B);
+/* Device pointers; dtype MO_ED_FP64 (double) or MO_ED_FP32 (float).  Issues
+ * the H*v kernel on the context's stream; no synchronization. */
+int mo_ed_multiply_h_dev(mo_ed_ctx *ctx, int ne_up, int ne_down, int dtype, const void *dA,
+                         void *dB);
+/* FP32 input, FP64-accumulated FP64 output (the refinement operator). */
+int mo_ed_multiply_h_mixed_dev(mo_ed_ctx *ctx, int ne_up, int ne_down, const float *dA,
+                               double *dB);
+
+/* ---- a11: apply_c (ed_operators.F90:10-61) ------------------------------ */
+/* vec_out = c^dagger_(iorb,ispin) vec (pm = 1) or c_(iorb,ispin) vec (pm = 2).
+ * The reference allocates vec_out; here the caller passes its capacity
+ * (query the target sector with mo_ed_sector_dims).  *ntot_out receives the
+ * target dimension; MO_ED_ERR_SECTOR if the target sector does not exist. */
+int mo_ed_apply_c(mo_ed_ctx *ctx, int ne_up, int ne_down, const double *vec, int pm, int iorb,
+                  int ispin, double *vec_out, long long capacity, long long *ntot_out);
+
+/* ---- a12: lanczos_iteration (ed_lanczos.F90:14-68) ---------------------- */
+/* The reference three-term recurrence on the device.  a, b have nstep+1
+ * entries (0:nstep); b holds squared norms; *nstep_calc as the reference.
+ * Precision per options. */
+int mo_ed_lanczos_iteration(mo_ed_ctx *ctx, int ne_up, int ne_down, const double *vec,
+                            int *nstep_calc, double *a, double *b);
+
+/* ---- a13: diag (ed_solver.F90:107-191) ---------------------------------- */
+/* nev lowest eigenpairs of one sector (thick-restart Lanczos with full
+ * reorthogonalisation; FP64 Rayleigh quotients).  eigval[nev] (unconverged /
+ * nonexistent levels: DBL_MAX, like the reference's huge()); eigvec may be
+ * NULL or a host (ntot, nev) column-major FP64 array. */
+int mo_ed_diag(mo_ed_ctx *ctx, int ne_up, int ne_down, int nev, double *eigval, double *eigvec);
+
+/* ---- a14: ed_solve (ed_solver.F90:28-105) ------------------------------- */
+/* All sectors of mo_ed_set_sectors: eigenpairs, heapsort, Boltzmann weights,
+ * nev_calc and normalized probabilities.  Eigenvectors of the kept states stay
+ * on the device for mo_ed_calc_green_ftn.  Outputs have capacity entries;
+ * sector / level are 1-based as eigval_t (ed_solver.F90:15-20). */
+int mo_ed_solve(mo_ed_ctx *ctx, int *nev_calc, double *val, double *prob, int *sector,
+                int *level, int capacity);
+
+/* ---- a15-a16: Green's function (ed_green.F90:60-185) -------------------- */
+/* Gr(norb, nw) after mo_ed_solve: for every kept state and orbital/spin,
+ * c^dagger psi and c psi, Lanczos, and the continued fractions, all
+ * excitations batched per Lanczos step.  Gr is overwritten (Gr(:,:) = 0 at
+ * ed_green.F90:78). */
+int mo_ed_calc_green_ftn(mo_ed_ctx *ctx, double *Gr);
+/* The continued-fraction coefficients of the last mo_ed_calc_green_ftn, in
+ * the order the reference writes apbpanbn.dat (ed_green.F90:112-115,
+ * 125-128): for record r, nstep_calc[2r] (particle) and nstep_calc[2r+1]
+ * (hole), coefficients ab[r][4][nstep+1] = ap, bp, an, bn.  *nrec receives
+ * the record count; ab / nstep_calc may be NULL to query it. */
+int mo_ed_green_coeffs(mo_ed_ctx *ctx, int *nrec, int *nstep_calc, double *ab, int capacity);
+
+/* ---- a18-a22: bath fit (func.f90, frprmn.f90, ed_green.F90:260-273) ------ */
+/* FUNC (func.f90:1-45): chi^2 at x(nxsize); D_ev (norb, nwloc) complex. */
+int mo_ed_func(mo_ed_ctx *ctx, const double *x, int ns, int nwloc, int nxsize,
+               const double *omega, const double *D_ev, int nbath, int norb, double *f);
+/* dfunc (func.f90:47-142): gradient p(nxsize) (argument order as the reference). */
+int mo_ed_dfunc(mo_ed_ctx *ctx, const double *x, double *p, int nwloc, int ns, int nxsize,
+                const double *omega, const double *D_ev, int nbath, int norb);
+/* minimization (func.f90:144-163): Polak-Ribiere CG (frprmn.f90) from x, in
+ * place, with FTOL = 1e-7; *fret = final chi^2, *iter = CG iterations. */
+int mo_ed_minimization(mo_ed_ctx *ctx, double *x, int nwloc, int ns, int nxsize,
+                       const double *omega, const double *D_ev, int nbath, int norb,
+                       double *fret, int *iter);
+/* nbatch independent fits in lockstep; every line-search FUNC call of all
+ * active fits is one batched device launch.  x[nbatch][nxsize] in place;
+ * fret, iter, status have nbatch entries (status: 0, or MO_ED_ERR_FIT). */
+int mo_ed_fit_batch(mo_ed_ctx *ctx, int nbatch, double *x, int nwloc, int ns, int nxsize,
+                    const double *omega, const double *D_ev, int nbath, int norb, double ftol,
+                    double *fret, int *iter, int *status);
+/* chi^2 and gradient of nbatch parameter sets on device pointers
+ * (x[nbatch][nxsize], f[nbatch], g[nbatch][nxsize]); dev is the device copy
+ * of D_ev, omega of the grid.  No synchronization. */
+int mo_ed_chi2_grad_dev(mo_ed_ctx *ctx, int nbatch, const double *x, int nwloc, int ns,
+                        int nxsize, const double *omega, const double *D_ev, int nbath,
+                        int norb, double *f, double *g);
+/* calc_dev (ed_green.F90:260-273): D_ev(norb, nwloc) from ek(nsite), vk, ef(norb). */
+int mo_ed_calc_dev(mo_ed_ctx *ctx, int norb, int nsite, int nwloc, const double *omega,
+                   const double *ek, const double *vk, const double *ef, double *D_ev);
+
+/* ---- host helpers of the same path (no device work) --------------------- */
+/* ev_to_x / x_to_ev (func.f90:165-216). */
+int mo_ed_ev_to_x(const double *ek, const double *vk, const double *ef, int ns, int nbath,
+                  int nxsize, double *x);
+int mo_ed_x_to_ev(const double *x, int nxsize, int ns, int nbath, int norb, double *ef,
+                  double *ek, double *vk);
+
+/* ---- instrumentation -------------------------------------------------- */
+/* Number of kernels this context has launched since creation. */
+long long mo_ed_kernel_launches(const mo_ed_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,10 @@
+"""GB300 exact-diagonalization impurity solver for MO-DMFT (sm_103a).
+
+The product is the C-ABI library ``lib/libmoed.so`` (sources in ``csrc/``,
+declared in ``include/mo_ed.h`` at the repository root); ``ed.py`` mirrors the
+reference's ED / bath-fit routines on top of it; ``configs.py`` holds the
+seeded synthetic benchmark models.
+"""
+from . import configs  # noqa: F401
+from .ed import (EDError, EDSolver, FP32, FP64, Options, ev_to_x, icom, lib, matsubara,  # noqa: F401
+                 x_to_ev)

@@ -1,0 +1,587 @@
+// fit.cu -- chi^2 bath fit: FUNC / dfunc as one adjoint kernel, frprmn on
+// the host, calc_dev.
+//
+// FUNC (func.f90:1-45) and dfunc (func.f90:47-142) for x = [eps(1:nbath),
+// V(1,1:nbath), ..., V(norb,1:nbath), ef(1:norb)] (x_to_ev, func.f90:193-216):
+//   Delta(a,n) = sum_k V_ak^2 / (i w_n - eps_k) + ef_a
+//   r(a,n)     = Delta(a,n) - D_ev(a,n)
+//   chi2       = sum_{n,a} |r|^2 / w_n / (norb^2 nw)
+//   d/d eps_k  = sum_{a,n} 2 Re[conj(r) V^2 / (i w_n - eps_k)^2] / w_n / (norb^2 nw)
+//   d/d V_ak   = sum_n     2 Re[2 conj(r) V / (i w_n - eps_k)]  / w_n / (norb^2 nw)
+//   d/d ef_a   = sum_n     2 Re[r] / w_n / (norb^2 nw)
+// The kernel evaluates the forward residual and its adjoint together: one CTA
+// per parameter set, one thread per frequency stripe, per-parameter partials
+// in shared memory summed in a fixed order.  Like the reference, i w_n is
+// formed by CMPLX(0, w_n) -- a single-precision w_n -- when fortran_cmplx is
+// set, while the 1/w_n weights use the double w_n.
+//
+// frprmn / linmin / mnbrak / brent (frprmn.f90) run on the host exactly as
+// the reference (its default-REAL constants included); every FUNC / dfunc
+// they call is a device launch.  mo_ed_fit_batch runs nbatch fits in
+// lockstep: each fit is a host thread, and the FUNC / dfunc requests of all
+// waiting fits are evaluated by one batched launch.
+#include <algorithm>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <mutex>
+#include <thread>
+
+#include "internal.h"
+
+namespace moed {
+
+constexpr int kFitThreads = 128;
+constexpr int kMaxX = 60;           // nmax of frprmn.f90:12
+
+__device__ __forceinline__ double2 zdiv(double2 a, double2 b)   // Smith (1962)
+{
+    if (fabs(b.x) >= fabs(b.y)) {
+        const double r = b.y / b.x, den = b.x + b.y * r;
+        return make_double2((a.x + a.y * r) / den, (a.y - a.x * r) / den);
+    }
+    const double r = b.x / b.y, den = b.x * r + b.y;
+    return make_double2((a.x * r + a.y) / den, (a.y * r - a.x) / den);
+}
+
+// x: [nreq][nx]; dev: Fortran (norb, nw) interleaved complex; f: [nreq];
+// g: [nreq][nx] (written only where want_grad[b] != 0, or all if want_grad null)
+__global__ void __launch_bounds__(kFitThreads)
+k_chi2(const double *__restrict__ x, int nx, const int *__restrict__ want_grad, int nw, int norb,
+       int nbath, const double *__restrict__ omega, const double *__restrict__ dev, int fcmplx,
+       double *__restrict__ f, double *__restrict__ g)
+{
+    extern __shared__ double sm[];          // [nx + 1][kFitThreads]
+    const int b = blockIdx.x, tid = threadIdx.x;
+    const double *xb = x + (size_t)b * nx;
+    const bool grad = g != nullptr && (want_grad ? want_grad[b] != 0 : true);
+    const int nrow = grad ? nx + 1 : 1;
+    for (int i = 0; i < nrow; ++i) sm[i * kFitThreads + tid] = 0.0;
+    // parameters (x_to_ev)
+    const double *eps = xb;                       // eps_k
+    const double *V = xb + nbath;                 // V[a*nbath + k]
+    const double *ef = xb + nx - norb;            // ef_a
+    for (int n = tid; n < nw; n += kFitThreads) {
+        const double w = omega[n];
+        const double wz = fcmplx ? (double)(float)w : w;
+        const double inv_w = 1.0 / w;
+        for (int a = 0; a < norb; ++a) {
+            double2 d = make_double2(0.0, 0.0);
+            for (int k = 0; k < nbath; ++k) {
+                const double v = V[a * nbath + k];
+                const double2 z = make_double2(0.0 - eps[k], wz);
+                const double2 t = zdiv(make_double2(v * v, 0.0), z);
+                d.x += t.x;
+                d.y += t.y;
+            }
+            d.x += ef[a];
+            const size_t di = 2 * ((size_t)n * norb + a);
+            const double2 r = make_double2(d.x - dev[di], d.y - dev[di + 1]);
+            const double ar = hypot(r.x, r.y);
+            sm[0 * kFitThreads + tid] += ar * ar / w;
+            if (grad) {
+                const double2 rc = make_double2(r.x, -r.y);
+                for (int k = 0; k < nbath; ++k) {
+                    const double v = V[a * nbath + k];
+                    const double2 z = make_double2(0.0 - eps[k], wz);
+                    // conjg(r)*vk*vk/(z)/(z)
+                    const double2 t1 = zdiv(zdiv(make_double2(rc.x * v * v, rc.y * v * v), z), z);
+                    sm[(1 + k) * kFitThreads + tid] += 2.0 * t1.x * inv_w;
+                    // conjg(r)*vk/(z) + conjg(r)*vk/(z)
+                    const double2 t2 = zdiv(make_double2(rc.x * v, rc.y * v), z);
+                    sm[(1 + nbath + a * nbath + k) * kFitThreads + tid] += 2.0 * (t2.x + t2.x) * inv_w;
+                }
+                sm[(1 + nx - norb + a) * kFitThreads + tid] += 2.0 * r.x * inv_w;
+            }
+        }
+    }
+    __syncthreads();
+    const double fn = (double)(float)(norb * norb * nw);
+    const double gn1 = (double)(float)(norb * norb), gn2 = (double)(float)nw;
+    for (int i = tid; i < nrow; i += kFitThreads) {
+        double s = 0.0;
+        for (int t = 0; t < kFitThreads; ++t) s += sm[i * kFitThreads + t];
+        if (i == 0) f[b] = s / fn;
+        else g[(size_t)b * nx + (i - 1)] = s / gn1 / gn2;
+    }
+}
+
+// calc_dev (ed_green.F90:260-273)
+__global__ void k_calc_dev(int norb, int nbath, int nw, const double *omega, const double *ek,
+                           const double *vk, const double *ef, int fcmplx, double *dev)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= norb * nw) return;
+    const int i = t / norb, a = t - i * norb;
+    const double wz = fcmplx ? (double)(float)omega[i] : omega[i];
+    double2 d = make_double2(0.0, 0.0);
+    for (int k = 0; k < nbath; ++k) {
+        const double v = vk[(size_t)k * norb + a];
+        const double2 q = zdiv(make_double2(v * v, 0.0), make_double2(0.0 - ek[norb + k], wz));
+        d.x += q.x;
+        d.y += q.y;
+    }
+    dev[2 * (size_t)t] = d.x + ef[a];
+    dev[2 * (size_t)t + 1] = d.y;
+}
+
+static int chi2_smem_attr(mo_ed_ctx *ctx)
+{
+    MOED_CUDA(ctx, cudaFuncSetAttribute(k_chi2, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)(sizeof(double) * (kMaxX + 1) * kFitThreads)));
+    return MO_ED_OK;
+}
+
+int chi2_grad_dev(mo_ed_ctx *ctx, int nbatch, const double *x, int nwloc, int ns, int nxsize,
+                  const double *omega, const double *dev, int nbath, int norb, double *f, double *g,
+                  int want_grad)
+{
+    (void)ns;
+    if (nbatch <= 0) return MO_ED_OK;
+    const size_t smem = sizeof(double) * (size_t)(nxsize + 1) * kFitThreads;
+    if (int rc = chi2_smem_attr(ctx)) return rc;
+    k_chi2<<<nbatch, kFitThreads, smem, ctx->stream>>>(x, nxsize, nullptr, nwloc, norb, nbath, omega, dev,
+                                                       ctx->opt.fortran_cmplx, f, want_grad ? g : nullptr);
+    MOED_CHECK_LAUNCH(ctx);
+    return MO_ED_OK;
+}
+
+// ---------------------------------------------------------------------------
+// device evaluator shared by the host fit drivers
+// ---------------------------------------------------------------------------
+struct FitProblem {
+    int nwloc, ns, nxsize, nbath, norb;
+    DevBuf omega, dev;        // device copies
+};
+
+static int fit_problem(mo_ed_ctx *ctx, FitProblem &P, const double *omega, const double *D_ev, int nwloc,
+                       int ns, int nxsize, int nbath, int norb)
+{
+    if (!omega || !D_ev || nwloc < 1 || nbath < 0 || norb < 1 || ns != norb + nbath ||
+        nxsize != nbath + nbath * norb + norb || nxsize > kMaxX)
+        return fail(ctx, MO_ED_ERR_ARG, "invalid fit dimensions");
+    P.nwloc = nwloc;
+    P.ns = ns;
+    P.nxsize = nxsize;
+    P.nbath = nbath;
+    P.norb = norb;
+    if (int rc = dev_alloc(ctx, P.omega, sizeof(double) * nwloc)) return rc;
+    if (int rc = dev_alloc(ctx, P.dev, sizeof(double) * 2 * (size_t)norb * nwloc)) return rc;
+    MOED_CUDA(ctx, cudaMemcpyAsync(P.omega.p, omega, sizeof(double) * nwloc, cudaMemcpyHostToDevice, ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpyAsync(P.dev.p, D_ev, sizeof(double) * 2 * (size_t)norb * nwloc,
+                                   cudaMemcpyHostToDevice, ctx->stream));
+    return chi2_smem_attr(ctx);
+}
+
+// Evaluate nreq requests (x host [nreq][nx], want_grad host [nreq]).
+struct Evaluator {
+    mo_ed_ctx *ctx;
+    FitProblem *P;
+    DevBuf dx, dw, df, dg;
+    size_t cap = 0;
+    int eval(int nreq, const double *x, const int *want, double *f, double *g)
+    {
+        const int nx = P->nxsize;
+        if ((size_t)nreq > cap) {
+            if (int rc = dev_alloc(ctx, dx, sizeof(double) * nreq * nx)) return rc;
+            if (int rc = dev_alloc(ctx, dw, sizeof(int) * nreq)) return rc;
+            if (int rc = dev_alloc(ctx, df, sizeof(double) * nreq)) return rc;
+            if (int rc = dev_alloc(ctx, dg, sizeof(double) * nreq * nx)) return rc;
+            cap = nreq;
+        }
+        MOED_CUDA(ctx, cudaMemcpyAsync(dx.p, x, sizeof(double) * nreq * nx, cudaMemcpyHostToDevice, ctx->stream));
+        MOED_CUDA(ctx, cudaMemcpyAsync(dw.p, want, sizeof(int) * nreq, cudaMemcpyHostToDevice, ctx->stream));
+        const size_t smem = sizeof(double) * (size_t)(nx + 1) * kFitThreads;
+        k_chi2<<<nreq, kFitThreads, smem, ctx->stream>>>((const double *)dx.p, nx, (const int *)dw.p, P->nwloc,
+                                                         P->norb, P->nbath, (const double *)P->omega.p,
+                                                         (const double *)P->dev.p, ctx->opt.fortran_cmplx,
+                                                         (double *)df.p, (double *)dg.p);
+        MOED_CHECK_LAUNCH(ctx);
+        MOED_CUDA(ctx, cudaMemcpyAsync(f, df.p, sizeof(double) * nreq, cudaMemcpyDeviceToHost, ctx->stream));
+        if (g)
+            MOED_CUDA(ctx, cudaMemcpyAsync(g, dg.p, sizeof(double) * nreq * nx, cudaMemcpyDeviceToHost, ctx->stream));
+        MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        return MO_ED_OK;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// frprmn.f90 restated on the host; func(x) / dfunc(x, g) through callbacks
+// ---------------------------------------------------------------------------
+template <typename F, typename DF>
+struct Frprmn {
+    F func;
+    DF dfunc;
+    int n;
+    const double *pcom = nullptr, *xicom = nullptr;
+    double xt[kMaxX];
+
+    static double fsign(double a, double b) { return b >= 0.0 ? std::fabs(a) : -std::fabs(a); }
+
+    double f1dim(double x)   // frprmn.f90:212-234
+    {
+        for (int j = 0; j < n; ++j) xt[j] = pcom[j] + x * xicom[j];
+        return func(xt);
+    }
+
+    void mnbrak(double &ax, double &bx, double &cx, double &fa, double &fb, double &fc)
+    {
+        const double GOLD = (double)1.618034f, GLIMIT = (double)100.f, TINY = (double)1.e-20f;
+        double dum, fu, q, r, u, ulim;
+        fa = f1dim(ax);
+        fb = f1dim(bx);
+        if (fb > fa) {
+            dum = ax; ax = bx; bx = dum;
+            dum = fb; fb = fa; fa = dum;
+        }
+        cx = bx + GOLD * (bx - ax);
+        fc = f1dim(cx);
+        while (fb >= fc) {
+            r = (bx - ax) * (fb - fc);
+            q = (bx - cx) * (fb - fa);
+            u = bx - ((bx - cx) * q - (bx - ax) * r) / (2. * fsign(std::fmax(std::fabs(q - r), TINY), q - r));
+            ulim = bx + GLIMIT * (cx - bx);
+            if ((bx - u) * (u - cx) > 0.) {
+                fu = f1dim(u);
+                if (fu < fc) {
+                    ax = bx; fa = fb; bx = u; fb = fu;
+                    return;
+                } else if (fu > fb) {
+                    cx = u; fc = fu;
+                    return;
+                }
+                u = cx + GOLD * (cx - bx);
+                fu = f1dim(u);
+            } else if ((cx - u) * (u - ulim) > 0.) {
+                fu = f1dim(u);
+                if (fu < fc) {
+                    bx = cx; cx = u; u = cx + GOLD * (cx - bx);
+                    fb = fc; fc = fu;
+                    fu = f1dim(u);
+                }
+            } else if ((u - ulim) * (ulim - cx) >= 0.) {
+                u = ulim;
+                fu = f1dim(u);
+            } else {
+                u = cx + GOLD * (cx - bx);
+                fu = f1dim(u);
+            }
+            ax = bx; bx = cx; cx = u;
+            fa = fb; fb = fc; fc = fu;
+        }
+    }
+
+    int brent(double ax, double bx, double cx, double tol, double &xmin, double &fret)
+    {
+        const int ITMAX = 100;
+        const double CGOLD = (double).3819660f, ZEPS = (double)1.0e-10f;
+        double a, b, d = 0.0, e, etemp, fu, fv, fw, fx, p, q, r, tol1, tol2, u, v, w, x, xm;
+        a = std::fmin(ax, cx);
+        b = std::fmax(ax, cx);
+        v = bx; w = v; x = v;
+        e = 0.;
+        fx = f1dim(x);
+        fv = fx; fw = fx;
+        for (int iter = 1; iter <= ITMAX; ++iter) {
+            xm = 0.5 * (a + b);
+            tol1 = tol * std::fabs(x) + ZEPS;
+            tol2 = 2. * tol1;
+            if (std::fabs(x - xm) <= (tol2 - .5 * (b - a))) {
+                xmin = x;
+                fret = fx;
+                return 0;
+            }
+            bool golden = true;
+            if (std::fabs(e) > tol1) {
+                r = (x - w) * (fx - fv);
+                q = (x - v) * (fx - fw);
+                p = (x - v) * q - (x - w) * r;
+                q = 2. * (q - r);
+                if (q > 0.) p = -p;
+                q = std::fabs(q);
+                etemp = e;
+                e = d;
+                if (!(std::fabs(p) >= std::fabs(.5 * q * etemp) || p <= q * (a - x) || p >= q * (b - x))) {
+                    d = p / q;
+                    u = x + d;
+                    if (u - a < tol2 || b - u < tol2) d = fsign(tol1, xm - x);
+                    golden = false;
+                }
+            }
+            if (golden) {
+                e = (x >= xm) ? a - x : b - x;
+                d = CGOLD * e;
+            }
+            u = (std::fabs(d) >= tol1) ? x + d : x + fsign(tol1, d);
+            fu = f1dim(u);
+            if (fu <= fx) {
+                if (u >= x) a = x; else b = x;
+                v = w; fv = fw; w = x; fw = fx; x = u; fx = fu;
+            } else {
+                if (u < x) a = u; else b = u;
+                if (fu <= fw || w == x) {
+                    v = w; fv = fw; w = u; fw = fu;
+                } else if (fu <= fv || v == x || v == w) {
+                    v = u; fv = fu;
+                }
+            }
+        }
+        xmin = x;
+        fret = fx;
+        return MO_ED_ERR_FIT;
+    }
+
+    int linmin(double *p, double *xi, double &fret)
+    {
+        const double TOL = (double)1.e-8f;
+        double pc[kMaxX], xc[kMaxX], ax, xx, bx, fa, fx, fb, xmin = 0.0;
+        for (int j = 0; j < n; ++j) {
+            pc[j] = p[j];
+            xc[j] = xi[j];
+        }
+        pcom = pc;
+        xicom = xc;
+        ax = 0.;
+        xx = 1.;
+        mnbrak(ax, xx, bx, fa, fx, fb);
+        int rc = brent(ax, xx, bx, TOL, xmin, fret);
+        for (int j = 0; j < n; ++j) {
+            xi[j] = xmin * xi[j];
+            p[j] = p[j] + xi[j];
+        }
+        return rc;
+    }
+
+    int run(double *p, double ftol, int &iter, double &fret)
+    {
+        const int itmax = 20000;
+        const double eps = 1.e-10;
+        double g[kMaxX], h[kMaxX], xi[kMaxX], dgg, fp, gam, gg;
+        fp = func(p);
+        dfunc(p, xi);
+        for (int j = 0; j < n; ++j) {
+            g[j] = -xi[j];
+            h[j] = g[j];
+            xi[j] = h[j];
+        }
+        for (int its = 1; its <= itmax; ++its) {
+            iter = its;
+            if (int rc = linmin(p, xi, fret)) return rc;
+            if (2. * std::fabs(fret - fp) <= ftol * (std::fabs(fret) + std::fabs(fp) + eps)) return 0;
+            fp = fret;
+            dfunc(p, xi);
+            gg = 0.;
+            dgg = 0.;
+            for (int j = 0; j < n; ++j) {
+                gg = gg + g[j] * g[j];
+                dgg = dgg + (xi[j] + g[j]) * xi[j];
+            }
+            if (gg == 0.) return 0;
+            gam = dgg / gg;
+            for (int j = 0; j < n; ++j) {
+                g[j] = -xi[j];
+                h[j] = g[j] + gam * h[j];
+                xi[j] = h[j];
+            }
+        }
+        return MO_ED_ERR_FIT;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// lockstep batching of many fits: each fit is a host thread; evaluations of
+// all waiting fits go to the device together
+// ---------------------------------------------------------------------------
+struct Batcher {
+    Evaluator *ev;
+    int nx;
+    std::mutex mu;
+    std::condition_variable cv_done;
+    int live = 0, waiting = 0;
+    long long generation = 0;
+    int err = 0;
+    std::vector<double> xs, fs, gs;   // requests of the open batch / results of the last one
+    std::vector<int> want;
+
+    void init(int nfit) { live = nfit; }
+
+    // Called by one fit; blocks until the batch holding its request has been
+    // evaluated.  A new batch can only close after every reader of the last
+    // one has submitted again or finished, so fs / gs stay valid for them.
+    double request(const double *x, double *g)
+    {
+        std::unique_lock<std::mutex> lk(mu);
+        const int slot = (int)want.size();
+        xs.insert(xs.end(), x, x + nx);
+        want.push_back(g != nullptr);
+        ++waiting;
+        const long long gen = generation;
+        if (waiting == live) flush();
+        else cv_done.wait(lk, [&] { return generation != gen; });
+        if (g)
+            for (int j = 0; j < nx; ++j) g[j] = gs[(size_t)slot * nx + j];
+        return fs[slot];
+    }
+    void finish()
+    {
+        std::unique_lock<std::mutex> lk(mu);
+        --live;
+        if (live > 0 && waiting == live) flush();
+    }
+
+  private:
+    void flush()
+    {
+        const int nreq = (int)want.size();
+        fs.assign(nreq, 0.0);
+        gs.assign((size_t)nreq * nx, 0.0);
+        if (int rc = ev->eval(nreq, xs.data(), want.data(), fs.data(), gs.data())) err = rc;
+        xs.clear();
+        want.clear();
+        waiting = 0;
+        ++generation;
+        cv_done.notify_all();
+    }
+};
+
+}  // namespace moed
+
+using namespace moed;
+
+extern "C" {
+
+int mo_ed_func(mo_ed_ctx *ctx, const double *x, int ns, int nwloc, int nxsize, const double *omega,
+               const double *D_ev, int nbath, int norb, double *f)
+{
+    if (!ctx) return MO_ED_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (!x || !f) return fail(ctx, MO_ED_ERR_ARG, "null argument");
+    FitProblem P;
+    if (int rc = fit_problem(ctx, P, omega, D_ev, nwloc, ns, nxsize, nbath, norb)) return rc;
+    Evaluator ev{ctx, &P};
+    int want = 0;
+    return ev.eval(1, x, &want, f, nullptr);
+}
+
+int mo_ed_dfunc(mo_ed_ctx *ctx, const double *x, double *p, int nwloc, int ns, int nxsize,
+                const double *omega, const double *D_ev, int nbath, int norb)
+{
+    if (!ctx) return MO_ED_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (!x || !p) return fail(ctx, MO_ED_ERR_ARG, "null argument");
+    FitProblem P;
+    if (int rc = fit_problem(ctx, P, omega, D_ev, nwloc, ns, nxsize, nbath, norb)) return rc;
+    Evaluator ev{ctx, &P};
+    int want = 1;
+    double f;
+    return ev.eval(1, x, &want, &f, p);
+}
+
+int mo_ed_chi2_grad_dev(mo_ed_ctx *ctx, int nbatch, const double *x, int nwloc, int ns, int nxsize,
+                        const double *omega, const double *D_ev, int nbath, int norb, double *f,
+                        double *g)
+{
+    if (!ctx) return MO_ED_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (!x || !f || !omega || !D_ev || nbatch < 0 || nxsize > kMaxX ||
+        nxsize != nbath + nbath * norb + norb || ns != norb + nbath)
+        return fail(ctx, MO_ED_ERR_ARG, "bad arguments");
+    return chi2_grad_dev(ctx, nbatch, x, nwloc, ns, nxsize, omega, D_ev, nbath, norb, f, g, g != nullptr);
+}
+
+int mo_ed_minimization(mo_ed_ctx *ctx, double *x, int nwloc, int ns, int nxsize, const double *omega,
+                       const double *D_ev, int nbath, int norb, double *fret, int *iter)
+{
+    if (!ctx) return MO_ED_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (!x || !fret || !iter) return fail(ctx, MO_ED_ERR_ARG, "null argument");
+    FitProblem P;
+    if (int rc = fit_problem(ctx, P, omega, D_ev, nwloc, ns, nxsize, nbath, norb)) return rc;
+    Evaluator ev{ctx, &P};
+    int err = 0;
+    auto func = [&](const double *xx) {
+        double f = 0;
+        int w = 0;
+        if (int rc = ev.eval(1, xx, &w, &f, nullptr)) err = rc;
+        return f;
+    };
+    auto dfunc = [&](const double *xx, double *g) {
+        double f = 0;
+        int w = 1;
+        if (int rc = ev.eval(1, xx, &w, &f, g)) err = rc;
+    };
+    Frprmn<decltype(func), decltype(dfunc)> fr{func, dfunc, nxsize};
+    int rc = fr.run(x, 1.0e-7, *iter, *fret);   // FTOL (func.f90:155)
+    if (err) return err;
+    if (rc) return fail(ctx, rc, "frprmn: iteration limit exceeded");
+    return MO_ED_OK;
+}
+
+int mo_ed_fit_batch(mo_ed_ctx *ctx, int nbatch, double *x, int nwloc, int ns, int nxsize,
+                    const double *omega, const double *D_ev, int nbath, int norb, double ftol,
+                    double *fret, int *iter, int *status)
+{
+    if (!ctx) return MO_ED_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (nbatch < 1 || !x || !fret || !iter || !status || !(ftol > 0))
+        return fail(ctx, MO_ED_ERR_ARG, "bad arguments");
+    FitProblem P;
+    if (int rc = fit_problem(ctx, P, omega, D_ev, nwloc, ns, nxsize, nbath, norb)) return rc;
+    Evaluator ev{ctx, &P};
+    Batcher B;
+    B.ev = &ev;
+    B.nx = nxsize;
+    B.init(nbatch);
+    std::vector<std::thread> th;
+    th.reserve(nbatch);
+    for (int b = 0; b < nbatch; ++b) {
+        th.emplace_back([&, b] {
+            auto func = [&](const double *xx) { return B.request(xx, nullptr); };
+            auto dfunc = [&](const double *xx, double *g) { B.request(xx, g); };
+            Frprmn<decltype(func), decltype(dfunc)> fr{func, dfunc, nxsize};
+            int it = 0;
+            double fr_ = 0.0;
+            int rc = fr.run(x + (size_t)b * nxsize, ftol, it, fr_);
+            fret[b] = fr_;
+            iter[b] = it;
+            status[b] = rc;
+            B.finish();
+        });
+    }
+    for (auto &t : th) t.join();
+    if (B.err) return fail(ctx, B.err, "batched chi^2 evaluation failed");
+    return MO_ED_OK;
+}
+
+int mo_ed_calc_dev(mo_ed_ctx *ctx, int norb, int nsite, int nwloc, const double *omega, const double *ek,
+                   const double *vk, const double *ef, double *D_ev)
+{
+    if (!ctx) return MO_ED_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    const int nbath = nsite - norb;
+    if (norb < 1 || nbath < 0 || nwloc < 1 || !omega || !ek || !ef || !D_ev || (nbath > 0 && !vk))
+        return fail(ctx, MO_ED_ERR_ARG, "bad arguments");
+    DevBuf dom, dek, dvk, def, ddev;
+    if (int rc = dev_alloc(ctx, dom, sizeof(double) * nwloc)) return rc;
+    if (int rc = dev_alloc(ctx, dek, sizeof(double) * nsite)) return rc;
+    if (int rc = dev_alloc(ctx, dvk, sizeof(double) * std::max(1, norb * nbath))) return rc;
+    if (int rc = dev_alloc(ctx, def, sizeof(double) * norb)) return rc;
+    if (int rc = dev_alloc(ctx, ddev, sizeof(double) * 2 * (size_t)norb * nwloc)) return rc;
+    MOED_CUDA(ctx, cudaMemcpyAsync(dom.p, omega, sizeof(double) * nwloc, cudaMemcpyHostToDevice, ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpyAsync(dek.p, ek, sizeof(double) * nsite, cudaMemcpyHostToDevice, ctx->stream));
+    if (nbath > 0)
+        MOED_CUDA(ctx, cudaMemcpyAsync(dvk.p, vk, sizeof(double) * norb * nbath, cudaMemcpyHostToDevice, ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpyAsync(def.p, ef, sizeof(double) * norb, cudaMemcpyHostToDevice, ctx->stream));
+    const int T = 128;
+    k_calc_dev<<<(norb * nwloc + T - 1) / T, T, 0, ctx->stream>>>(norb, nbath, nwloc, (const double *)dom.p,
+                                                                  (const double *)dek.p, (const double *)dvk.p,
+                                                                  (const double *)def.p, ctx->opt.fortran_cmplx,
+                                                                  (double *)ddev.p);
+    MOED_CHECK_LAUNCH(ctx);
+    MOED_CUDA(ctx, cudaMemcpyAsync(D_ev, ddev.p, sizeof(double) * 2 * (size_t)norb * nwloc, cudaMemcpyDeviceToHost,
+                                   ctx->stream));
+    MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return MO_ED_OK;
+}
+
+}  // extern "C"

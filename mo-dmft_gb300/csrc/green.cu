@@ -1,0 +1,489 @@
+// green.cu -- excitations, ed_solve and the continued-fraction Green's function.
+//
+//  apply_c        ed_operators.F90:10-61  (one thread per target element)
+//  ed_solve       ed_solver.F90:28-105    (sectors -> eigenpairs, heapsort,
+//                                          Boltzmann weights, nev_calc)
+//  ed_calc_green  ed_green.F90:60-185     (all c+psi / c psi starts of all
+//                                          kept states advance together in
+//                                          the batched reference recurrence;
+//                                          G(i w_n) from one CF kernel)
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+
+#include "krylov.cuh"
+
+namespace moed {
+
+// ---------------------------------------------------------------------------
+// apply_c
+// ---------------------------------------------------------------------------
+// Row i of the target sector: apply the opposite operator to its state
+// (destruction for pm = 1, creation for pm = 2) and gather the source
+// element with the operator's sign; zero where the operator annihilates the
+// state (ed_operators.F90:44-58).
+template <typename T>
+__global__ void k_apply_c_up(const T *__restrict__ x, T *__restrict__ y, int nu_out, int nd, int nu_in,
+                             const int *__restrict__ out_words, const int *__restrict__ in_rank,
+                             int bit, int pm)
+{
+    const long long n = (long long)nu_out * nd;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int u = (int)(i % nu_out);
+        const long long d = i / nu_out;
+        const unsigned w = (unsigned)out_words[u];
+        const bool occ = (w >> bit) & 1u;
+        T v = T(0);
+        if ((pm == 1) == occ) {
+            const int sgn = __popc(w & ((1u << bit) - 1u)) & 1;
+            const int j = in_rank[w ^ (1u << bit)];
+            const T src = x[d * nu_in + j];
+            v = sgn ? -src : src;
+        }
+        y[i] = v;
+    }
+}
+
+// spin down: the sign also counts every up-spin bit (bitidx = nsite + iorb - 1),
+// i.e. a factor (-1)^(N_up) on top of the down-word parity.
+template <typename T>
+__global__ void k_apply_c_dn(const T *__restrict__ x, T *__restrict__ y, int nu, int nd_out,
+                             const int *__restrict__ out_words, const int *__restrict__ in_rank,
+                             int bit, int pm, int up_parity)
+{
+    const long long n = (long long)nu * nd_out;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int u = (int)(i % nu);
+        const int d = (int)(i / nu);
+        const unsigned w = (unsigned)out_words[d];
+        const bool occ = (w >> bit) & 1u;
+        T v = T(0);
+        if ((pm == 1) == occ) {
+            const int sgn = (__popc(w & ((1u << bit) - 1u)) + up_parity) & 1;
+            const int j = in_rank[w ^ (1u << bit)];
+            const T src = x[(long long)j * nu + u];
+            v = sgn ? -src : src;
+        }
+        y[i] = v;
+    }
+}
+
+int apply_c_dev(mo_ed_ctx *ctx, const Sector &in, const Sector &out, int prec, const void *x, void *y,
+                int pm, int iorb, int ispin)
+{
+    const long long n = out.D();
+    if (n <= 0) return MO_ED_OK;
+    const int T = 256;
+    const int g = (int)std::max(1LL, std::min((n + T - 1) / T, (long long)ctx->num_sms * 8));
+    const int bit = iorb - 1;
+    if (ispin == 1) {
+        if (prec == MO_ED_FP32)
+            k_apply_c_up<float><<<g, T, 0, ctx->stream>>>((const float *)x, (float *)y, out.up->n, out.dn->n,
+                                                         in.up->n, out.up->words, in.up->rank, bit, pm);
+        else
+            k_apply_c_up<double><<<g, T, 0, ctx->stream>>>((const double *)x, (double *)y, out.up->n, out.dn->n,
+                                                          in.up->n, out.up->words, in.up->rank, bit, pm);
+    } else {
+        const int upar = out.ne_up & 1;
+        if (prec == MO_ED_FP32)
+            k_apply_c_dn<float><<<g, T, 0, ctx->stream>>>((const float *)x, (float *)y, out.up->n, out.dn->n,
+                                                         out.dn->words, in.dn->rank, bit, pm, upar);
+        else
+            k_apply_c_dn<double><<<g, T, 0, ctx->stream>>>((const double *)x, (double *)y, out.up->n, out.dn->n,
+                                                          out.dn->words, in.dn->rank, bit, pm, upar);
+    }
+    MOED_CHECK_LAUNCH(ctx);
+    return MO_ED_OK;
+}
+
+// ---------------------------------------------------------------------------
+// host restatements used by ed_solve: heapsort (func.f90:301-353) and
+// boltzmann_factor (ed_solver.F90:193-219) -- O(nev*nsector) scalar work
+// ---------------------------------------------------------------------------
+static void heapsort_index(int n, const double *arrin, int *indx)
+{
+    const double *A = arrin - 1;
+    int *X = indx - 1;
+    if (n == 1) {
+        X[1] = 1;
+        return;
+    }
+    for (int j = 1; j <= n; ++j) X[j] = j;
+    int l = n / 2 + 1, ir = n, indxt, i, j;
+    double q;
+    for (;;) {
+        if (l > 1) {
+            l = l - 1;
+            indxt = X[l];
+            q = A[indxt];
+        } else {
+            indxt = X[ir];
+            q = A[indxt];
+            X[ir] = X[1];
+            ir = ir - 1;
+            if (ir == 1) {
+                X[1] = indxt;
+                return;
+            }
+        }
+        i = l;
+        j = l + l;
+        while (j <= ir) {
+            if (j < ir && A[X[j]] < A[X[j + 1]]) j = j + 1;
+            if (q < A[X[j]]) {
+                X[i] = X[j];
+                i = j;
+                j = j + j;
+            } else {
+                j = ir + 1;
+            }
+        }
+        X[i] = indxt;
+    }
+}
+
+static void boltzmann(const double *elv, int nev, double beta, double *p)
+{
+    for (int i = 0; i < nev; ++i) {
+        double Z = 0.0, en = elv[i];
+        bool zero = false;
+        for (int k = 0; k < nev; ++k) {
+            if (-beta * (elv[k] - en) > 10.0) {
+                zero = true;
+                break;
+            }
+            Z = Z + std::exp(-beta * (elv[k] - en));
+        }
+        p[i] = zero ? 0.0 : 1.0 / Z;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// continued fraction (ed_green.F90:160-168, 176-184)
+// ---------------------------------------------------------------------------
+struct CfRec {
+    int iorb;        // 0-based
+    int np, nn;      // nstep_calc of the particle / hole runs (-1: no run)
+    double E, weight;  // eigenvalue, pev*factor
+};
+
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b)   // Smith (1962)
+{
+    if (fabs(b.x) >= fabs(b.y)) {
+        const double r = b.y / b.x, den = b.x + b.y * r;
+        return make_double2((a.x + a.y * r) / den, (a.y - a.x * r) / den);
+    }
+    const double r = b.x / b.y, den = b.x * r + b.y;
+    return make_double2((a.x * r + a.y) / den, (a.y * r - a.x) / den);
+}
+
+// One thread per (iorb, iw); records accumulated in the reference's order.
+__global__ void k_green_cf(const CfRec *__restrict__ rec, int nrec, const double *__restrict__ ab,
+                           int ld, const double *__restrict__ omega, int nw, int norb,
+                           int fcmplx, double *__restrict__ Gr)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nw * norb) return;
+    const int iw = t / norb, iorb = t - iw * norb;
+    const double w = fcmplx ? (double)(float)omega[iw] : omega[iw];
+    double gre = 0.0, gim = 0.0;
+    for (int r = 0; r < nrec; ++r) {
+        const CfRec R = rec[r];
+        if (R.iorb != iorb) continue;
+        const double *ap = ab + (size_t)r * 4 * ld, *bp = ap + ld, *an = bp + ld, *bn = an + ld;
+        if (R.np >= 0) {
+            const double er = fcmplx ? (double)(float)R.E : R.E;
+            double2 z = make_double2(er, w);
+            double2 g = cdiv(make_double2(bp[R.np], 0.0), make_double2(z.x - ap[R.np], z.y));
+            for (int j = R.np - 1; j >= 0; --j)
+                g = cdiv(make_double2(bp[j], 0.0), make_double2(z.x - ap[j] - g.x, z.y - g.y));
+            gre += R.weight * g.x;
+            gim += R.weight * g.y;
+        }
+        if (R.nn >= 0) {
+            const double er = fcmplx ? (double)(float)(-R.E) : -R.E;
+            double2 z = make_double2(er, w);
+            double2 g = cdiv(make_double2(bn[R.nn], 0.0), make_double2(z.x + an[R.nn], z.y));
+            for (int j = R.nn - 1; j >= 0; --j)
+                g = cdiv(make_double2(bn[j], 0.0), make_double2(z.x + an[j] - g.x, z.y - g.y));
+            gre += R.weight * g.x;
+            gim += R.weight * g.y;
+        }
+    }
+    Gr[2 * ((size_t)iw * norb + iorb)] = gre;
+    Gr[2 * ((size_t)iw * norb + iorb) + 1] = gim;
+}
+
+// ---------------------------------------------------------------------------
+// ed_calc_green_ftn
+// ---------------------------------------------------------------------------
+int calc_green(mo_ed_ctx *ctx, double *Gr)
+{
+    if (ctx->states.empty()) return fail(ctx, MO_ED_ERR_STATE, "mo_ed_solve has not been run");
+    if (ctx->omega.empty()) return fail(ctx, MO_ED_ERR_STATE, "omega grid not set");
+    const int prec = ctx->opt.precision;
+    const int nstep = ctx->opt.nstep;
+    const int norb = ctx->norb;
+    const size_t es = prec == MO_ED_FP32 ? sizeof(float) : sizeof(double);
+
+    // excitation list in the reference's record order
+    struct Exc {
+        int iev, ispin, iorb, pm;
+        Sector in, out;
+        bool ok;
+    };
+    std::vector<Exc> exc;
+    std::vector<GreenRecord> recs;
+    for (size_t iev = 0; iev < ctx->states.size(); ++iev) {
+        const StateVec &st = ctx->states[iev];
+        const int nu = ctx->nup[st.sector], nd = ctx->nelec[st.sector] - nu;
+        const bool even = nd == nu;
+        Sector in;
+        if (int rc = get_sector(ctx, nu, nd, &in)) return rc;
+        for (int ispin = 1; ispin <= (even ? 1 : 2); ++ispin)
+            for (int iorb = 1; iorb <= norb; ++iorb) {
+                GreenRecord g;
+                g.iev = (int)iev + 1;
+                g.iorb = iorb;
+                g.even = even;
+                g.val = st.val;
+                g.prob = st.prob;
+                g.np = g.nn = 0;
+                recs.push_back(g);
+                for (int pm = 1; pm <= 2; ++pm) {
+                    Exc e;
+                    e.iev = (int)iev;
+                    e.ispin = ispin;
+                    e.iorb = iorb;
+                    e.pm = pm;
+                    e.in = in;
+                    const int d = pm == 1 ? 1 : -1;
+                    const int tu = nu + (ispin == 1 ? d : 0), td = nd + (ispin == 2 ? d : 0);
+                    e.ok = tu >= 0 && tu <= ctx->nsite && td >= 0 && td <= ctx->nsite;
+                    if (e.ok)
+                        if (int rc = get_sector(ctx, tu, td, &e.out)) return rc;
+                    exc.push_back(e);
+                }
+            }
+    }
+    // batched reference Lanczos over all valid excitations
+    std::vector<double> normsq(exc.size(), 0.0);
+    std::vector<int> nsc(exc.size(), -1);
+    std::vector<std::vector<double>> A(exc.size()), B(exc.size());
+    std::vector<int> valid;
+    for (size_t i = 0; i < exc.size(); ++i)
+        if (exc[i].ok) valid.push_back((int)i);
+    for (size_t b0 = 0; b0 < valid.size(); b0 += kLzMaxRuns) {
+        const size_t b1 = std::min(valid.size(), b0 + kLzMaxRuns);
+        std::vector<Sector> secs;
+        for (size_t k = b0; k < b1; ++k) secs.push_back(exc[valid[k]].out);
+        LzBatch lb;
+        if (int rc = lz_setup(ctx, lb, secs, prec, nstep)) return rc;
+        for (size_t k = b0; k < b1; ++k) {
+            const Exc &e = exc[valid[k]];
+            const StateVec &st = ctx->states[e.iev];
+            if (int rc = apply_c_dev(ctx, e.in, e.out, prec, st.vec.p, lz_start_vector(lb, (int)(k - b0)),
+                                     e.pm, e.iorb, e.ispin))
+                return rc;
+        }
+        std::vector<std::vector<double>> a, bb;
+        std::vector<int> nc;
+        if (int rc = lz_run(ctx, lb, a, bb, nc)) return rc;
+        // normsq = ||start||^2 (ed_green.F90:157): nrm[0] of each run
+        std::vector<double> coef(lb.coef.bytes / sizeof(double));
+        MOED_CUDA(ctx, cudaMemcpyAsync(coef.data(), lb.coef.p, lb.coef.bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        for (size_t k = b0; k < b1; ++k) {
+            const int r = (int)(k - b0), i = valid[k];
+            normsq[i] = coef[(size_t)2 * (nstep + 1) * r + (nstep + 1)];
+            nsc[i] = nc[r];
+            A[i] = a[r];
+            B[i] = bb[r];
+        }
+        (void)es;
+    }
+    // records: ap, bp(0) = normsq, an, bn(0) = 1 - normsq (ed_green.F90:158,174)
+    const int ld = nstep + 1;
+    std::vector<double> ab(recs.size() * 4 * (size_t)ld, 0.0);
+    std::vector<CfRec> cf(recs.size());
+    for (size_t r = 0; r < recs.size(); ++r) {
+        const Exc &ep = exc[2 * r], &en = exc[2 * r + 1];
+        GreenRecord &g = recs[r];
+        const double nsq = normsq[2 * r];
+        g.ap.assign(ld, 0.0);
+        g.bp.assign(ld, 0.0);
+        g.an.assign(ld, 0.0);
+        g.bn.assign(ld, 0.0);
+        if (ep.ok) {
+            g.ap = A[2 * r];
+            g.bp = B[2 * r];
+        }
+        if (en.ok) {
+            g.an = A[2 * r + 1];
+            g.bn = B[2 * r + 1];
+        }
+        g.bp[0] = nsq;
+        g.bn[0] = 1.0 - nsq;
+        g.np = ep.ok ? nsc[2 * r] : 0;
+        g.nn = en.ok ? nsc[2 * r + 1] : 0;
+        const StateVec &st = ctx->states[ep.iev];
+        const int nu = ctx->nup[st.sector], nd = ctx->nelec[st.sector] - nu;
+        cf[r].iorb = g.iorb - 1;
+        cf[r].np = ep.ok ? g.np : -1;
+        cf[r].nn = en.ok ? g.nn : -1;
+        cf[r].E = st.val;
+        cf[r].weight = st.prob * (nd == nu ? 1.0 : 0.5);
+        std::copy(g.ap.begin(), g.ap.end(), ab.begin() + (r * 4 + 0) * ld);
+        std::copy(g.bp.begin(), g.bp.end(), ab.begin() + (r * 4 + 1) * ld);
+        std::copy(g.an.begin(), g.an.end(), ab.begin() + (r * 4 + 2) * ld);
+        std::copy(g.bn.begin(), g.bn.end(), ab.begin() + (r * 4 + 3) * ld);
+    }
+    ctx->green = recs;
+    const int nw = (int)ctx->omega.size();
+    DevBuf drec, dab, dom, dG;
+    if (int rc = dev_alloc(ctx, drec, sizeof(CfRec) * std::max<size_t>(1, cf.size()))) return rc;
+    if (int rc = dev_alloc(ctx, dab, sizeof(double) * std::max<size_t>(1, ab.size()))) return rc;
+    if (int rc = dev_alloc(ctx, dom, sizeof(double) * nw)) return rc;
+    if (int rc = dev_alloc(ctx, dG, sizeof(double) * 2 * (size_t)nw * norb)) return rc;
+    MOED_CUDA(ctx, cudaMemcpyAsync(drec.p, cf.data(), sizeof(CfRec) * cf.size(), cudaMemcpyHostToDevice, ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpyAsync(dab.p, ab.data(), sizeof(double) * ab.size(), cudaMemcpyHostToDevice, ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpyAsync(dom.p, ctx->omega.data(), sizeof(double) * nw, cudaMemcpyHostToDevice, ctx->stream));
+    const int T = 128;
+    k_green_cf<<<(nw * norb + T - 1) / T, T, 0, ctx->stream>>>((const CfRec *)drec.p, (int)cf.size(),
+                                                              (const double *)dab.p, ld, (const double *)dom.p,
+                                                              nw, norb, ctx->opt.fortran_cmplx, (double *)dG.p);
+    MOED_CHECK_LAUNCH(ctx);
+    MOED_CUDA(ctx, cudaMemcpyAsync(Gr, dG.p, sizeof(double) * 2 * (size_t)nw * norb, cudaMemcpyDeviceToHost, ctx->stream));
+    MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return MO_ED_OK;
+}
+
+}  // namespace moed
+
+using namespace moed;
+
+extern "C" {
+
+int mo_ed_diag(mo_ed_ctx *ctx, int ne_up, int ne_down, int nev, double *eigval, double *eigvec)
+{
+    if (!ctx) return MO_ED_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (nev < 1 || !eigval) return fail(ctx, MO_ED_ERR_ARG, "bad arguments");
+    Sector s;
+    if (int rc = get_sector(ctx, ne_up, ne_down, &s)) return rc;
+    std::vector<double> vals;
+    std::vector<DevBuf> vecs;
+    if (int rc = diag_sector(ctx, s, nev, vals, eigvec ? &vecs : nullptr)) return rc;
+    for (int i = 0; i < nev; ++i) eigval[i] = vals[i];
+    if (eigvec) {
+        const long long D = s.D();
+        DevBuf tmp;
+        if (ctx->opt.precision == MO_ED_FP32)
+            if (int rc = dev_alloc(ctx, tmp, sizeof(double) * D)) return rc;
+        for (int i = 0; i < nev; ++i) {
+            double *dst = eigvec + (size_t)i * D;
+            if (i >= (int)vecs.size()) {
+                memset(dst, 0, sizeof(double) * D);
+                continue;
+            }
+            if (ctx->opt.precision == MO_ED_FP32) {
+                if (int rc = convert_f32_to_f64(ctx, (const float *)vecs[i].p, (double *)tmp.p, D)) return rc;
+                MOED_CUDA(ctx, cudaMemcpyAsync(dst, tmp.p, sizeof(double) * D, cudaMemcpyDeviceToHost, ctx->stream));
+            } else {
+                MOED_CUDA(ctx, cudaMemcpyAsync(dst, vecs[i].p, sizeof(double) * D, cudaMemcpyDeviceToHost, ctx->stream));
+            }
+            MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        }
+    }
+    return MO_ED_OK;
+}
+
+int mo_ed_solve(mo_ed_ctx *ctx, int *nev_calc, double *val, double *prob, int *sector, int *level,
+                int capacity)
+{
+    if (!ctx) return MO_ED_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (!nev_calc) return fail(ctx, MO_ED_ERR_ARG, "null nev_calc");
+    if (ctx->nelec.empty()) return fail(ctx, MO_ED_ERR_STATE, "sectors not set");
+    const int nsector = (int)ctx->nelec.size(), nev = ctx->opt.nev;
+    std::vector<double> eig_all((size_t)nev * nsector, DBL_MAX);
+    std::vector<std::vector<DevBuf>> vecs(nsector);
+    ctx->states.clear();
+    for (int is = 0; is < nsector; ++is) {
+        Sector s;
+        if (int rc = get_sector(ctx, ctx->nup[is], ctx->nelec[is] - ctx->nup[is], &s)) return rc;
+        std::vector<double> v;
+        if (int rc = diag_sector(ctx, s, nev, v, &vecs[is])) return rc;
+        for (int i = 0; i < nev; ++i) eig_all[(size_t)is * nev + i] = v[i];
+    }
+    const int ntot = nev * nsector;
+    std::vector<int> ind(ntot);
+    std::vector<double> pev(ntot);
+    heapsort_index(ntot, eig_all.data(), ind.data());
+    boltzmann(eig_all.data(), ntot, ctx->opt.beta, pev.data());
+    int nc = 0;
+    for (int i = 0; i < nev && i < ntot; ++i)
+        if (pev[ind[i] - 1] > 0.001) ++nc;   // PROB_THRESHOLD (ed_solver.F90:14)
+    double Z = 0.0;
+    for (int i = 0; i < nc; ++i) Z += pev[ind[i] - 1];
+    *nev_calc = nc;
+    for (int i = 0; i < nc; ++i) {
+        const int k = ind[i] - 1;
+        StateVec st;
+        st.sector = k / nev;
+        st.level = k % nev;
+        st.val = eig_all[k];
+        st.prob = pev[k] / Z;
+        if (st.level < (int)vecs[st.sector].size()) std::swap(st.vec, vecs[st.sector][st.level]);
+        ctx->states.push_back(std::move(st));
+        // std::move of DevBuf: ensure ownership transferred
+    }
+    if (nc > capacity) return fail(ctx, MO_ED_ERR_CAPACITY, "output capacity below nev_calc");
+    for (int i = 0; i < nc; ++i) {
+        if (val) val[i] = ctx->states[i].val;
+        if (prob) prob[i] = ctx->states[i].prob;
+        if (sector) sector[i] = ctx->states[i].sector + 1;
+        if (level) level[i] = ctx->states[i].level + 1;
+    }
+    return MO_ED_OK;
+}
+
+int mo_ed_calc_green_ftn(mo_ed_ctx *ctx, double *Gr)
+{
+    if (!ctx) return MO_ED_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (!Gr) return fail(ctx, MO_ED_ERR_ARG, "null Gr");
+    return calc_green(ctx, Gr);
+}
+
+int mo_ed_green_coeffs(mo_ed_ctx *ctx, int *nrec, int *nstep_calc, double *ab, int capacity)
+{
+    if (!ctx || !nrec) return MO_ED_ERR_ARG;
+    const int n = (int)ctx->green.size();
+    *nrec = n;
+    if (!nstep_calc && !ab) return MO_ED_OK;
+    if (capacity < n) return fail(ctx, MO_ED_ERR_CAPACITY, "capacity below record count");
+    const int ld = ctx->opt.nstep + 1;
+    for (int r = 0; r < n; ++r) {
+        const GreenRecord &g = ctx->green[r];
+        if (nstep_calc) {
+            nstep_calc[2 * r] = g.np;
+            nstep_calc[2 * r + 1] = g.nn;
+        }
+        if (ab) {
+            double *o = ab + (size_t)r * 4 * ld;
+            for (int j = 0; j < ld; ++j) {
+                o[j] = j < (int)g.ap.size() ? g.ap[j] : 0.0;
+                o[ld + j] = j < (int)g.bp.size() ? g.bp[j] : 0.0;
+                o[2 * ld + j] = j < (int)g.an.size() ? g.an[j] : 0.0;
+                o[3 * ld + j] = j < (int)g.bn.size() ? g.bn[j] : 0.0;
+            }
+        }
+    }
+    return MO_ED_OK;
+}
+
+}  // extern "C"

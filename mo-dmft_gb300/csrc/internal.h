@@ -1,0 +1,233 @@
+// internal.h -- shared declarations of the GB300 ED solver (sm_103a).
+//
+// Data layout in HBM
+//   A sector vector X of dimension D = nup*ndown is stored as ndown rows of
+//   nup contiguous elements: X[idown][iup] (row index iup + idown*nup,
+//   0-based) -- the reference's row order (ed_basis.F90:120-123,137-138).
+//   Every H*v term that moves only up-spin electrons stays inside a row;
+//   down-spin moves are whole-row AXPYs.
+//
+//   Per spin species (nsite sites, N electrons) the device holds
+//     words[n]          ascending state words (colex unrank),
+//     rank[2^nsite]     inverse table (-1 outside the species),
+//     hop_tgt/val[hw][n] up to hw compacted hybridisation moves per word
+//                        (slot-major so a warp reading slot s of 32
+//                        consecutive words is coalesced),
+//     hop_cnt[n]        number of valid moves,
+//     diag[n]           species part of the diagonal.
+//   Because the impurity orbitals are the lowest bits, words sharing their
+//   bath bits are contiguous in rank order ("bath groups"); spin-flip and
+//   pair-hopping only move within a bath group by a rank offset that depends
+//   on the impurity bits alone, kept in a 2^norb-entry table.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/mo_ed.h"
+
+namespace moed {
+
+constexpr int kMaxSite = 15;      // 2*nsite <= 30 bits in an int32 state word (ed_config.f90:8)
+constexpr int kMaxOrb = 5;        // impurity orbitals handled by the 4-operator tables
+constexpr int kMaxPair = kMaxOrb * (kMaxOrb - 1);
+constexpr int kMaxImp = 1 << kMaxOrb;
+constexpr int kMaxHop = 64;       // max nonzero couplings norb*nbath (15 sites: <= 56)
+
+// ---------------------------------------------------------------------------
+// device model constants (one per context; rebuilt by mo_ed_set_model)
+// ---------------------------------------------------------------------------
+struct ModelDev {
+    int norb, nbath, nsite, npair, nimp, ncpl;
+    double U, J;
+    // 4-operator transfer table T_{i<-j}(I) for impurity pattern I and ordered
+    // pair p=(i,j): bit31 valid, bit30 negative sign, low 16 bits signed rank delta
+    int t4[kMaxPair * kMaxImp];
+    int pair_rev[kMaxPair];       // index of (j,i) for p=(i,j)
+    double cross[kMaxImp * kMaxImp];  // interspecies diagonal U n_i^up n_i^dn + (U-2J) n_i^up n_j^dn
+};
+
+// ---------------------------------------------------------------------------
+// spin species tables
+// ---------------------------------------------------------------------------
+struct Species {
+    int nsite = 0, N = 0, n = 0, hw = 0;
+    int *words = nullptr;
+    int *rank = nullptr;
+    int *hop_cnt = nullptr;
+    int *hop_tgt = nullptr;
+    double *hop_val_d = nullptr;
+    float *hop_val_f = nullptr;
+    double *diag_d = nullptr;
+    float *diag_f = nullptr;
+    int max_cnt = 0;              // largest hop_cnt over words
+    ~Species();
+};
+
+struct Sector {
+    int ne_up, ne_down;
+    Species *up, *dn;
+    long long D() const { return (long long)up->n * dn->n; }
+};
+
+// ---------------------------------------------------------------------------
+// H*v job (one vector of one sector); the kernel walks a list of jobs
+// ---------------------------------------------------------------------------
+template <typename TA>
+struct HvJobT {
+    const void *x;            // input vector (TX)
+    void *y;                  // output vector (TY)
+    double *dot_partial;      // optional [nitems]: sum over the item of x*y
+    int nu, nd;
+    int item0, nitems;
+    const int *up_words, *up_cnt, *up_tgt;
+    const TA *up_val, *up_diag;
+    const int *dn_words, *dn_cnt, *dn_tgt;
+    const TA *dn_val, *dn_diag;
+    int up_hw, dn_hw, dn_maxcnt, pad;
+    const int *active;        // optional device flag: job skipped when *active == 0
+};
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+struct DevBuf {              // owning device allocation (move-only)
+    void *p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    DevBuf(DevBuf &&o) noexcept : p(o.p), bytes(o.bytes)
+    {
+        o.p = nullptr;
+        o.bytes = 0;
+    }
+    DevBuf &operator=(DevBuf &&o) noexcept
+    {
+        if (this != &o) {
+            release();
+            p = o.p;
+            bytes = o.bytes;
+            o.p = nullptr;
+            o.bytes = 0;
+        }
+        return *this;
+    }
+    void release();
+    ~DevBuf() { release(); }
+};
+
+struct StateVec {             // an eigenpair kept on the device after ed_solve
+    int sector;               // 0-based index into the sector list
+    int level;                // 0-based level within the sector
+    double val, prob;
+    DevBuf vec;               // FP32 or FP64 per precision
+};
+
+struct GreenRecord {          // one apbpanbn.dat record (ed_green.F90:112-115)
+    int iev, iorb, even;
+    double val, prob;
+    int np, nn;
+    std::vector<double> ap, bp, an, bn;
+};
+
+}  // namespace moed
+
+struct mo_ed_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int num_sms = 0;
+    std::string err;
+    mo_ed_options opt;
+    long long launches = 0;
+
+    // model
+    bool have_model = false;
+    int norb = 0, nbath = 0, nsite = 0;
+    double U = 0, J = 0;
+    std::vector<double> ek, vk;   // vk column-major (norb fastest)
+    moed::ModelDev mdl;
+    moed::ModelDev *d_mdl = nullptr;
+    std::vector<int> cpl_orb, cpl_bath;  // nonzero couplings in reference loop order
+    std::vector<double> cpl_val;
+    std::map<int, std::unique_ptr<moed::Species>> species;  // by N
+
+    // sectors / omega
+    std::vector<int> nelec, nup;
+    std::vector<double> omega;
+
+    // results of ed_solve / green
+    std::vector<moed::StateVec> states;
+    std::vector<moed::GreenRecord> green;
+
+    // scratch
+    moed::DevBuf scratch_a, scratch_b, scratch_part;
+};
+
+namespace moed {
+
+// ---- error helpers --------------------------------------------------------
+int fail(mo_ed_ctx *ctx, int code, const std::string &msg);
+int cuda_fail(mo_ed_ctx *ctx, cudaError_t e, const char *what);
+#define MOED_CUDA(ctx, call)                                              \
+    do {                                                                  \
+        cudaError_t e_ = (call);                                          \
+        if (e_ != cudaSuccess) return ::moed::cuda_fail((ctx), e_, #call); \
+    } while (0)
+#define MOED_CHECK_LAUNCH(ctx)                                            \
+    do {                                                                  \
+        (ctx)->launches++;                                                \
+        cudaError_t e_ = cudaGetLastError();                              \
+        if (e_ != cudaSuccess) return ::moed::cuda_fail((ctx), e_, "kernel launch"); \
+    } while (0)
+
+int dev_alloc(mo_ed_ctx *ctx, DevBuf &b, size_t bytes);
+int ensure(mo_ed_ctx *ctx, DevBuf &b, size_t bytes);
+
+// ---- tables (tables.cu) ----------------------------------------------------
+long long binom(int n, int k);
+int build_model(mo_ed_ctx *ctx);
+int get_species(mo_ed_ctx *ctx, int N, Species **out);
+int get_sector(mo_ed_ctx *ctx, int ne_up, int ne_down, Sector *out);
+int basis_get_dev(mo_ed_ctx *ctx, const Sector &s, long long n, const long long *d_idx,
+                  unsigned *d_state);
+int basis_idx_dev(mo_ed_ctx *ctx, const Sector &s, long long n, const unsigned *d_state,
+                  long long *d_idx);
+
+// ---- H*v (hv.cu) ------------------------------------------------------------
+enum HvKind { HV_F64 = 0, HV_F32 = 1, HV_MIXED = 2 };
+// Fill a job for sector s (x, y device pointers).  nitems computed for kind.
+template <typename TA>
+void hv_fill_job(const mo_ed_ctx *ctx, const Sector &s, int kind, const void *x, void *y,
+                 HvJobT<TA> &job);
+// Launch H*v over a host list of jobs (item0 is assigned here); jobs are
+// passed to the kernel by value, so the call can be captured in a CUDA graph.
+int hv_launch_f32(mo_ed_ctx *ctx, const HvJobT<float> *jobs, int njobs);
+int hv_launch_f64(mo_ed_ctx *ctx, int kind, const HvJobT<double> *jobs, int njobs);
+int hv_rows_per_item(int kind);
+// Convenience: one vector, jobs staged through scratch.
+int hv_single(mo_ed_ctx *ctx, const Sector &s, int kind, const void *x, void *y);
+
+// ---- Krylov (krylov.cu) -----------------------------------------------------
+int lanczos_reference(mo_ed_ctx *ctx, const Sector &s, const double *h_vec, int nstep,
+                      int *nstep_calc, double *a, double *b);
+int diag_sector(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<double> &vals,
+                std::vector<DevBuf> *vecs);
+
+// ---- Green's function (green.cu) ---------------------------------------------
+int apply_c_dev(mo_ed_ctx *ctx, const Sector &in, const Sector &out, int prec, const void *x,
+                void *y, int pm, int iorb, int ispin);
+int calc_green(mo_ed_ctx *ctx, double *Gr);
+
+// ---- fit (fit.cu) ------------------------------------------------------------
+int chi2_grad_dev(mo_ed_ctx *ctx, int nbatch, const double *x, int nwloc, int ns, int nxsize,
+                  const double *omega, const double *dev, int nbath, int norb, double *f,
+                  double *g, int want_grad);
+
+}  // namespace moed

@@ -1,0 +1,888 @@
+// krylov.cu -- Lanczos on the device.
+//
+//  * lz_* : the reference three-term recurrence (ed_lanczos.F90:14-68) as
+//    batched kernels: update -> H*v (fused alpha partials) -> finalize, so
+//    that every excitation vector of the Green's function advances in the
+//    same three launches per step and no host round trip occurs.
+//  * diag_sector : replaces the PARPACK 'SA' solve of diag()
+//    (ed_solver.F90:107-191) by a thick-restart Lanczos with full
+//    reorthogonalisation (classical Gram-Schmidt, two passes), an FP64
+//    projected matrix and an FP64 parallel-Jacobi eigensolve in one CTA;
+//    eigenvalues are returned as FP64 Rayleigh quotients of the Ritz
+//    vectors (FP64-accumulated H*v for FP32 vectors).
+// All reductions are per-block partials summed in a fixed order (run-to-run
+// deterministic).  Per-element work of FP32 vectors stays in FP32; FP64 is
+// used once per 4-8 elements in the partial sums.
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+
+#include "krylov.cuh"
+
+namespace moed {
+
+constexpr int kVecThreads = 256;
+
+// ---------------------------------------------------------------------------
+// reductions
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v)
+{
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    return v;
+}
+
+// block-wide sum, result valid in thread 0
+__device__ double block_sum(double v, double *sred)
+{
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sred[wid] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sred[w];
+    return t;
+}
+
+template <typename TX, typename TY>
+__global__ void k_dot_part(const TX *__restrict__ x, const TY *__restrict__ y, long long n,
+                           double *part)
+{
+    __shared__ double sred[32];
+    double acc = 0.0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < n; i += 4 * stride) {
+        double p = (double)x[i] * (double)y[i];
+        if (sizeof(TX) == 4 && sizeof(TY) == 4) {
+            float q = (float)x[i] * (float)y[i] + (float)x[i + stride] * (float)y[i + stride] +
+                      (float)x[i + 2 * stride] * (float)y[i + 2 * stride] +
+                      (float)x[i + 3 * stride] * (float)y[i + 3 * stride];
+            acc += (double)q;
+        } else {
+            acc += p + (double)x[i + stride] * (double)y[i + stride] +
+                   (double)x[i + 2 * stride] * (double)y[i + 2 * stride] +
+                   (double)x[i + 3 * stride] * (double)y[i + 3 * stride];
+        }
+    }
+    for (; i < n; i += stride) acc += (double)x[i] * (double)y[i];
+    double t = block_sum(acc, sred);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+__global__ void k_sum_parts(const double *part, int n, double *out)
+{
+    __shared__ double sred[32];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) acc += part[i];
+    double t = block_sum(acc, sred);
+    if (threadIdx.x == 0) *out = t;
+}
+
+static int dot_grid(mo_ed_ctx *ctx, long long n)
+{
+    long long g = (n + kVecThreads * 4 - 1) / (kVecThreads * 4);
+    return (int)std::max(1LL, std::min(g, (long long)ctx->num_sms * 4));
+}
+
+int dot_dev(mo_ed_ctx *ctx, int prec_x, const void *x, int prec_y, const void *y, long long n,
+            double *d_out)
+{
+    const int g = dot_grid(ctx, n);
+    if (int rc = ensure(ctx, ctx->scratch_part, sizeof(double) * g)) return rc;
+    double *part = (double *)ctx->scratch_part.p;
+    if (prec_x == MO_ED_FP32 && prec_y == MO_ED_FP32)
+        k_dot_part<float, float><<<g, kVecThreads, 0, ctx->stream>>>((const float *)x, (const float *)y, n, part);
+    else if (prec_x == MO_ED_FP32)
+        k_dot_part<float, double><<<g, kVecThreads, 0, ctx->stream>>>((const float *)x, (const double *)y, n, part);
+    else if (prec_y == MO_ED_FP32)
+        k_dot_part<double, float><<<g, kVecThreads, 0, ctx->stream>>>((const double *)x, (const float *)y, n, part);
+    else
+        k_dot_part<double, double><<<g, kVecThreads, 0, ctx->stream>>>((const double *)x, (const double *)y, n, part);
+    MOED_CHECK_LAUNCH(ctx);
+    k_sum_parts<<<1, kVecThreads, 0, ctx->stream>>>(part, g, d_out);
+    MOED_CHECK_LAUNCH(ctx);
+    return MO_ED_OK;
+}
+
+template <typename TI, typename TO>
+__global__ void k_convert(const TI *__restrict__ in, TO *__restrict__ out, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        out[i] = (TO)in[i];
+}
+
+int convert_f64_to_f32(mo_ed_ctx *ctx, const double *in, float *out, long long n)
+{
+    if (n <= 0) return MO_ED_OK;
+    k_convert<double, float><<<dot_grid(ctx, n), kVecThreads, 0, ctx->stream>>>(in, out, n);
+    MOED_CHECK_LAUNCH(ctx);
+    return MO_ED_OK;
+}
+
+int convert_f32_to_f64(mo_ed_ctx *ctx, const float *in, double *out, long long n)
+{
+    if (n <= 0) return MO_ED_OK;
+    k_convert<float, double><<<dot_grid(ctx, n), kVecThreads, 0, ctx->stream>>>(in, out, n);
+    MOED_CHECK_LAUNCH(ctx);
+    return MO_ED_OK;
+}
+
+// ---------------------------------------------------------------------------
+// reference recurrence, batched
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int find_run_upd(const LzBatchDev &b, int item)
+{
+    int r = 0;
+    while (r + 1 < b.nrun && item >= b.run[r + 1].upd_item0) ++r;
+    return r;
+}
+
+// step j = 0: partial sums of ||u_0||^2
+template <typename T>
+__global__ void k_lz_norm0(const __grid_constant__ LzBatchDev b)
+{
+    __shared__ double sred[32];
+    for (int item = blockIdx.x; item < b.total_items; item += gridDim.x) {
+        const int r = find_run_upd(b, item);
+        const LzRunDev &R = b.run[r];
+        const int it = item - R.upd_item0;
+        const long long i0 = (long long)it * kVecChunk, i1 = min(R.D, i0 + kVecChunk);
+        const T *u = (const T *)R.u[0];
+        double acc = 0.0;
+        for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) acc += (double)u[i] * (double)u[i];
+        double t = block_sum(acc, sred);
+        if (threadIdx.x == 0) R.upd_part[it] = t;
+    }
+}
+
+// step j >= 1: u_j = s (w - a_{j-1} u_{j-1}) - c u_{j-2},  s = 1/sqrt(b_{j-1}),
+// c = sqrt(b_{j-1}/b_{j-2}) -- ed_lanczos.F90:38 (j = 1) and :54 (j >= 2)
+// with the reference's normalized vectors written as scaled stored ones.
+template <typename T>
+__global__ void k_lz_update(const __grid_constant__ LzBatchDev b, int j)
+{
+    __shared__ double sred[32];
+    for (int item = blockIdx.x; item < b.total_items; item += gridDim.x) {
+        const int r = find_run_upd(b, item);
+        const LzRunDev &R = b.run[r];
+        if (*R.active == 0) continue;
+        const int it = item - R.upd_item0;
+        const long long i0 = (long long)it * kVecChunk, i1 = min(R.D, i0 + kVecChunk);
+        const double nb1 = R.nrm[j - 1];
+        const T s = (T)(1.0 / sqrt(nb1));
+        const T a = (T)R.a[j - 1];
+        const T c = (j >= 2) ? (T)sqrt(nb1 / R.nrm[j - 2]) : T(0);
+        const T *w = (const T *)R.w;
+        const T *uc = (const T *)R.u[(j - 1) % 3];
+        const T *up = (const T *)R.u[(j + 1) % 3];   // (j-2) mod 3
+        T *un = (T *)R.u[j % 3];
+        double acc = 0.0;
+        if (j >= 2) {
+            for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+                T v = s * (w[i] - a * uc[i]) - c * up[i];
+                un[i] = v;
+                acc += (double)(v * v);
+            }
+        } else {
+            for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+                T v = s * (w[i] - a * uc[i]);
+                un[i] = v;
+                acc += (double)(v * v);
+            }
+        }
+        double t = block_sum(acc, sred);
+        if (threadIdx.x == 0) R.upd_part[it] = t;
+    }
+}
+
+// nrm_j and a_j from the partials; the reference's stop test b(j) < 1.e-12
+// (a default-REAL literal, ed_lanczos.F90:62) -- applied from j = 1 on.
+__global__ void k_lz_finalize(const __grid_constant__ LzBatchDev b, int j, int nstep)
+{
+    __shared__ double sred[32];
+    const LzRunDev &R = b.run[blockIdx.x];
+    if (*R.active == 0) return;
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < R.upd_nitems; i += blockDim.x) acc += R.upd_part[i];
+    const double nrm = block_sum(acc, sred);
+    acc = 0.0;
+    for (int i = threadIdx.x; i < R.hv_nitems; i += blockDim.x) acc += R.hv_part[i];
+    const double dot = block_sum(acc, sred);
+    if (threadIdx.x == 0) {
+        R.nrm[j] = nrm;
+        if (j == 0 && nrm == 0.0) {        // zero start vector: no contribution
+            R.a[0] = 0.0;
+            *R.nstep_calc = 0;
+            *R.active = 0;
+            return;
+        }
+        R.a[j] = dot / nrm;
+        const double tiny = (double)1.e-12f;
+        if (j >= 1 && nrm < tiny) {
+            *R.nstep_calc = j;
+            *R.active = 0;
+        } else if (j == nstep) {
+            *R.nstep_calc = nstep;
+            *R.active = 0;
+        }
+    }
+}
+
+void *lz_start_vector(LzBatch &b, int r) { return b.vecs[4 * r].p; }
+
+int lz_setup(mo_ed_ctx *ctx, LzBatch &b, const std::vector<Sector> &secs, int prec, int nstep)
+{
+    const int nrun = (int)secs.size();
+    if (nrun > kLzMaxRuns) return fail(ctx, MO_ED_ERR_ARG, "too many Lanczos runs in one batch");
+    b.prec = prec;
+    b.nstep = nstep;
+    b.sec = secs;
+    b.vecs.clear();
+    b.vecs.resize(4 * nrun);
+    const size_t es = prec == MO_ED_FP32 ? sizeof(float) : sizeof(double);
+    for (int r = 0; r < nrun; ++r)
+        for (int k = 0; k < 4; ++k)
+            if (int rc = dev_alloc(ctx, b.vecs[4 * r + k], es * (size_t)secs[r].D())) return rc;
+    if (int rc = dev_alloc(ctx, b.coef, sizeof(double) * 2 * (nstep + 1) * nrun)) return rc;
+    if (int rc = dev_alloc(ctx, b.flags, sizeof(int) * 2 * nrun)) return rc;
+    MOED_CUDA(ctx, cudaMemsetAsync(b.coef.p, 0, b.coef.bytes, ctx->stream));
+    std::vector<int> fl(2 * nrun);
+    for (int r = 0; r < nrun; ++r) {
+        fl[2 * r] = 1;
+        fl[2 * r + 1] = 0;
+    }
+    MOED_CUDA(ctx, cudaMemcpyAsync(b.flags.p, fl.data(), sizeof(int) * 2 * nrun,
+                                   cudaMemcpyHostToDevice, ctx->stream));
+    b.upd_item0.resize(nrun);
+    b.upd_nitems.resize(nrun);
+    b.hv_item0.resize(nrun);
+    b.hv_nitems.resize(nrun);
+    b.upd_total = b.hv_total = 0;
+    const int R = hv_rows_per_item(prec == MO_ED_FP32 ? HV_F32 : HV_F64);
+    for (int r = 0; r < nrun; ++r) {
+        b.upd_item0[r] = b.upd_total;
+        b.upd_nitems[r] = (int)((secs[r].D() + kVecChunk - 1) / kVecChunk);
+        b.upd_total += b.upd_nitems[r];
+        b.hv_item0[r] = b.hv_total;
+        b.hv_nitems[r] = (secs[r].dn->n + R - 1) / R;
+        b.hv_total += b.hv_nitems[r];
+    }
+    if (int rc = dev_alloc(ctx, b.upd_part, sizeof(double) * std::max(1, b.upd_total))) return rc;
+    if (int rc = dev_alloc(ctx, b.hv_part, sizeof(double) * std::max(1, b.hv_total))) return rc;
+    return MO_ED_OK;
+}
+
+static void lz_fill_dev(LzBatch &b, LzBatchDev &d)
+{
+    const int nrun = (int)b.sec.size();
+    memset(&d, 0, sizeof(d));
+    d.nrun = nrun;
+    d.total_items = b.upd_total;
+    double *coef = (double *)b.coef.p;
+    int *fl = (int *)b.flags.p;
+    for (int r = 0; r < nrun; ++r) {
+        LzRunDev &R = d.run[r];
+        for (int k = 0; k < 3; ++k) R.u[k] = b.vecs[4 * r + k].p;
+        R.w = b.vecs[4 * r + 3].p;
+        R.D = b.sec[r].D();
+        R.upd_item0 = b.upd_item0[r];
+        R.upd_nitems = b.upd_nitems[r];
+        R.hv_item0 = b.hv_item0[r];
+        R.hv_nitems = b.hv_nitems[r];
+        R.a = coef + (size_t)2 * (b.nstep + 1) * r;
+        R.nrm = R.a + (b.nstep + 1);
+        R.active = fl + 2 * r;
+        R.nstep_calc = fl + 2 * r + 1;
+        R.upd_part = (double *)b.upd_part.p + b.upd_item0[r];
+        R.hv_part = (double *)b.hv_part.p + b.hv_item0[r];
+    }
+}
+
+template <typename T>
+static int lz_steps(mo_ed_ctx *ctx, LzBatch &b, LzBatchDev &d)
+{
+    const int nrun = d.nrun;
+    const int kind = sizeof(T) == 4 ? HV_F32 : HV_F64;
+    std::vector<HvJobT<T>> jobs[3];
+    for (int k = 0; k < 3; ++k) {
+        jobs[k].resize(nrun);
+        for (int r = 0; r < nrun; ++r) {
+            hv_fill_job<T>(ctx, b.sec[r], kind, d.run[r].u[k], d.run[r].w, jobs[k][r]);
+            jobs[k][r].dot_partial = d.run[r].hv_part;
+            jobs[k][r].active = d.run[r].active;
+        }
+    }
+    const int gv = std::max(1, std::min(d.total_items, ctx->num_sms * 8));
+    for (int j = 0; j <= b.nstep; ++j) {
+        if (j == 0) {
+            k_lz_norm0<T><<<gv, kVecThreads, 0, ctx->stream>>>(d);
+        } else {
+            k_lz_update<T><<<gv, kVecThreads, 0, ctx->stream>>>(d, j);
+        }
+        MOED_CHECK_LAUNCH(ctx);
+        int rc = (sizeof(T) == 4) ? hv_launch_f32(ctx, (const HvJobT<float> *)jobs[j % 3].data(), nrun)
+                                  : hv_launch_f64(ctx, HV_F64, (const HvJobT<double> *)jobs[j % 3].data(), nrun);
+        if (rc) return rc;
+        k_lz_finalize<<<nrun, kVecThreads, 0, ctx->stream>>>(d, j, b.nstep);
+        MOED_CHECK_LAUNCH(ctx);
+    }
+    return MO_ED_OK;
+}
+
+int lz_run(mo_ed_ctx *ctx, LzBatch &b, std::vector<std::vector<double>> &a,
+           std::vector<std::vector<double>> &bb, std::vector<int> &nstep_calc)
+{
+    LzBatchDev d;
+    lz_fill_dev(b, d);
+    const int nrun = d.nrun;
+    int rc = (b.prec == MO_ED_FP32) ? lz_steps<float>(ctx, b, d) : lz_steps<double>(ctx, b, d);
+    if (rc) return rc;
+    std::vector<double> coef((size_t)2 * (b.nstep + 1) * nrun);
+    std::vector<int> fl(2 * nrun);
+    MOED_CUDA(ctx, cudaMemcpyAsync(coef.data(), b.coef.p, sizeof(double) * coef.size(),
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpyAsync(fl.data(), b.flags.p, sizeof(int) * fl.size(),
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+    MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    a.assign(nrun, std::vector<double>(b.nstep + 1, 0.0));
+    bb.assign(nrun, std::vector<double>(b.nstep + 1, 0.0));
+    nstep_calc.assign(nrun, 0);
+    for (int r = 0; r < nrun; ++r) {
+        const double *ar = coef.data() + (size_t)2 * (b.nstep + 1) * r;
+        const double *nr = ar + (b.nstep + 1);
+        nstep_calc[r] = fl[2 * r + 1];
+        for (int j = 0; j <= b.nstep; ++j) {
+            a[r][j] = ar[j];
+            bb[r][j] = (j == 0) ? 0.0 : nr[j];
+        }
+    }
+    return MO_ED_OK;
+}
+
+int lanczos_reference(mo_ed_ctx *ctx, const Sector &s, const double *h_vec, int nstep,
+                      int *nstep_calc, double *a, double *b)
+{
+    LzBatch lb;
+    const int prec = ctx->opt.precision;
+    if (int rc = lz_setup(ctx, lb, {s}, prec, nstep)) return rc;
+    const long long D = s.D();
+    if (prec == MO_ED_FP32) {
+        if (int rc = ensure(ctx, ctx->scratch_a, sizeof(double) * D)) return rc;
+        MOED_CUDA(ctx, cudaMemcpyAsync(ctx->scratch_a.p, h_vec, sizeof(double) * D,
+                                       cudaMemcpyHostToDevice, ctx->stream));
+        if (int rc = convert_f64_to_f32(ctx, (const double *)ctx->scratch_a.p,
+                                        (float *)lz_start_vector(lb, 0), D))
+            return rc;
+    } else {
+        MOED_CUDA(ctx, cudaMemcpyAsync(lz_start_vector(lb, 0), h_vec, sizeof(double) * D,
+                                       cudaMemcpyHostToDevice, ctx->stream));
+    }
+    std::vector<std::vector<double>> A, B;
+    std::vector<int> nc;
+    if (int rc = lz_run(ctx, lb, A, B, nc)) return rc;
+    *nstep_calc = nc[0];
+    for (int j = 0; j <= nstep; ++j) {
+        a[j] = A[0][j];
+        b[j] = B[0][j];
+    }
+    return MO_ED_OK;
+}
+
+// ---------------------------------------------------------------------------
+// thick-restart Lanczos with full reorthogonalisation (diag replacement)
+// ---------------------------------------------------------------------------
+constexpr int kMaxNcv = 200;
+constexpr int kMdTile = 2048;      // elements per multi-dot tile
+
+template <typename T>
+struct VPtrs {
+    const T *p[kMaxNcv + 1];
+};
+
+// part[b][l] = sum over block b's tiles of V_l . w
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads)
+k_multidot(const __grid_constant__ VPtrs<T> V, int nv, const T *__restrict__ w, long long D,
+           double *part)
+{
+    __shared__ T sw[kMdTile];
+    constexpr int kWarps = kVecThreads / 32;
+    constexpr int kPerWarp = (kMaxNcv + 1 + kWarps - 1) / kWarps;
+    double acc[kPerWarp];
+#pragma unroll
+    for (int i = 0; i < kPerWarp; ++i) acc[i] = 0.0;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const long long ntile = (D + kMdTile - 1) / kMdTile;
+    for (long long t = blockIdx.x; t < ntile; t += gridDim.x) {
+        const long long i0 = t * kMdTile;
+        const int len = (int)min((long long)kMdTile, D - i0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < len; i += kVecThreads) sw[i] = w[i0 + i];
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kPerWarp; ++k) {
+            const int l = wid + k * kWarps;
+            if (l < nv) {
+                const T *v = V.p[l] + i0;
+                T s = T(0);
+                double sd = 0.0;
+                int c = 0;
+                for (int i = lane; i < len; i += 32) {
+                    s += v[i] * sw[i];
+                    if (++c == 8) {
+                        sd += (double)s;
+                        s = T(0);
+                        c = 0;
+                    }
+                }
+                acc[k] += sd + (double)s;
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kPerWarp; ++k) {
+        const int l = wid + k * kWarps;
+        double v = warp_sum(acc[k]);
+        if (lane == 0 && l < nv) part[(size_t)blockIdx.x * nv + l] = v;
+    }
+}
+
+// out[l] = sum_b part[b][l]  (fixed order)
+__global__ void k_reduce_cols(const double *part, int G, int nv, double *out)
+{
+    for (int l = threadIdx.x; l < nv; l += blockDim.x) {
+        double s = 0.0;
+        for (int b = 0; b < G; ++b) s += part[(size_t)b * nv + l];
+        out[l] = s;
+    }
+}
+
+// w -= sum_l V_l h_l ; optional partial of ||w||^2
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads)
+k_multiaxpy(const __grid_constant__ VPtrs<T> V, int nv, const double *__restrict__ h, T *w,
+            long long D, double *norm_part)
+{
+    __shared__ T sh[kMaxNcv + 1];
+    __shared__ double sred[32];
+    for (int l = threadIdx.x; l < nv; l += blockDim.x) sh[l] = (T)h[l];
+    __syncthreads();
+    double acc = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < D;
+         i += (long long)gridDim.x * blockDim.x) {
+        T s = T(0);
+        for (int l = 0; l < nv; ++l) s += V.p[l][i] * sh[l];
+        T v = w[i] - s;
+        w[i] = v;
+        acc += (double)(v * v);
+    }
+    if (norm_part) {
+        double t = block_sum(acc, sred);
+        if (threadIdx.x == 0) norm_part[blockIdx.x] = t;
+    }
+}
+
+// column j of the projected matrix, beta, 1/beta
+__global__ void k_cgs_finish(const double *h1, const double *h2, int nv, const double *norm_part,
+                             int G, double *Hcol, double *beta_out)
+{
+    __shared__ double sred[32];
+    for (int l = threadIdx.x; l < nv; l += blockDim.x) Hcol[l] = h1[l] + h2[l];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < G; i += blockDim.x) acc += norm_part[i];
+    double t = block_sum(acc, sred);
+    if (threadIdx.x == 0) {
+        double beta = sqrt(t);
+        Hcol[nv] = beta;
+        beta_out[0] = beta;
+        beta_out[1] = beta > 0 ? 1.0 / beta : 0.0;
+    }
+}
+
+template <typename T>
+__global__ void k_scale_copy(const T *__restrict__ in, T *__restrict__ out, long long n,
+                             const double *scale)
+{
+    const T s = (T)*scale;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        out[i] = in[i] * s;
+}
+
+// deterministic pseudo-random start vector in [-1, 1)
+template <typename T>
+__global__ void k_random(T *x, long long n, unsigned long long seed)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        unsigned long long z = (unsigned long long)i + seed * 0x9E3779B97F4A7C15ull;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        x[i] = (T)((double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0);
+    }
+}
+
+// X_c = sum_l V_l Y[l][c] for c in [c0, c0+KC)
+template <typename T, int KC>
+__global__ void __launch_bounds__(kVecThreads)
+k_rotate(const __grid_constant__ VPtrs<T> V, int nv, const double *__restrict__ Y, int ldy, int c0,
+         int nc, const __grid_constant__ VPtrs<T> X, long long D)
+{
+    __shared__ double sy[kMaxNcv * KC];
+    for (int idx = threadIdx.x; idx < nv * KC; idx += blockDim.x) {
+        int l = idx / KC, c = idx - l * KC;
+        sy[idx] = (c < nc) ? Y[(size_t)(c0 + c) * ldy + l] : 0.0;
+    }
+    __syncthreads();
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < D;
+         i += (long long)gridDim.x * blockDim.x) {
+        double acc[KC];
+#pragma unroll
+        for (int c = 0; c < KC; ++c) acc[c] = 0.0;
+        for (int l = 0; l < nv; ++l) {
+            const double v = (double)V.p[l][i];
+#pragma unroll
+            for (int c = 0; c < KC; ++c) acc[c] += v * sy[l * KC + c];
+        }
+#pragma unroll
+        for (int c = 0; c < KC; ++c)
+            if (c < nc) const_cast<T *>(X.p[c])[i] = (T)acc[c];
+    }
+}
+
+// FP64 parallel (round-robin) two-sided Jacobi on the symmetrized projected
+// matrix.  M[i][j] (i <= j) = kept-block diag(theta) for j < kk, else the
+// computed column j (Hp[j*ldh + i]).  One CTA.  Outputs ascending eigenvalues
+// and the matching eigenvectors (column-major m x m).
+__global__ void k_jacobi(const double *__restrict__ Hp, int ldh, int m, int kk,
+                         const double *__restrict__ theta, double *A, double *V, double *evals,
+                         double *evecs, int max_sweeps)
+{
+    __shared__ double s_c[kMaxNcv / 2 + 1], s_s[kMaxNcv / 2 + 1];
+    __shared__ int s_p[kMaxNcv / 2 + 1], s_q[kMaxNcv / 2 + 1];
+    const int n = m + (m & 1);
+    const int half = n / 2;
+    for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+        const int i = idx % n, j = idx / n;
+        double v;
+        if (i >= m || j >= m) {
+            v = 0.0;
+        } else {
+            const int r = min(i, j), c = max(i, j);
+            if (c < kk) v = (r == c) ? theta[r] : 0.0;
+            else v = Hp[(size_t)c * ldh + r];
+        }
+        A[idx] = v;
+        V[idx] = (i == j) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    __shared__ int s_rot;
+    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+        // threshold Jacobi: a sweep that rotates nothing ends the iteration
+        if (threadIdx.x == 0) s_rot = 0;
+        __syncthreads();
+        for (int rnd = 0; rnd < n - 1; ++rnd) {
+            for (int k = threadIdx.x; k < half; k += blockDim.x) {
+                int p, q;
+                if (k == 0) {
+                    p = 0;
+                    q = (rnd % (n - 1)) + 1;
+                } else {
+                    p = ((rnd + k) % (n - 1)) + 1;
+                    q = ((rnd - k + (n - 1)) % (n - 1)) + 1;
+                }
+                const double apq = A[(size_t)q * n + p];
+                const double app = A[(size_t)p * n + p], aqq = A[(size_t)q * n + q];
+                double c = 1.0, s = 0.0;
+                if (fabs(apq) > 1e-17 * sqrt(fabs(app) * fabs(aqq)) + 1e-300) {
+                    atomicAdd(&s_rot, 1);
+                    const double tau = (aqq - app) / (2.0 * apq);
+                    const double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+                    c = 1.0 / sqrt(1.0 + t * t);
+                    s = t * c;
+                }
+                s_p[k] = p;
+                s_q[k] = q;
+                s_c[k] = c;
+                s_s[k] = s;
+            }
+            __syncthreads();
+            for (int idx = threadIdx.x; idx < half * n; idx += blockDim.x) {   // A <- A J
+                const int k = idx / n, r = idx - k * n;
+                const int p = s_p[k], q = s_q[k];
+                const double c = s_c[k], s = s_s[k];
+                const double arp = A[(size_t)p * n + r], arq = A[(size_t)q * n + r];
+                A[(size_t)p * n + r] = c * arp - s * arq;
+                A[(size_t)q * n + r] = s * arp + c * arq;
+            }
+            __syncthreads();
+            for (int idx = threadIdx.x; idx < half * n; idx += blockDim.x) {   // A <- J^T A
+                const int k = idx / n, col = idx - k * n;
+                const int p = s_p[k], q = s_q[k];
+                const double c = s_c[k], s = s_s[k];
+                const double apc = A[(size_t)col * n + p], aqc = A[(size_t)col * n + q];
+                A[(size_t)col * n + p] = c * apc - s * aqc;
+                A[(size_t)col * n + q] = s * apc + c * aqc;
+            }
+            for (int idx = threadIdx.x; idx < half * n; idx += blockDim.x) {   // V <- V J
+                const int k = idx / n, r = idx - k * n;
+                const int p = s_p[k], q = s_q[k];
+                const double c = s_c[k], s = s_s[k];
+                const double vrp = V[(size_t)p * n + r], vrq = V[(size_t)q * n + r];
+                V[(size_t)p * n + r] = c * vrp - s * vrq;
+                V[(size_t)q * n + r] = s * vrp + c * vrq;
+            }
+            __syncthreads();
+        }
+        if (s_rot == 0) break;
+        __syncthreads();
+    }
+    // sort ascending (pad index, if any, excluded)
+    __shared__ int order[kMaxNcv + 1];
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < m; ++i) order[i] = i;
+        for (int i = 1; i < m; ++i) {
+            int t = order[i];
+            double v = A[(size_t)t * n + t];
+            int k = i - 1;
+            while (k >= 0 && A[(size_t)order[k] * n + order[k]] > v) {
+                order[k + 1] = order[k];
+                --k;
+            }
+            order[k + 1] = t;
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < m; i += blockDim.x) evals[i] = A[(size_t)order[i] * n + order[i]];
+    for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) {
+        const int r = idx % m, c = idx / m;
+        evecs[idx] = V[(size_t)order[c] * n + r];
+    }
+}
+
+template <typename T>
+static VPtrs<T> make_ptrs(const std::vector<DevBuf *> &v, int n)
+{
+    VPtrs<T> p;
+    memset(&p, 0, sizeof(p));
+    for (int i = 0; i < n; ++i) p.p[i] = (const T *)v[i]->p;
+    return p;
+}
+
+template <typename T>
+static int orthogonalize(mo_ed_ctx *ctx, const std::vector<DevBuf *> &basis, int nv, T *w,
+                         long long D, double *h1, double *h2, double *part, double *norm_part,
+                         int G)
+{
+    VPtrs<T> P = make_ptrs<T>(basis, nv);
+    const int Gm = (int)std::max(1LL, std::min((D + kMdTile - 1) / kMdTile, (long long)ctx->num_sms * 2));
+    for (int pass = 0; pass < 2; ++pass) {
+        double *h = pass == 0 ? h1 : h2;
+        k_multidot<T><<<Gm, kVecThreads, 0, ctx->stream>>>(P, nv, w, D, part);
+        MOED_CHECK_LAUNCH(ctx);
+        k_reduce_cols<<<1, 256, 0, ctx->stream>>>(part, Gm, nv, h);
+        MOED_CHECK_LAUNCH(ctx);
+        k_multiaxpy<T><<<G, kVecThreads, 0, ctx->stream>>>(P, nv, h, w, D, pass == 1 ? norm_part : nullptr);
+        MOED_CHECK_LAUNCH(ctx);
+    }
+    return MO_ED_OK;
+}
+
+template <typename T>
+static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<double> &vals,
+                     std::vector<DevBuf> *vecs)
+{
+    const long long D = s.D();
+    const int prec = sizeof(T) == 4 ? MO_ED_FP32 : MO_ED_FP64;
+    const int kind = sizeof(T) == 4 ? HV_F32 : HV_F64;
+    const int nwant = (int)std::min<long long>(nev, D);
+    int ncv = ctx->opt.gs_ncv > 0 ? ctx->opt.gs_ncv : std::max(2 * nwant + 10, 40);
+    ncv = (int)std::min<long long>(std::min(ncv, kMaxNcv - 1), D);
+    if (ncv < nwant) return fail(ctx, MO_ED_ERR_ARG, "gs_ncv smaller than nev");
+    int kkeep = std::min(ncv - 1, nwant + (ncv - nwant) / 2);
+    if (kkeep < nwant) kkeep = nwant;
+    const double tol = ctx->opt.gs_tol > 0 ? ctx->opt.gs_tol : (prec == MO_ED_FP32 ? 2e-6 : 1e-11);
+    const size_t vb = sizeof(T) * (size_t)D;
+
+    std::vector<DevBuf> store(ncv + 2 + kkeep);
+    for (auto &b : store)
+        if (int rc = dev_alloc(ctx, b, vb)) return rc;
+    std::vector<DevBuf *> V(ncv + 1);
+    for (int i = 0; i <= ncv; ++i) V[i] = &store[i];
+    DevBuf *W = &store[ncv + 1];
+    std::vector<DevBuf *> spare(kkeep);
+    for (int i = 0; i < kkeep; ++i) spare[i] = &store[ncv + 2 + i];
+
+    const int G = (int)std::max(1LL, std::min((D + kVecThreads - 1) / kVecThreads, (long long)ctx->num_sms * 4));
+    const int n2 = ncv + 2;
+    DevBuf dHp, dh1, dh2, dpart, dnorm, dbeta, dA, dVj, devals, devecs, dtheta, dsc;
+    if (int rc = dev_alloc(ctx, dHp, sizeof(double) * (size_t)n2 * n2)) return rc;
+    if (int rc = dev_alloc(ctx, dh1, sizeof(double) * n2)) return rc;
+    if (int rc = dev_alloc(ctx, dh2, sizeof(double) * n2)) return rc;
+    if (int rc = dev_alloc(ctx, dpart, sizeof(double) * (size_t)n2 * ctx->num_sms * 2)) return rc;
+    if (int rc = dev_alloc(ctx, dnorm, sizeof(double) * G)) return rc;
+    if (int rc = dev_alloc(ctx, dbeta, sizeof(double) * 2)) return rc;
+    if (int rc = dev_alloc(ctx, dA, sizeof(double) * (size_t)n2 * n2)) return rc;
+    if (int rc = dev_alloc(ctx, dVj, sizeof(double) * (size_t)n2 * n2)) return rc;
+    if (int rc = dev_alloc(ctx, devals, sizeof(double) * n2)) return rc;
+    if (int rc = dev_alloc(ctx, devecs, sizeof(double) * (size_t)n2 * n2)) return rc;
+    if (int rc = dev_alloc(ctx, dtheta, sizeof(double) * n2)) return rc;
+    if (int rc = dev_alloc(ctx, dsc, sizeof(double) * 4)) return rc;
+    MOED_CUDA(ctx, cudaMemsetAsync(dHp.p, 0, dHp.bytes, ctx->stream));
+    double *Hp = (double *)dHp.p;
+    const int ldh = n2;
+
+    auto hv = [&](const void *x, void *y) -> int { return hv_single(ctx, s, kind, x, y); };
+    auto normalize_into = [&](T *src, DevBuf *dst) -> int {
+        // dst = src / ||src||
+        if (int rc = dot_dev(ctx, prec, src, prec, src, D, (double *)dsc.p)) return rc;
+        double nrm2;
+        MOED_CUDA(ctx, cudaMemcpyAsync(&nrm2, dsc.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        double inv = nrm2 > 0 ? 1.0 / std::sqrt(nrm2) : 0.0;
+        MOED_CUDA(ctx, cudaMemcpyAsync((double *)dsc.p + 1, &inv, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        k_scale_copy<T><<<G, kVecThreads, 0, ctx->stream>>>(src, (T *)dst->p, D, (double *)dsc.p + 1);
+        MOED_CHECK_LAUNCH(ctx);
+        return MO_ED_OK;
+    };
+
+    // start vector
+    unsigned long long seed = 0x5eedULL + 977ULL * (unsigned)s.ne_up + 131ULL * (unsigned)s.ne_down;
+    k_random<T><<<G, kVecThreads, 0, ctx->stream>>>((T *)W->p, D, seed);
+    MOED_CHECK_LAUNCH(ctx);
+    if (int rc = normalize_into((T *)W->p, V[0])) return rc;
+
+    int k = 0;           // kept Ritz vectors at the front of V
+    int m = ncv;
+    std::vector<double> theta(n2), ylast(n2), evecs_h;
+    bool done = false;
+    int cycle = 0;
+    double anorm = 0.0;
+    for (; cycle < ctx->opt.gs_maxcycles && !done; ++cycle) {
+        m = ncv;
+        for (int j = k; j < ncv; ++j) {
+            if (int rc = hv(V[j]->p, W->p)) return rc;
+            if (int rc = orthogonalize<T>(ctx, V, j + 1, (T *)W->p, D, (double *)dh1.p, (double *)dh2.p,
+                                          (double *)dpart.p, (double *)dnorm.p, G))
+                return rc;
+            k_cgs_finish<<<1, 256, 0, ctx->stream>>>((const double *)dh1.p, (const double *)dh2.p, j + 1,
+                                                     (const double *)dnorm.p, G, Hp + (size_t)j * ldh,
+                                                     (double *)dbeta.p);
+            MOED_CHECK_LAUNCH(ctx);
+            double beta[2], diag;
+            MOED_CUDA(ctx, cudaMemcpyAsync(beta, dbeta.p, sizeof(beta), cudaMemcpyDeviceToHost, ctx->stream));
+            MOED_CUDA(ctx, cudaMemcpyAsync(&diag, Hp + (size_t)j * ldh + j, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+            MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            anorm = std::max(anorm, std::fabs(diag) + beta[0]);
+            if (j + 1 >= D) {             // Krylov space is the whole sector
+                m = j + 1;
+                break;
+            }
+            const double bd = (prec == MO_ED_FP32 ? 1e-5 : 1e-12) * std::max(anorm, 1.0);
+            if (beta[0] <= bd) {
+                // invariant subspace: continue from a fresh random direction
+                double zero = 0.0;
+                MOED_CUDA(ctx, cudaMemcpyAsync(Hp + (size_t)j * ldh + j + 1, &zero, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+                k_random<T><<<G, kVecThreads, 0, ctx->stream>>>((T *)W->p, D, seed + 7919ULL * (cycle * kMaxNcv + j + 1));
+                MOED_CHECK_LAUNCH(ctx);
+                if (int rc = orthogonalize<T>(ctx, V, j + 1, (T *)W->p, D, (double *)dh1.p, (double *)dh2.p,
+                                              (double *)dpart.p, (double *)dnorm.p, G))
+                    return rc;
+                if (int rc = normalize_into((T *)W->p, V[j + 1])) return rc;
+            } else {
+                k_scale_copy<T><<<G, kVecThreads, 0, ctx->stream>>>((const T *)W->p, (T *)V[j + 1]->p, D,
+                                                                    (double *)dbeta.p + 1);
+                MOED_CHECK_LAUNCH(ctx);
+            }
+        }
+        // Rayleigh-Ritz on span V[0..m-1]
+        MOED_CUDA(ctx, cudaMemcpyAsync(dtheta.p, theta.data(), sizeof(double) * std::max(k, 1),
+                                       cudaMemcpyHostToDevice, ctx->stream));
+        k_jacobi<<<1, 256, 0, ctx->stream>>>(Hp, ldh, m, k, (const double *)dtheta.p, (double *)dA.p,
+                                             (double *)dVj.p, (double *)devals.p, (double *)devecs.p, 60);
+        MOED_CHECK_LAUNCH(ctx);
+        evecs_h.resize((size_t)m * m);
+        double beta_m = 0.0;
+        MOED_CUDA(ctx, cudaMemcpyAsync(theta.data(), devals.p, sizeof(double) * m, cudaMemcpyDeviceToHost, ctx->stream));
+        MOED_CUDA(ctx, cudaMemcpyAsync(evecs_h.data(), devecs.p, sizeof(double) * (size_t)m * m, cudaMemcpyDeviceToHost, ctx->stream));
+        if (m < D)
+            MOED_CUDA(ctx, cudaMemcpyAsync(&beta_m, Hp + (size_t)(m - 1) * ldh + m, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        int nconv = 0;
+        for (int i = 0; i < nwant; ++i) {
+            double res = std::fabs(beta_m * evecs_h[(size_t)i * m + (m - 1)]);
+            if (res <= tol * std::max(anorm, 1.0)) ++nconv;
+            else break;
+        }
+        if (nconv >= nwant || m >= D) {
+            done = true;
+            break;
+        }
+        // thick restart: keep kkeep lowest Ritz vectors, then the residual vector
+        const int kk = std::min(kkeep, m - 1);
+        VPtrs<T> P = make_ptrs<T>(V, m);
+        for (int c0 = 0; c0 < kk; c0 += 8) {
+            const int nc = std::min(8, kk - c0);
+            std::vector<DevBuf *> outs(spare.begin() + c0, spare.begin() + c0 + nc);
+            VPtrs<T> X = make_ptrs<T>(outs, nc);
+            k_rotate<T, 8><<<G, kVecThreads, 0, ctx->stream>>>(P, m, (const double *)devecs.p, m, c0, nc, X, D);
+            MOED_CHECK_LAUNCH(ctx);
+        }
+        for (int i = 0; i < kk; ++i) std::swap(V[i], spare[i]);
+        std::swap(V[kk], V[m]);
+        k = kk;
+        MOED_CUDA(ctx, cudaMemsetAsync(dHp.p, 0, dHp.bytes, ctx->stream));
+    }
+    if (!done) return fail(ctx, MO_ED_ERR_NOCONV, "eigensolver did not converge");
+
+    // Ritz vectors and FP64 Rayleigh quotients
+    vals.assign(nev, DBL_MAX);
+    const int nout = nwant;
+    std::vector<DevBuf> X(nout);
+    for (auto &b : X)
+        if (int rc = dev_alloc(ctx, b, vb)) return rc;
+    {
+        VPtrs<T> P = make_ptrs<T>(V, m);
+        for (int c0 = 0; c0 < nout; c0 += 8) {
+            const int nc = std::min(8, nout - c0);
+            std::vector<DevBuf *> outs;
+            for (int c = 0; c < nc; ++c) outs.push_back(&X[c0 + c]);
+            VPtrs<T> Xp = make_ptrs<T>(outs, nc);
+            k_rotate<T, 8><<<G, kVecThreads, 0, ctx->stream>>>(P, m, (const double *)devecs.p, m, c0, nc, Xp, D);
+            MOED_CHECK_LAUNCH(ctx);
+        }
+    }
+    DevBuf Y;
+    if (int rc = dev_alloc(ctx, Y, sizeof(double) * (size_t)D)) return rc;
+    for (int i = 0; i < nout; ++i) {
+        const int hk = prec == MO_ED_FP32 ? HV_MIXED : HV_F64;
+        if (int rc = hv_single(ctx, s, hk, X[i].p, Y.p)) return rc;
+        if (int rc = dot_dev(ctx, prec, X[i].p, MO_ED_FP64, Y.p, D, (double *)dsc.p)) return rc;
+        if (int rc = dot_dev(ctx, prec, X[i].p, prec, X[i].p, D, (double *)dsc.p + 1)) return rc;
+        double r[2];
+        MOED_CUDA(ctx, cudaMemcpyAsync(r, dsc.p, sizeof(r), cudaMemcpyDeviceToHost, ctx->stream));
+        MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        vals[i] = r[0] / r[1];
+    }
+    if (vecs) {
+        vecs->clear();
+        vecs->resize(nout);
+        for (int i = 0; i < nout; ++i) std::swap((*vecs)[i], X[i]);
+    }
+    return MO_ED_OK;
+}
+
+int diag_sector(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<double> &vals,
+                std::vector<DevBuf> *vecs)
+{
+    if (ctx->opt.precision == MO_ED_FP32) return trl_solve<float>(ctx, s, nev, vals, vecs);
+    return trl_solve<double>(ctx, s, nev, vals, vecs);
+}
+
+}  // namespace moed

@@ -1,0 +1,376 @@
+// tables.cu -- sector basis and operator tables, built on the device.
+//
+// Replaces generate_basis / ed_basis_get / ed_basis_idx (ed_basis.F90:35-139)
+// and the per-row operator bit loops of ed_operators.F90:63-348.
+//
+// The reference enumerates all words in [minrange, maxrange] and keeps those
+// with popcount N in ascending integer order (ed_basis.F90:69-105).  Ascending
+// order of N-subsets of bit positions is colexicographic order, so the
+// 0-based rank of a word with set bits p_1 < ... < p_N is sum_i C(p_i, i)
+// (combinatorial number system) and a rank is unranked greedily from the top
+// bit.  Both directions are one thread per element here.
+#include <algorithm>
+#include <cstring>
+
+#include "internal.h"
+
+namespace moed {
+
+__constant__ int c_binom[kMaxSite + 1][kMaxSite + 2];
+
+long long binom(int n, int k)
+{
+    if (k < 0 || n < 0 || k > n) return 0;
+    long long r = 1;
+    for (int i = 1; i <= k; ++i) r = r * (n - k + i) / i;
+    return r;
+}
+
+static int upload_binom(mo_ed_ctx *ctx)
+{
+    static int h[kMaxSite + 1][kMaxSite + 2];
+    for (int n = 0; n <= kMaxSite; ++n)
+        for (int k = 0; k <= kMaxSite + 1; ++k) h[n][k] = (int)binom(n, k);
+    MOED_CUDA(ctx, cudaMemcpyToSymbolAsync(c_binom, h, sizeof(h), 0, cudaMemcpyHostToDevice,
+                                           ctx->stream));
+    MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return MO_ED_OK;
+}
+
+Species::~Species()
+{
+    cudaFree(words);
+    cudaFree(rank);
+    cudaFree(hop_cnt);
+    cudaFree(hop_tgt);
+    cudaFree(hop_val_d);
+    cudaFree(hop_val_f);
+    cudaFree(diag_d);
+    cudaFree(diag_f);
+}
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int parity_below(unsigned w, int bit)
+{
+    return __popc(w & ((1u << bit) - 1u)) & 1;
+}
+
+// colex unrank: rank r -> word with N bits among nsite
+__global__ void k_unrank(int nsite, int N, int n, int *words)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    int k = N, rem = r;
+    unsigned w = 0;
+    for (int p = nsite - 1; p >= 0 && k > 0; --p) {
+        int c = c_binom[p][k];
+        if (rem >= c) {
+            w |= 1u << p;
+            rem -= c;
+            --k;
+        }
+    }
+    words[r] = (int)w;
+}
+
+// colex rank over all 2^nsite words (-1 outside the species)
+__global__ void k_rank(int nsite, int N, int *rank)
+{
+    int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= (1 << nsite)) return;
+    if (__popc(w) != N) {
+        rank[w] = -1;
+        return;
+    }
+    int r = 0, i = 1;
+    for (int p = 0; p < nsite; ++p)
+        if ((w >> p) & 1) r += c_binom[p][i++];
+    rank[w] = r;
+}
+
+struct CplList {
+    int n;
+    int orb[kMaxHop];   // impurity bit (0-based orbital)
+    int bath[kMaxHop];  // bath bit (norb + ibath - 1)
+    double val[kMaxHop];
+};
+
+// Hybridisation moves of one species word, compacted, in the reference's loop
+// order (iorb outer, ibath inner; hybridization1 then hybridization2,
+// ed_hamiltonian.F90:146-161).  Signs: product of the destruction / creation
+// signs (parity of occupied bits below the target bit), ed_operators.F90:292-348.
+// For the down species the reference also counts all up-spin bits below; that
+// parity appears once in each of the two operators and cancels.
+__global__ void k_hops(int n, CplList cpl, const int *words, const int *rank, int *cnt, int *tgt,
+                       double *vd, float *vf, int *max_cnt)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    unsigned w = (unsigned)words[r];
+    int c = 0;
+    for (int i = 0; i < cpl.n; ++i) {
+        int o = cpl.orb[i], k = cpl.bath[i];
+        int ob = (w >> o) & 1, kb = (w >> k) & 1;
+        int src, dst;
+        if (kb && !ob) {          // hybridization1: c_k then c+_o
+            src = k;
+            dst = o;
+        } else if (ob && !kb) {   // hybridization2: c_o then c+_k
+            src = o;
+            dst = k;
+        } else {
+            continue;
+        }
+        int s1 = parity_below(w, src);
+        unsigned w1 = w & ~(1u << src);
+        int s2 = parity_below(w1, dst);
+        unsigned w2 = w1 | (1u << dst);
+        double v = cpl.val[i] * (((s1 ^ s2) & 1) ? -1.0 : 1.0);
+        tgt[(size_t)c * n + r] = rank[w2];
+        vd[(size_t)c * n + r] = v;
+        vf[(size_t)c * n + r] = (float)v;
+        ++c;
+    }
+    for (int i = c; i < cpl.n; ++i) {
+        tgt[(size_t)i * n + r] = r;   // padding: harmless in-range target
+        vd[(size_t)i * n + r] = 0.0;
+        vf[(size_t)i * n + r] = 0.0f;
+    }
+    cnt[r] = c;
+    atomicMax(max_cnt, c);
+}
+
+// Species part of the diagonal: sum_site ek(site) n_site (onsite,
+// ed_operators.F90:68-84) + (U-3J) sum_{i<j} n_i n_j over impurity orbitals
+// (same-spin dens_dens, ed_operators.F90:157-159).
+__global__ void k_species_diag(int n, int nsite, int norb, const int *words, const double *ek,
+                               double Usame, double *dd, float *df)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    unsigned w = (unsigned)words[r];
+    double s = 0.0;
+    for (int i = 0; i < nsite; ++i)
+        if ((w >> i) & 1) s += ek[i];
+    for (int i = 0; i < norb; ++i)
+        for (int j = i + 1; j < norb; ++j)
+            if (((w >> i) & 1) && ((w >> j) & 1)) s += Usame;
+    dd[r] = s;
+    df[r] = (float)s;
+}
+
+__global__ void k_basis_get(long long n, const long long *idx, unsigned *state, const int *up,
+                            const int *dn, int nu, int nsite)
+{
+    long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    long long i = idx[t] - 1;
+    long long iu = i % nu, id = i / nu;
+    state[t] = (unsigned)up[iu] + (1u << nsite) * (unsigned)dn[id];
+}
+
+__global__ void k_basis_idx(long long n, const unsigned *state, long long *idx, const int *rank_up,
+                            const int *rank_dn, int nu, int nsite)
+{
+    long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    unsigned s = state[t];
+    unsigned su = s & ((1u << nsite) - 1u), sd = s >> nsite;
+    int ru = (sd >> nsite) ? -1 : rank_up[su];
+    int rd = (sd >> nsite) ? -1 : rank_dn[sd];
+    idx[t] = (ru < 0 || rd < 0) ? 0 : (long long)rd * nu + ru + 1;
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static int imp_pos(int I, int norb)
+{
+    // rank of impurity pattern I among norb-bit patterns of equal popcount
+    int pc = __builtin_popcount(I), pos = 0;
+    for (int J = 0; J < I; ++J)
+        if (__builtin_popcount(J) == pc) ++pos;
+    (void)norb;
+    return pos;
+}
+
+int build_model(mo_ed_ctx *ctx)
+{
+    ModelDev &m = ctx->mdl;
+    memset(&m, 0, sizeof(m));
+    const int norb = ctx->norb, nbath = ctx->nbath;
+    m.norb = norb;
+    m.nbath = nbath;
+    m.nsite = norb + nbath;
+    m.nimp = 1 << norb;
+    m.npair = norb * (norb - 1);
+    m.U = ctx->U;
+    m.J = ctx->J;
+
+    // nonzero couplings in the reference loop order (iorb outer, ibath inner)
+    ctx->cpl_orb.clear();
+    ctx->cpl_bath.clear();
+    ctx->cpl_val.clear();
+    for (int io = 0; io < norb; ++io)
+        for (int ib = 0; ib < nbath; ++ib) {
+            double v = ctx->vk[(size_t)ib * norb + io];
+            if (v != 0.0) {
+                ctx->cpl_orb.push_back(io);
+                ctx->cpl_bath.push_back(norb + ib);
+                ctx->cpl_val.push_back(v);
+            }
+        }
+    m.ncpl = (int)ctx->cpl_val.size();
+    if (m.ncpl > kMaxHop) return fail(ctx, MO_ED_ERR_ARG, "too many nonzero couplings");
+
+    // ordered pairs (i,j), i != j, in the reference's (iorb, jorb) loop order
+    int pidx[kMaxOrb][kMaxOrb];
+    int p = 0;
+    for (int i = 0; i < norb; ++i)
+        for (int j = 0; j < norb; ++j)
+            if (i != j) pidx[i][j] = p++;
+    for (int i = 0; i < norb; ++i)
+        for (int j = 0; j < norb; ++j)
+            if (i != j) {
+                int pp = pidx[i][j];
+                m.pair_rev[pp] = pidx[j][i];
+                for (int I = 0; I < m.nimp; ++I) {
+                    int e = 0;
+                    if (((I >> j) & 1) && !((I >> i) & 1)) {
+                        int s1 = __builtin_popcount(I & ((1 << j) - 1)) & 1;
+                        int I1 = I & ~(1 << j);
+                        int s2 = __builtin_popcount(I1 & ((1 << i) - 1)) & 1;
+                        int I2 = I1 | (1 << i);
+                        int delta = imp_pos(I2, norb) - imp_pos(I, norb);
+                        e = (int)(0x80000000u | ((s1 ^ s2) ? 0x40000000u : 0u) | (unsigned)(delta & 0xffff));
+                    }
+                    m.t4[pp * m.nimp + I] = e;
+                }
+            }
+    // interspecies diagonal: U n_i^up n_i^dn (ed_operators.F90:148-156) and
+    // (U-2J) n_i^sigma n_j^-sigma, i != j (ed_operators.F90:160-162)
+    for (int Iu = 0; Iu < m.nimp; ++Iu)
+        for (int Id = 0; Id < m.nimp; ++Id) {
+            double s = 0.0;
+            for (int i = 0; i < norb; ++i)
+                if (((Iu >> i) & 1) && ((Id >> i) & 1)) s += ctx->U;
+            for (int i = 0; i < norb; ++i)
+                for (int j = 0; j < norb; ++j)
+                    if (i != j && ((Iu >> i) & 1) && ((Id >> j) & 1)) s += ctx->U - 2 * ctx->J;
+            m.cross[Iu * m.nimp + Id] = s;
+        }
+    if (!ctx->d_mdl) MOED_CUDA(ctx, cudaMalloc(&ctx->d_mdl, sizeof(ModelDev)));
+    MOED_CUDA(ctx, cudaMemcpyAsync(ctx->d_mdl, &m, sizeof(m), cudaMemcpyHostToDevice, ctx->stream));
+    MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->species.clear();
+    return upload_binom(ctx);
+}
+
+int get_species(mo_ed_ctx *ctx, int N, Species **out)
+{
+    auto it = ctx->species.find(N);
+    if (it != ctx->species.end()) {
+        *out = it->second.get();
+        return MO_ED_OK;
+    }
+    const int nsite = ctx->nsite;
+    std::unique_ptr<Species> s(new Species);
+    s->nsite = nsite;
+    s->N = N;
+    s->n = (int)binom(nsite, N);
+    s->hw = std::max(ctx->mdl.ncpl, 1);
+    const int n = s->n;
+    const size_t nh = (size_t)n * s->hw;
+    MOED_CUDA(ctx, cudaMalloc(&s->words, sizeof(int) * n));
+    MOED_CUDA(ctx, cudaMalloc(&s->rank, sizeof(int) << nsite));
+    MOED_CUDA(ctx, cudaMalloc(&s->hop_cnt, sizeof(int) * n));
+    MOED_CUDA(ctx, cudaMalloc(&s->hop_tgt, sizeof(int) * nh));
+    MOED_CUDA(ctx, cudaMalloc(&s->hop_val_d, sizeof(double) * nh));
+    MOED_CUDA(ctx, cudaMalloc(&s->hop_val_f, sizeof(float) * nh));
+    MOED_CUDA(ctx, cudaMalloc(&s->diag_d, sizeof(double) * n));
+    MOED_CUDA(ctx, cudaMalloc(&s->diag_f, sizeof(float) * n));
+
+    const int T = 256;
+    k_unrank<<<(n + T - 1) / T, T, 0, ctx->stream>>>(nsite, N, n, s->words);
+    MOED_CHECK_LAUNCH(ctx);
+    k_rank<<<((1 << nsite) + T - 1) / T, T, 0, ctx->stream>>>(nsite, N, s->rank);
+    MOED_CHECK_LAUNCH(ctx);
+
+    CplList cl;
+    memset(&cl, 0, sizeof(cl));
+    cl.n = ctx->mdl.ncpl;
+    for (int i = 0; i < cl.n; ++i) {
+        cl.orb[i] = ctx->cpl_orb[i];
+        cl.bath[i] = ctx->cpl_bath[i];
+        cl.val[i] = ctx->cpl_val[i];
+    }
+    DevBuf dmax, dek;
+    if (int rc = dev_alloc(ctx, dmax, sizeof(int))) return rc;
+    if (int rc = dev_alloc(ctx, dek, sizeof(double) * nsite)) return rc;
+    MOED_CUDA(ctx, cudaMemsetAsync(dmax.p, 0, sizeof(int), ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpyAsync(dek.p, ctx->ek.data(), sizeof(double) * nsite,
+                                   cudaMemcpyHostToDevice, ctx->stream));
+    if (cl.n > 0) {
+        k_hops<<<(n + T - 1) / T, T, 0, ctx->stream>>>(n, cl, s->words, s->rank, s->hop_cnt,
+                                                       s->hop_tgt, s->hop_val_d, s->hop_val_f,
+                                                       (int *)dmax.p);
+        MOED_CHECK_LAUNCH(ctx);
+    } else {
+        MOED_CUDA(ctx, cudaMemsetAsync(s->hop_cnt, 0, sizeof(int) * n, ctx->stream));
+        MOED_CUDA(ctx, cudaMemsetAsync(s->hop_tgt, 0, sizeof(int) * nh, ctx->stream));
+        MOED_CUDA(ctx, cudaMemsetAsync(s->hop_val_d, 0, sizeof(double) * nh, ctx->stream));
+        MOED_CUDA(ctx, cudaMemsetAsync(s->hop_val_f, 0, sizeof(float) * nh, ctx->stream));
+    }
+    k_species_diag<<<(n + T - 1) / T, T, 0, ctx->stream>>>(n, nsite, ctx->norb, s->words,
+                                                           (const double *)dek.p,
+                                                           ctx->U - 3 * ctx->J, s->diag_d,
+                                                           s->diag_f);
+    MOED_CHECK_LAUNCH(ctx);
+    MOED_CUDA(ctx, cudaMemcpyAsync(&s->max_cnt, dmax.p, sizeof(int), cudaMemcpyDeviceToHost,
+                                   ctx->stream));
+    MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    *out = s.get();
+    ctx->species[N] = std::move(s);
+    return MO_ED_OK;
+}
+
+int get_sector(mo_ed_ctx *ctx, int ne_up, int ne_down, Sector *out)
+{
+    if (!ctx->have_model) return fail(ctx, MO_ED_ERR_STATE, "model not set");
+    if (ne_up < 0 || ne_up > ctx->nsite || ne_down < 0 || ne_down > ctx->nsite)
+        return fail(ctx, MO_ED_ERR_SECTOR, "sector (" + std::to_string(ne_up) + "," +
+                                               std::to_string(ne_down) + ") out of range");
+    out->ne_up = ne_up;
+    out->ne_down = ne_down;
+    if (int rc = get_species(ctx, ne_up, &out->up)) return rc;
+    if (int rc = get_species(ctx, ne_down, &out->dn)) return rc;
+    return MO_ED_OK;
+}
+
+int basis_get_dev(mo_ed_ctx *ctx, const Sector &s, long long n, const long long *d_idx,
+                  unsigned *d_state)
+{
+    if (n <= 0) return MO_ED_OK;
+    const int T = 256;
+    k_basis_get<<<(unsigned)((n + T - 1) / T), T, 0, ctx->stream>>>(n, d_idx, d_state, s.up->words,
+                                                                     s.dn->words, s.up->n,
+                                                                     ctx->nsite);
+    MOED_CHECK_LAUNCH(ctx);
+    return MO_ED_OK;
+}
+
+int basis_idx_dev(mo_ed_ctx *ctx, const Sector &s, long long n, const unsigned *d_state,
+                  long long *d_idx)
+{
+    if (n <= 0) return MO_ED_OK;
+    const int T = 256;
+    k_basis_idx<<<(unsigned)((n + T - 1) / T), T, 0, ctx->stream>>>(n, d_state, d_idx, s.up->rank,
+                                                                     s.dn->rank, s.up->n,
+                                                                     ctx->nsite);
+    MOED_CHECK_LAUNCH(ctx);
+    return MO_ED_OK;
+}
+
+}  // namespace moed

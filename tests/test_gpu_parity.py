@@ -1,0 +1,302 @@
+"""GPU parity tests: CUDA path through the C-ABI vs the CPU oracle.
+
+Tolerances (stated per test):
+  * basis words, ranks, rows, apply_c signs / values: bit-exact;
+  * FP64 H*v: 1e-13 relative (max-norm) -- summation order only;
+  * FP32 H*v: 2e-6 relative (max-norm) on FP32-rounded input;
+  * FP32-in / FP64-accumulated H*v: 1e-13 relative on the same FP32 input;
+  * FP64 Lanczos coefficients: 1e-9 relative over the first 12 steps (later
+    steps amplify rounding after loss of orthogonality in both codes);
+  * FP64 eigenvalues: 1e-9 absolute; FP32-mixed eigenvalues: 1e-8 absolute;
+  * G(i w_n): FP64 1e-8, FP32-mixed 1e-5, relative to max |G|;
+  * chi^2 / gradient: 1e-12 relative.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.abs(np.asarray(a) - np.asarray(b)).max() / max(1e-300, np.abs(np.asarray(b)).max())
+
+
+MODELS = {
+    # name: (norb, nbath, U, J, dense V)
+    "1x4": (1, 4, 2.0, 0.0, True),
+    "2x6_block": (2, 6, 4.0, 1.0, False),
+    "2x3_dense": (2, 3, 3.1, 0.7, True),
+    "3x3_dense": (3, 3, 3.0, 0.5, True),
+    "3x6_block": (3, 6, 3.0, 0.5, False),
+    "4x4_mixed": (4, 4, 2.5, 0.4, None),
+    "5x2_dense": (5, 2, 2.0, 0.3, True),
+}
+
+
+def make_model(name, seed=0):
+    norb, nbath, U, J, dense = MODELS[name]
+    rng = np.random.default_rng(seed + 17 * norb + nbath)
+    ek = np.concatenate([rng.uniform(-2, 0, norb), rng.uniform(-1, 1, nbath)])
+    vk = rng.uniform(0.1, 0.6, (norb, nbath))
+    if dense is False:
+        per = nbath // norb
+        mask = np.zeros_like(vk)
+        for a in range(norb):
+            mask[a, a * per:(a + 1) * per] = 1
+        vk *= mask
+    elif dense is None:
+        vk[rng.random(vk.shape) < 0.4] = 0.0
+    return norb, nbath, U, J, ek, vk
+
+
+@pytest.fixture
+def setup(solver, oracle):
+    def f(name, seed=0, precision="fp64", **opt):
+        norb, nbath, U, J, ek, vk = make_model(name, seed)
+        solver.set_options(precision=precision, **opt)
+        solver.set_model(norb, nbath, U, J, ek, vk)
+        return solver, oracle.Model(norb, nbath, U, J, ek, vk)
+    return f
+
+
+# ---------------------------------------------------------------- basis
+@pytest.mark.parametrize("norb,nbath", [(1, 4), (2, 6), (3, 9), (3, 12)])
+def test_generate_basis_bitexact(solver, oracle, norb, nbath):
+    ns = norb + nbath
+    solver.set_model(norb, nbath, 1.0, 0.1, np.zeros(ns), np.full((norb, nbath), 0.2))
+    for ne in sorted({0, 1, ns // 2, (ns + 1) // 2, ns - 1, ns}):
+        ne2 = ns - ne
+        g = solver.generate_basis(ne, ne2)
+        b = oracle.Basis(ns, ne, ne2)
+        assert g["nup"] == b.nup and g["ndown"] == b.ndown
+        assert np.array_equal(g["up"], b.up) and np.array_equal(g["down"], b.down)
+        assert np.array_equal(g["idx_up"], b.idx_up) and np.array_equal(g["idx_down"], b.idx_down)
+
+
+def test_basis_get_idx_bitexact(solver, oracle):
+    ns = 12
+    solver.set_model(3, 9, 1.0, 0.1, np.zeros(ns), np.full((3, 9), 0.2))
+    b = oracle.Basis(ns, 6, 5)
+    rng = np.random.default_rng(0)
+    rows = rng.integers(1, b.ntot + 1, 5000)
+    st = solver.ed_basis_get(6, 5, rows)
+    assert np.array_equal(st, [b.get(int(i)) for i in rows])
+    assert np.array_equal(solver.ed_basis_idx(6, 5, st), rows)
+    # a word outside the sector maps to 0
+    assert solver.ed_basis_idx(6, 5, np.array([0], np.uint32))[0] == 0
+
+
+# ---------------------------------------------------------------- H*v
+def sectors_of(ns):
+    out = {(ns // 2, (ns + 1) // 2), (1, 0), (0, ns), (ns, ns - 1), (ns // 2, ns // 2), (2, ns - 3)}
+    return sorted(s for s in out if 0 <= s[0] <= ns and 0 <= s[1] <= ns)
+
+
+@pytest.mark.parametrize("name", list(MODELS))
+def test_multiply_h_fp64(setup, oracle, name):
+    s, m = setup(name)
+    ns = m.nsite
+    rng = np.random.default_rng(1)
+    for nu, nd in sectors_of(ns):
+        b = oracle.Basis(ns, nu, nd)
+        x = rng.standard_normal(b.ntot)
+        y = s.multiply_H(nu, nd, x)
+        assert rel(y, oracle.multiply_H(m, b, x)) < 1e-13, (name, nu, nd)
+
+
+@pytest.mark.parametrize("name", ["1x4", "2x6_block", "3x6_block", "4x4_mixed", "5x2_dense"])
+def test_multiply_h_fp32(setup, oracle, name):
+    s, m = setup(name, precision="fp32")
+    ns = m.nsite
+    rng = np.random.default_rng(2)
+    for nu, nd in sectors_of(ns):
+        b = oracle.Basis(ns, nu, nd)
+        x = rng.standard_normal(b.ntot).astype(np.float32)
+        y = s.multiply_H(nu, nd, x)
+        assert y.dtype == np.float32
+        assert rel(y, oracle.multiply_H(m, b, x.astype(np.float64))) < 2e-6, (name, nu, nd)
+
+
+def test_multiply_h_mixed(setup, oracle):
+    import torch
+    s, m = setup("3x6_block")
+    nu, nd = 4, 5
+    b = oracle.Basis(m.nsite, nu, nd)
+    x = np.random.default_rng(3).standard_normal(b.ntot).astype(np.float32)
+    dx = torch.from_numpy(x).cuda()
+    dy = torch.empty(b.ntot, dtype=torch.float64, device="cuda")
+    s.multiply_H_mixed_dev(nu, nd, dx.data_ptr(), dy.data_ptr())
+    torch.cuda.synchronize()
+    assert rel(dy.cpu().numpy(), oracle.multiply_H(m, b, x.astype(np.float64))) < 1e-13
+
+
+def test_multiply_h_symmetric_c3(setup, oracle):
+    """Full C3 sector (D = 853,776): <x|H y> = <y|H x> and FP32 vs FP64 agreement."""
+    from __graft_entry__ import load_package
+    cfg = load_package().configs.config("C3")
+    ek, vk = cfg.model()
+    s = setup("1x4")[0]
+    s.set_model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
+    rng = np.random.default_rng(4)
+    D = 924 * 924
+    x, y = rng.standard_normal(D), rng.standard_normal(D)
+    hx, hy = s.multiply_H(6, 6, x), s.multiply_H(6, 6, y)
+    assert abs(x @ hy - y @ hx) < 1e-11 * abs(x @ hy)
+    hx32 = s.multiply_H(6, 6, x.astype(np.float32))
+    assert rel(hx32, s.multiply_H(6, 6, x.astype(np.float32).astype(np.float64))) < 2e-6
+    # linearity
+    assert rel(s.multiply_H(6, 6, 2.0 * x - y), 2.0 * hx - hy) < 1e-13
+
+
+# ---------------------------------------------------------------- apply_c
+@pytest.mark.parametrize("name", ["1x4", "3x3_dense", "4x4_mixed"])
+def test_apply_c_bitexact(setup, oracle, name):
+    s, m = setup(name)
+    ns = m.nsite
+    rng = np.random.default_rng(5)
+    for nu, nd in [(ns // 2, (ns + 1) // 2), (1, ns - 1)]:
+        b = oracle.Basis(ns, nu, nd)
+        v = rng.standard_normal(b.ntot)
+        for ispin in (1, 2):
+            for iorb in range(1, m.norb + 1):
+                for pm in (1, 2):
+                    tu = nu + ((1 if pm == 1 else -1) if ispin == 1 else 0)
+                    td = nd + ((1 if pm == 1 else -1) if ispin == 2 else 0)
+                    if not (0 <= tu <= ns and 0 <= td <= ns):
+                        continue
+                    _, out = s.apply_c(nu, nd, v, pm, iorb, ispin)
+                    _, ref = oracle.apply_c(m, b, v, pm, iorb, ispin)
+                    assert np.array_equal(out, ref), (nu, nd, pm, iorb, ispin)
+
+
+# ---------------------------------------------------------------- Lanczos
+@pytest.mark.parametrize("name,sector", [("2x6_block", (4, 4)), ("3x3_dense", (3, 3)), ("1x4", (2, 3))])
+def test_lanczos_iteration_fp64(setup, oracle, name, sector):
+    s, m = setup(name, nstep=40)
+    b = oracle.Basis(m.nsite, *sector)
+    v = np.random.default_rng(6).standard_normal(b.ntot)
+    n, a, bb = s.lanczos_iteration(*sector, v)
+    n0, a0, b0 = oracle.lanczos_iteration(m, b, v, 40)
+    k = min(12, n0)
+    assert n == n0
+    assert rel(a[:k], a0[:k]) < 1e-9 and rel(bb[:k], b0[:k]) < 1e-9
+
+
+def test_lanczos_breakdown_small_sector(setup, oracle):
+    """A sector of dimension 5: b(j) falls below 1e-12 and nstep_calc stops there."""
+    s, m = setup("1x4", nstep=30)
+    b = oracle.Basis(m.nsite, 1, 0)
+    v = np.random.default_rng(7).standard_normal(b.ntot)
+    n, a, bb = s.lanczos_iteration(1, 0, v)
+    n0, a0, b0 = oracle.lanczos_iteration(m, b, v, 30)
+    assert n == n0 <= 6
+    assert rel(a[:n], a0[:n]) < 1e-9
+
+
+def test_lanczos_iteration_fp32(setup, oracle):
+    s, m = setup("3x6_block", precision="fp32", nstep=20)
+    b = oracle.Basis(m.nsite, 4, 5)
+    v = np.random.default_rng(8).standard_normal(b.ntot)
+    n, a, bb = s.lanczos_iteration(4, 5, v)
+    n0, a0, b0 = oracle.lanczos_iteration(m, b, v.astype(np.float32).astype(np.float64), 20)
+    assert rel(a[:6], a0[:6]) < 1e-5 and rel(bb[1:6], b0[1:6]) < 1e-5
+
+
+# ---------------------------------------------------------------- diag
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("fp32", 1e-8)])
+def test_diag_vs_dense(setup, oracle, precision, tol):
+    s, m = setup("2x6_block", precision=precision)
+    for nu, nd in [(4, 4), (3, 5), (1, 1), (8, 7)]:
+        b = oracle.Basis(m.nsite, nu, nd)
+        w = np.linalg.eigvalsh(oracle.dense_H(m, b))
+        nev = min(4, b.ntot)
+        ev, vec = s.diag(nu, nd, nev)
+        assert np.abs(ev[:nev] - w[:nev]).max() < tol, (nu, nd, ev[:nev], w[:nev])
+        H = oracle.dense_H(m, b)
+        for i in range(nev):
+            r = H @ vec[:, i] - ev[i] * vec[:, i]
+            assert np.linalg.norm(r) < (1e-7 if precision == "fp64" else 1e-4)
+
+
+# ---------------------------------------------------------------- ed_solve + G
+@pytest.mark.parametrize("precision,etol,gtol", [("fp64", 1e-9, 1e-8), ("fp32", 1e-8, 1e-5)])
+def test_ed_solve_green_c1(solver, oracle, pkg, precision, etol, gtol):
+    """Config 1 (single band, 4 bath levels, all 36 sectors, beta = 50, 1024 w,
+    100 steps): states, probabilities and G(i w_n) vs the oracle."""
+    cfg = pkg.configs.config("C1")
+    ek, vk = cfg.model()
+    nev = 8
+    solver.set_options(precision=precision, nstep=cfg.nstep, nev=nev, beta=cfg.beta)
+    solver.set_model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
+    solver.set_sectors([n for n, _ in cfg.sectors], [u for _, u in cfg.sectors])
+    om = cfg.omega()
+    solver.set_omega(om)
+    st = solver.ed_solve()
+    m = oracle.Model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
+    st_o, vecs = oracle.ed_solve(m, cfg.sectors, nev, cfg.beta)
+    assert [(a["sector"], a["level"]) for a in st] == [(a["sector"], a["level"]) for a in st_o]
+    for a, c in zip(st, st_o):
+        assert abs(a["val"] - c["val"]) < etol
+        assert abs(a["prob"] - c["prob"]) < 1e3 * etol
+    G = solver.ed_calc_green_ftn()
+    Go = oracle.ed_calc_green_ftn(m, cfg.sectors, st_o, vecs, cfg.nstep, om)
+    assert rel(G, Go) < gtol
+
+
+# ---------------------------------------------------------------- bath fit
+def fit_problem(pkg, nbatch=8):
+    return pkg.configs.fit_config(seed=4, nbatch=nbatch)
+
+
+def test_func_dfunc_vs_oracle(solver, oracle, pkg):
+    P = fit_problem(pkg)
+    solver.set_options(precision="fp64")
+    norb, nbath = P["norb"], P["nbath"]
+    ns, nx = norb + nbath, P["X0"].shape[1]
+    for x in P["X0"][:4]:
+        f = solver.FUNC(x, ns, P["nw"], nx, P["omega"], P["dev"], nbath, norb)
+        fo = oracle.func(x, ns, P["omega"], P["dev"], nbath, norb)
+        assert abs(f - fo) < 1e-12 * abs(fo)
+        g = solver.dfunc(x, P["nw"], ns, nx, P["omega"], P["dev"], nbath, norb)
+        go = oracle.dfunc(x, ns, P["omega"], P["dev"], nbath, norb)
+        assert rel(g, go) < 1e-12
+
+
+def test_dfunc_finite_difference_device(solver, pkg):
+    """Device adjoint gradient vs central differences of the device chi^2."""
+    P = fit_problem(pkg)
+    norb, nbath = P["norb"], P["nbath"]
+    ns, nx = norb + nbath, P["X0"].shape[1]
+    x = P["X0"][1]
+    g = solver.dfunc(x, P["nw"], ns, nx, P["omega"], P["dev"], nbath, norb)
+    for i in range(nx):
+        h = 1e-5 * max(1.0, abs(x[i]))
+        xp, xm = x.copy(), x.copy()
+        xp[i] += h
+        xm[i] -= h
+        fd = (solver.FUNC(xp, ns, P["nw"], nx, P["omega"], P["dev"], nbath, norb) -
+              solver.FUNC(xm, ns, P["nw"], nx, P["omega"], P["dev"], nbath, norb)) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-6 * max(abs(g[i]), 1e-6 * np.abs(g).max()), (i, fd, g[i])
+
+
+def test_minimization_vs_oracle_and_batch(solver, oracle, pkg):
+    P = fit_problem(pkg, nbatch=4)
+    norb, nbath = P["norb"], P["nbath"]
+    ns, nx = norb + nbath, P["X0"].shape[1]
+    X, fret, it, st = solver.fit_batch(P["X0"], P["omega"], P["dev"], nbath, norb)
+    for b in range(4):
+        x1, f1, i1 = solver.minimization(P["X0"][b], P["nw"], ns, nx, P["omega"], P["dev"], nbath, norb)
+        # batching does not change a fit: bit-identical to the single fit
+        assert st[b] == 0 and it[b] == i1 and fret[b] == f1 and np.array_equal(X[b], x1)
+        xo, fo, io, rc = oracle.frprmn(P["X0"][b], ns, P["omega"], P["dev"], nbath, norb)
+        assert rc == 0
+        assert abs(f1 - fo) <= 1e-6 * abs(fo) + 1e-12
+
+
+def test_calc_dev_vs_oracle(solver, oracle):
+    rng = np.random.default_rng(10)
+    norb, nbath = 3, 12
+    om = (2 * np.arange(200) + 1) * np.pi / 200.0
+    ek, vk, ef = rng.standard_normal(norb + nbath), rng.standard_normal((norb, nbath)), rng.standard_normal(norb)
+    d = solver.calc_dev(norb, norb + nbath, om, ek, vk, ef)
+    assert rel(d, oracle.calc_dev(norb, norb + nbath, om, ek, vk, ef)) < 1e-14

@@ -1,0 +1,266 @@
+"""CPU tests of the oracle: pinned against the reference's own known answer
+(the 9x9 Hamiltonian of mathematica/MO-DMFT-ED.nb), against an independent
+Jordan-Wigner construction, and against brute-force / textbook checks."""
+import itertools
+import json
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _nb():
+    with open(os.path.join(GOLDEN, "notebook_hmat.json")) as f:
+        return json.load(f)
+
+
+def _model(O, d):
+    m = d["model"]
+    return O.Model(m["norb"], m["nbath"], m["U"], m["J"], np.array(m["ek"]), np.array(m["vk"]))
+
+
+def test_notebook_spectrum(oracle):
+    """mathematica/MO-DMFT-ED.nb:1498-1590: same spectrum in sectors (2,1) and (1,2)."""
+    d = _nb()
+    m = _model(oracle, d)
+    ref = np.linalg.eigvalsh(np.array(d["hmat"]))
+    for nu, nd in [(2, 1), (1, 2)]:
+        H = oracle.dense_H(m, oracle.Basis(3, nu, nd))
+        assert np.allclose(H, H.T)
+        np.testing.assert_allclose(np.linalg.eigvalsh(H), ref, rtol=0, atol=1e-9)
+
+
+def test_notebook_matrix_up_to_gauge(oracle):
+    """The oracle's H equals the notebook matrix entry by entry, in the
+    notebook's basis order, up to a diagonal +-1 gauge of the basis states."""
+    d = _nb()
+    m = _model(oracle, d)
+    b = oracle.Basis(3, 2, 1)
+    H = oracle.dense_H(m, b)
+    Hn = np.array(d["hmat"])
+    modes = {"orb1_up": (1, 1), "orb1_dn": (1, 2), "orb2_up": (2, 1), "orb2_dn": (2, 2),
+             "bath_up": (3, 1), "bath_dn": (3, 2)}
+    order = [modes[k] for k in d["vc_order"]]
+    rows = []
+    for vc in d["basis_vc"]:
+        w = sum(1 << ((sp - 1) * 3 + s - 1) for (s, sp), n in zip(order, vc) if n)
+        rows.append(b.idx(w) - 1)
+    P = H[np.ix_(rows, rows)]
+    assert np.array_equal(np.abs(P), np.abs(Hn))
+    s = np.zeros(9)
+    s[0] = 1
+    for _ in range(9):
+        for i, j in itertools.product(range(9), range(9)):
+            if s[i] and not s[j] and Hn[i, j]:
+                s[j] = np.sign(Hn[i, j] / P[i, j]) * s[i]
+    assert np.all(s != 0)
+    assert np.array_equal(np.outer(s, s) * P, Hn)
+
+
+@pytest.mark.parametrize("norb,nbath,dense", [(1, 3, True), (2, 2, True), (2, 2, False), (3, 1, True), (3, 2, False)])
+def test_restatement_vs_jordan_wigner(oracle, norb, nbath, dense):
+    rng = np.random.default_rng(norb * 10 + nbath)
+    ns = norb + nbath
+    vk = rng.uniform(-0.6, 0.6, (norb, nbath))
+    if not dense:
+        vk[rng.random((norb, nbath)) < 0.5] = 0.0
+    m = oracle.Model(norb, nbath, 2.7, 0.45, rng.uniform(-1, 1, ns), vk)
+    for nu in range(ns + 1):
+        for nd in range(ns + 1):
+            H = oracle.dense_H(m, oracle.Basis(ns, nu, nd))
+            Hj = oracle.jw_sector_H(m, nu, nd)
+            assert np.abs(H - Hj).max() < 1e-12, (nu, nd)
+
+
+@pytest.mark.parametrize("nsite", [1, 4, 7, 10])
+def test_basis_ranks_brute_force(oracle, nsite):
+    """generate_basis: ascending popcount-N words, 1-based inverse tables, and
+    ed_basis_get / ed_basis_idx as inverse maps (ed_basis.F90:35-139)."""
+    for ne in range(nsite + 1):
+        words = [w for w in range(1 << nsite) if bin(w).count("1") == ne]
+        b = oracle.Basis(nsite, ne, nsite - ne)
+        assert b.nup == len(words) == oracle.icom(nsite, ne)
+        assert list(b.up) == words
+        for r, w in enumerate(words):
+            assert b.idx_up[w] == r + 1
+    b = oracle.Basis(nsite, nsite // 2, (nsite + 1) // 2)
+    for i in range(1, b.ntot + 1, max(1, b.ntot // 97)):
+        assert b.idx(b.get(i)) == i
+
+
+def test_icom_matches_binomial(oracle):
+    from math import comb
+    for n in range(0, 16):
+        for m in range(0, n + 1):
+            assert oracle.icom(n, m) == comb(n, m)
+
+
+def test_operator_signs(oracle):
+    """destruction/creation signs = parity of occupied bits below the target."""
+    L = oracle.lib()
+    import ctypes as C
+    out = C.c_uint32()
+    for w in range(64):
+        for site in (1, 2, 3):
+            for spin in (1, 2):
+                bit = (spin - 1) * 3 + site - 1
+                par = -1 if bin(w & ((1 << bit) - 1)).count("1") % 2 else 1
+                s = L.or_destruction_op(w, site, spin, 3, C.byref(out))
+                assert s == (par if (w >> bit) & 1 else 0)
+                s = L.or_creation_op(w, site, spin, 3, C.byref(out))
+                assert s == (0 if (w >> bit) & 1 else par)
+
+
+def test_heapsort_and_boltzmann(oracle):
+    rng = np.random.default_rng(5)
+    a = rng.standard_normal(37)
+    ind = oracle.sort(a)
+    assert np.all(np.diff(a[ind - 1]) >= 0)
+    assert sorted(ind.tolist()) == list(range(1, 38))
+    assert list(oracle.sort(np.array([3.0]))) == [1]
+    e = np.array([0.0, 0.01, 0.5, 1.5, np.finfo(np.float64).max])
+    p = oracle.boltzmann_factor(e, 10.0)
+    Z = np.exp(-10 * (e[:4] - e[0])).sum()
+    assert abs(p[0] - 1 / Z) < 1e-15
+    assert abs(p[2] - 1 / np.exp(-10 * (e[:4] - e[2])).sum()) < 1e-15
+    # -beta*(E_k - E_i) > 10 for some k -> p_i = 0 (ed_solver.F90:207-212)
+    assert p[3] == 0.0 and p[4] == 0.0
+
+
+def test_ev_x_roundtrip(oracle):
+    rng = np.random.default_rng(1)
+    norb, nbath = 3, 12
+    ns = norb + nbath
+    ek = rng.standard_normal(ns)
+    vk = rng.standard_normal((norb, nbath))
+    ef = ek[:norb].copy()
+    x = oracle.ev_to_x(ek, vk, ef, ns, nbath)
+    assert np.array_equal(x[:nbath], ek[norb:])
+    assert np.array_equal(x[nbath:nbath + norb * nbath], vk.ravel())
+    assert np.array_equal(x[-norb:], ef)
+    ef2, ek2, vk2 = oracle.x_to_ev(x, ns, nbath, norb)
+    assert np.array_equal(ef2, ef) and np.array_equal(ek2, ek) and np.array_equal(vk2, vk)
+
+
+def _fit_problem(seed=0, norb=2, nbath=4, nw=64, beta=50.0):
+    rng = np.random.default_rng(seed)
+    ns = norb + nbath
+    om = (2 * np.arange(nw) + 1) * np.pi / beta
+    eps = rng.uniform(-2, 2, nbath)
+    vk = rng.uniform(0.1, 0.6, (norb, nbath))
+    ef = rng.uniform(-0.5, 0.5, norb)
+    z = 1j * om[None, :, None] - eps[None, None, :]
+    dev = (vk[:, None, :] ** 2 / z).sum(-1) + ef[:, None]
+    return ns, om, dev, eps, vk, ef
+
+
+def test_func_matches_formula(oracle):
+    """FUNC (func.f90:1-45) against the closed form with CMPLX-rounded i*w."""
+    ns, om, dev, eps, vk, ef = _fit_problem()
+    norb, nbath = 2, 4
+    rng = np.random.default_rng(3)
+    x = oracle.ev_to_x(np.concatenate([ef, eps]), vk, ef, ns, nbath) + 0.1 * rng.standard_normal(nbath + nbath * norb + norb)
+    ef2, ek2, vk2 = oracle.x_to_ev(x, ns, nbath, norb)
+    omf = om.astype(np.float32).astype(np.float64)
+    z = 1j * omf[None, :, None] - ek2[norb:][None, None, :]
+    delta = (vk2[:, None, :] ** 2 / z).sum(-1) + ef2[:, None]
+    f = (np.abs(delta - dev) ** 2 / om[None, :]).sum() / (norb * norb * len(om))
+    assert abs(oracle.func(x, ns, om, dev, nbath, norb) - f) < 1e-13 * abs(f)
+
+
+def test_dfunc_finite_difference(oracle):
+    ns, om, dev, eps, vk, ef = _fit_problem(seed=2)
+    norb, nbath = 2, 4
+    rng = np.random.default_rng(4)
+    x = oracle.ev_to_x(np.concatenate([ef, eps]), vk, ef, ns, nbath) + 0.2 * rng.standard_normal(nbath + nbath * norb + norb)
+    g = oracle.dfunc(x, ns, om, dev, nbath, norb)
+    h = 1e-6
+    for i in range(len(x)):
+        xp, xm = x.copy(), x.copy()
+        xp[i] += h
+        xm[i] -= h
+        fd = (oracle.func(xp, ns, om, dev, nbath, norb) - oracle.func(xm, ns, om, dev, nbath, norb)) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-6 * max(1e-3, abs(g[i])), (i, fd, g[i])
+
+
+def test_frprmn_recovers_bath(oracle):
+    ns, om, dev, eps, vk, ef = _fit_problem(seed=7)
+    norb, nbath = 2, 4
+    rng = np.random.default_rng(8)
+    x_true = oracle.ev_to_x(np.concatenate([ef, eps]), vk, ef, ns, nbath)
+    x0 = x_true + 0.05 * rng.standard_normal(len(x_true))
+    f0 = oracle.func(x0, ns, om, dev, nbath, norb)
+    x, fret, it, rc = oracle.frprmn(x0, ns, om, dev, nbath, norb)
+    assert rc == 0 and it >= 1
+    assert fret < 1e-3 * f0
+
+
+def test_calc_dev_formula(oracle):
+    norb, nbath = 3, 6
+    rng = np.random.default_rng(9)
+    om = (2 * np.arange(32) + 1) * np.pi / 40.0
+    ek = rng.standard_normal(norb + nbath)
+    vk = rng.standard_normal((norb, nbath))
+    ef = rng.standard_normal(norb)
+    d = oracle.calc_dev(norb, norb + nbath, om, ek, vk, ef)
+    omf = om.astype(np.float32).astype(np.float64)
+    z = 1j * omf[None, :, None] - ek[norb:][None, None, :]
+    ref = (vk[:, None, :] ** 2 / z).sum(-1) + ef[:, None]
+    assert np.abs(d - ref).max() < 1e-13
+
+
+def test_green_cf_equals_exact_resolvent(oracle):
+    """Lanczos continued fraction with nstep >= dimension reproduces the exact
+    sum over poles of the reference's particle / hole G (ed_green.F90:136-185)."""
+    rng = np.random.default_rng(11)
+    norb, nbath = 1, 3
+    ns = norb + nbath
+    m = oracle.Model(norb, nbath, 2.0, 0.0, np.concatenate([[-1.0], rng.uniform(-1, 1, nbath)]),
+                     rng.uniform(0.2, 0.5, (norb, nbath)))
+    nu = nd = 2
+    b = oracle.Basis(ns, nu, nd)
+    w, V = np.linalg.eigh(oracle.dense_H(m, b))
+    E0, psi = w[0], V[:, 0]
+    om = (2 * np.arange(16) + 1) * np.pi / 10.0
+    gr = np.zeros(16, complex)
+    oracle.green_diag(m, b, psi, E0, 1.0, 1.0, 1, 1, 40, om, gr)
+    # exact
+    bo, v = oracle.apply_c(m, b, psi, 1, 1, 1)
+    wp, Vp = np.linalg.eigh(oracle.dense_H(m, bo))
+    wts = (Vp.T @ v) ** 2
+    bo2, v2 = oracle.apply_c(m, b, psi, 2, 1, 1)
+    wm, Vm = np.linalg.eigh(oracle.dense_H(m, bo2))
+    wts2 = (Vm.T @ v2) ** 2
+    z = 1j * om.astype(np.float32).astype(np.float64)
+    e0f = float(np.float32(E0))
+    exact = (wts[None, :] / (z[:, None] + e0f - wp[None, :])).sum(1) + \
+            (wts2[None, :] / (z[:, None] - e0f + wm[None, :])).sum(1)
+    # the hole weight uses the sum rule 1 - ||c+psi||^2
+    assert abs(wts.sum() + wts2.sum() - 1.0) < 1e-12
+    assert np.abs(gr - exact).max() < 1e-9 * np.abs(exact).max()
+
+
+def test_lanczos_iteration_tridiagonal(oracle):
+    """a/b from lanczos_iteration reproduce the Krylov projection of H."""
+    rng = np.random.default_rng(12)
+    norb, nbath = 2, 2
+    m = oracle.Model(norb, nbath, 3.0, 0.6, rng.uniform(-1, 1, 4), rng.uniform(0.1, 0.5, (2, 2)))
+    b = oracle.Basis(4, 2, 2)
+    H = oracle.dense_H(m, b)
+    v0 = rng.standard_normal(b.ntot)
+    n, a, bb = oracle.lanczos_iteration(m, b, v0, 8)
+    assert n == 8
+    # explicit Lanczos in numpy (modified, with reorthogonalisation)
+    Q = [v0 / np.linalg.norm(v0)]
+    al, be2 = [], []
+    for j in range(6):
+        w = H @ Q[-1]
+        al.append(Q[-1] @ w)
+        for q in Q:
+            w -= (q @ w) * q
+        be2.append(w @ w)
+        Q.append(w / np.sqrt(be2[-1]))
+    np.testing.assert_allclose(a[:6], al, rtol=1e-10, atol=1e-10)
+    np.testing.assert_allclose(bb[1:6], be2[:5], rtol=1e-10)
