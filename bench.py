@@ -1,0 +1,354 @@
+"""Benchmark: H*v GB/s on the 3-orbital x 4-bath Kanamori ground sector, plus
+Lanczos + G time, FP32-mixed vs FP64, on one GB300.
+
+A step is one matrix-free H*v (FP32 vectors) on the ground sector (Nup=7,
+Ndn=8) of the 15-site impurity (D = 6435^2 = 41,409,225; x and y are 166 MB
+each, so every step streams inputs larger than the 129 MB L2).  `value` is
+algorithmic bytes (2*D*4: read x once, write y once) per second, aggregated
+over ranks; `e2e` is the same metric through the C-ABI entry point with host
+buffers (pinned H2D of x and D2H of y inside the timed region).  The
+`lanczos_g` object times the full eigensolve + Green's function pipeline on
+one configuration in both precisions and states the E0 / G differences.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Under torchrun (N > 1) every rank runs an independent replica on its own GPU
+("replicas only": the path has no inter-GPU exchange); value = sum over ranks
+with the max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+METRIC = "H*v GB/s and Lanczos+G time, FP32-mixed vs FP64 on one GB300 at dE0<1e-8"
+WORKLOAD = ("ground sector (Nup=7, Ndn=8) of the 3-orbital x 4-bath-per-orbital Kanamori impurity "
+            "(15 sites, D=41,409,225), FP32 matrix-free H*v")
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the H*v kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "hv_c4_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(prefix="clocks_", suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.device)],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("BENCH_BACKEND", "nccl") == "nccl" else "gloo")
+        return dist, dist.get_rank(), ws
+    return None, 0, 1
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline_sample(cfg, nup, ndn, seconds=3.0):
+    """The oracle (C port of multiply_H) on every host core, over a bounded
+    row sample of the same sector; GB/s with the FP64 algorithmic bytes."""
+    import __graft_entry__ as g
+    O = g.load_oracle()
+    ek, vk = cfg.model()
+    m = O.Model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
+    b = O.Basis(cfg.nsite, nup, ndn)
+    x = np.random.default_rng(0).standard_normal(b.ntot)
+    y = np.zeros_like(x)
+    rows = max(1, b.ntot // 256)
+    O.multiply_H_rows(m, b, x, y, 0, rows, 0)       # warm
+    t0 = time.perf_counter()
+    done = 0
+    r0 = 0
+    while time.perf_counter() - t0 < seconds:
+        r1 = min(b.ntot, r0 + rows)
+        O.multiply_H_rows(m, b, x, y, r0, r1, 0)
+        done += r1 - r0
+        r0 = r1 % b.ntot
+    dt = time.perf_counter() - t0
+    return dict(value=2.0 * done * 8 / dt / 1e9, unit="GB/s", cores=os.cpu_count(), kind="port",
+                sample=f"{done} of {b.ntot} rows of one FP64 H*v (oracle C port, OpenMP over rows), {dt:.2f} s")
+
+
+def lanczos_g(pkg, name, nev):
+    """Eigensolve + Green's function in FP32-mixed and FP64; times and errors."""
+    import torch
+    cfg = pkg.configs.config(name)
+    ek, vk = cfg.model()
+    out = {"config": name}
+    res = {}
+    for prec in ("fp32", "fp64"):
+        s = pkg.EDSolver(torch.cuda.current_device(), torch.cuda.current_stream().cuda_stream)
+        s.set_options(precision=prec, nstep=cfg.nstep, nev=nev, beta=cfg.beta)
+        s.set_model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
+        s.set_sectors([n for n, _ in cfg.sectors], [u for _, u in cfg.sectors])
+        s.set_omega(cfg.omega())
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = s.ed_solve()
+        t1 = time.perf_counter()
+        G = s.ed_calc_green_ftn()
+        t2 = time.perf_counter()
+        res[prec] = (st, G)
+        out[prec] = {"solve_s": round(t1 - t0, 4), "green_s": round(t2 - t1, 4), "total_s": round(t2 - t0, 4),
+                     "E0": float(st[0]["val"]), "nev_calc": len(st), "launches": s.kernel_launches,
+                     "eigensolver": s.diag_stats()}
+        s.close()
+    (s32, g32), (s64, g64) = res["fp32"], res["fp64"]
+    out["dE0"] = abs(s32[0]["val"] - s64[0]["val"])
+    out["dE_kept_max"] = max(abs(a["val"] - b["val"]) for a, b in zip(s32, s64)) if len(s32) == len(s64) else None
+    out["dG_rel"] = float(np.abs(g32 - g64).max() / np.abs(g64).max())
+    out["speedup_fp32_vs_fp64"] = round(out["fp64"]["total_s"] / out["fp32"]["total_s"], 3)
+    return out
+
+
+def run_ours(args):
+    import torch
+    dist, rank, ws = dist_init()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    import __graft_entry__ as g
+    pkg = g.load_package()
+    cfg = pkg.configs.config("C4")
+    nelec, nup = cfg.sectors[0]
+    ndn = nelec - nup
+    ek, vk = cfg.model()
+    # a dedicated stream: the solver's kernels and the timing events share it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    s = pkg.EDSolver(local, stream.cuda_stream)
+    s.set_options(precision="fp32")
+    s.set_model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
+    nu_, nd_, D = s.sector_dims(nup, ndn)
+    ld, nelem = s.vector_layout(nup, ndn)
+    # device layout: nd rows of stride ld (128-byte aligned rows), zero pads
+    x = torch.zeros((nd_, ld), dtype=torch.float32, device="cuda")
+    x[:, :nu_] = torch.randn((nd_, nu_), dtype=torch.float32, device="cuda",
+                             generator=torch.Generator("cuda").manual_seed(rank))
+    y = torch.empty_like(x)
+
+    def step():
+        s.multiply_H_dev(nup, ndn, x.data_ptr(), y.data_ptr(), pkg.FP32)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clk = ClockSampler(local)
+    clk.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = s.kernel_launches
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches = s.kernel_launches - l0
+    clocks = clk.stop()
+    t_ms = e0.elapsed_time(e1) / args.steps
+    t_ms = max_over_ranks(dist, t_ms)
+    bytes_step = 2.0 * D * 4
+    value = ws * bytes_step / (t_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peaks()
+    achieved = bytes_step / (t_ms * 1e-3) / 1e9
+    traffic = profile_traffic()
+
+    # end to end through the C-ABI with pinned host buffers
+    xh = torch.empty(D, dtype=torch.float32, pin_memory=True)
+    xh.copy_(x[:, :nu_].reshape(-1).cpu())
+    xn = xh.numpy()
+    yn = torch.empty(D, dtype=torch.float32, pin_memory=True).numpy()
+    import ctypes
+    L = pkg.lib()
+    fp = ctypes.POINTER(ctypes.c_float)
+    xp, yp = xn.ctypes.data_as(fp), yn.ctypes.data_as(fp)
+    for _ in range(2):
+        L.mo_ed_multiply_h_f32(s._ctx, nup, ndn, xp, yp)
+    e2e_steps = max(3, min(args.steps, 20))
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        rc = L.mo_ed_multiply_h_f32(s._ctx, nup, ndn, xp, yp)
+        assert rc == 0
+    t_e2e = (time.perf_counter() - t0) / e2e_steps
+    t_e2e = max_over_ranks(dist, t_e2e)
+    # the e2e output equals the device-resident result
+    step()
+    torch.cuda.synchronize()
+    assert np.array_equal(yn, y[:, :nu_].reshape(-1).cpu().numpy()), "e2e result differs from the device path"
+
+
+    lg = None
+    if rank == 0 and not args.no_lanczos_g:
+        lg = lanczos_g(pkg, args.lg_config, args.lg_nev)
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        cpu = cpu_baseline_sample(cfg, nup, ndn)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(t_ms, 5), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "D": D, "nup": nu_, "ndown": nd_, "row_stride": ld, "seed": cfg.seed,
+                       "l2": "inputs larger than L2 (x and y 166 MB each)", "parallelism": f"replicas{ws}"},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                         "traffic": (traffic or {}).get("bytes_per_launch"),
+                         "traffic_note": (traffic or {}).get("note")},
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(bytes_step / t_e2e / 1e9 * ws, 3), "unit": "GB/s",
+                    "h2d_bytes_per_step": D * 4, "d2h_bytes_per_step": D * 4,
+                    "ms_per_step": round(t_e2e * 1e3, 4)},
+            "gpu_launches": launches,
+            "clocks": clocks,
+            "lanczos_g": lg,
+        }
+        print(json.dumps(line), flush=True)
+    s.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import __graft_entry__ as g
+    pkg = g.load_package()
+    cfg = pkg.configs.config("C4")
+    nelec, nup = cfg.sectors[0]
+    ndn = nelec - nup
+    O = g.load_oracle()
+    ek, vk = cfg.model()
+    m = O.Model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
+    b = O.Basis(cfg.nsite, nup, ndn)
+    x = np.random.default_rng(0).standard_normal(b.ntot)
+    y = np.zeros_like(x)
+    rows = max(1, b.ntot // 512)
+    for _ in range(args.warmup):
+        O.multiply_H_rows(m, b, x, y, 0, rows, 0)
+    times = []
+    r0 = 0
+    for _ in range(args.steps):
+        r1 = min(b.ntot, r0 + rows)
+        t0 = time.perf_counter()
+        O.multiply_H_rows(m, b, x, y, r0, r1, 0)
+        times.append(time.perf_counter() - t0)
+        r0 = r1 % b.ntot
+    t = sum(times) / len(times)
+    v = 2.0 * rows * 8 / t / 1e9
+    sample = (f"{rows} of {b.ntot} rows of one FP64 H*v per step (oracle C port of multiply_H, "
+              f"OpenMP over rows)")
+    line = {
+        "metric": METRIC, "value": round(v, 5), "unit": "GB/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": WORKLOAD.replace("FP32", "FP64 (reference CPU path)"), "D": b.ntot},
+        "cpu_baseline": {"value": round(v, 5), "unit": "GB/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(v, 5), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-lanczos-g", action="store_true")
+    ap.add_argument("--lg-config", default="C3")
+    ap.add_argument("--lg-nev", type=int, default=6)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

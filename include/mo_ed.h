@@ -113,16 +113,24 @@ int mo_ed_basis_get(mo_ed_ctx *ctx, int ne_up, int ne_down, long long n, const l
 int mo_ed_basis_idx(mo_ed_ctx *ctx, int ne_up, int ne_down, long long n,
                     const unsigned int *state, long long *idx);
 
+/* Device layout of a sector vector: ndown rows of nup elements (the
+ * reference's order) with row stride *ld = roundup(nup, 32) elements, so
+ * *nelem = ndown * ld; pad elements must be zero.  The *_dev entry points
+ * take vectors in this layout; host entry points use the reference layout. */
+int mo_ed_vector_layout(mo_ed_ctx *ctx, int ne_up, int ne_down, int *ld, long long *nelem);
+
 /* ---- a6-a10: matrix-free H*v (ed_hamiltonian.F90:88-191 multiply_H) ------ */
 /* B = H*A on host FP64 arrays of ntot entries, computed on the FP64 device path. */
 int mo_ed_multiply_h(mo_ed_ctx *ctx, int ne_up, int ne_down, const double *A, double *B);
 /* Host FP32 arrays, computed on the FP32 device path. */
 int mo_ed_multiply_h_f32(mo_ed_ctx *ctx, int ne_up, int ne_down, const float *A, float *B);
-/* Device pointers; dtype MO_ED_FP64 (double) or MO_ED_FP32 (float).  Issues
- * the H*v kernel on the context's stream; no synchronization. */
+/* Device pointers in the device layout (mo_ed_vector_layout); dtype
+ * MO_ED_FP64 (double) or MO_ED_FP32 (float).  Issues the H*v kernel on the
+ * context's stream; no synchronization. */
 int mo_ed_multiply_h_dev(mo_ed_ctx *ctx, int ne_up, int ne_down, int dtype, const void *dA,
                          void *dB);
-/* FP32 input, FP64-accumulated FP64 output (the refinement operator). */
+/* FP32 input, FP64-accumulated FP64 output (the refinement operator);
+ * device layout. */
 int mo_ed_multiply_h_mixed_dev(mo_ed_ctx *ctx, int ne_up, int ne_down, const float *dA,
                                double *dB);
 
@@ -147,6 +155,12 @@ int mo_ed_lanczos_iteration(mo_ed_ctx *ctx, int ne_up, int ne_down, const double
  * nonexistent levels: DBL_MAX, like the reference's huge()); eigvec may be
  * NULL or a host (ntot, nev) column-major FP64 array. */
 int mo_ed_diag(mo_ed_ctx *ctx, int ne_up, int ne_down, int nev, double *eigval, double *eigvec);
+
+/* Statistics of the last eigensolve (like ARPACK's iparam(3) / iparam(9)):
+ * restart cycles, H*v applications, the largest Ritz residual estimate and
+ * the largest FP64 residual ||H x - E x|| / ||x|| of the returned vectors. */
+int mo_ed_diag_stats(mo_ed_ctx *ctx, int *cycles, long long *matvecs, double *res_est,
+                     double *res_true);
 
 /* ---- a14: ed_solve (ed_solver.F90:28-105) ------------------------------- */
 /* All sectors of mo_ed_set_sectors: eigenpairs, heapsort, Boltzmann weights,

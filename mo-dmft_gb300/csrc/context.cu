@@ -46,6 +46,24 @@ int ensure(mo_ed_ctx *ctx, DevBuf &b, size_t bytes)
     return dev_alloc(ctx, b, bytes);
 }
 
+int upload_padded(mo_ed_ctx *ctx, const Sector &s, const void *host, void *dev, size_t es)
+{
+    const size_t nu = s.up->n, ld = s.ld(), nd = s.dn->n;
+    if (ld > nu)
+        MOED_CUDA(ctx, cudaMemset2DAsync((char *)dev + nu * es, ld * es, 0, (ld - nu) * es, nd, ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpy2DAsync(dev, ld * es, host, nu * es, nu * es, nd, cudaMemcpyHostToDevice,
+                                     ctx->stream));
+    return MO_ED_OK;
+}
+
+int download_padded(mo_ed_ctx *ctx, const Sector &s, const void *dev, void *host, size_t es)
+{
+    const size_t nu = s.up->n, ld = s.ld(), nd = s.dn->n;
+    MOED_CUDA(ctx, cudaMemcpy2DAsync(host, nu * es, dev, ld * es, nu * es, nd, cudaMemcpyDeviceToHost,
+                                     ctx->stream));
+    return MO_ED_OK;
+}
+
 }  // namespace moed
 
 using namespace moed;
@@ -204,6 +222,16 @@ int mo_ed_sector_dims(mo_ed_ctx *ctx, int ne_up, int ne_down, int *nup, int *ndo
     return MO_ED_OK;
 }
 
+int mo_ed_vector_layout(mo_ed_ctx *ctx, int ne_up, int ne_down, int *ld, long long *nelem)
+{
+    CTX_CHECK(ctx);
+    Sector s;
+    if (int rc = get_sector(ctx, ne_up, ne_down, &s)) return rc;
+    if (ld) *ld = s.ld();
+    if (nelem) *nelem = s.Dpad();
+    return MO_ED_OK;
+}
+
 int mo_ed_generate_basis(mo_ed_ctx *ctx, int ne_up, int ne_down, int *up, int *down, int *idx_up,
                          int *idx_down)
 {
@@ -281,12 +309,12 @@ static int multiply_host(mo_ed_ctx *ctx, int ne_up, int ne_down, const void *A, 
     if (!A || !B) return fail(ctx, MO_ED_ERR_ARG, "null vector");
     Sector s;
     if (int rc = get_sector(ctx, ne_up, ne_down, &s)) return rc;
-    const size_t bytes = es * (size_t)s.D();
+    const size_t bytes = es * (size_t)s.Dpad();
     if (int rc = ensure(ctx, ctx->scratch_a, bytes)) return rc;
     if (int rc = ensure(ctx, ctx->scratch_b, bytes)) return rc;
-    MOED_CUDA(ctx, cudaMemcpyAsync(ctx->scratch_a.p, A, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    if (int rc = upload_padded(ctx, s, A, ctx->scratch_a.p, es)) return rc;
     if (int rc = hv_single(ctx, s, kind, ctx->scratch_a.p, ctx->scratch_b.p)) return rc;
-    MOED_CUDA(ctx, cudaMemcpyAsync(B, ctx->scratch_b.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    if (int rc = download_padded(ctx, s, ctx->scratch_b.p, B, es)) return rc;
     MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return MO_ED_OK;
 }
@@ -336,15 +364,14 @@ int mo_ed_apply_c(mo_ed_ctx *ctx, int ne_up, int ne_down, const double *vec, int
     if (ntot_out) *ntot_out = out.D();
     if (!vec_out || capacity < out.D())
         return fail(ctx, MO_ED_ERR_CAPACITY, "vec_out capacity below target dimension");
-    const size_t bin = sizeof(double) * in.D(), bout = sizeof(double) * out.D();
+    const size_t bin = sizeof(double) * in.Dpad(), bout = sizeof(double) * out.Dpad();
     if (int rc = ensure(ctx, ctx->scratch_a, bin)) return rc;
     if (int rc = ensure(ctx, ctx->scratch_b, bout)) return rc;
-    MOED_CUDA(ctx, cudaMemcpyAsync(ctx->scratch_a.p, vec, bin, cudaMemcpyHostToDevice, ctx->stream));
+    if (int rc = upload_padded(ctx, in, vec, ctx->scratch_a.p, sizeof(double))) return rc;
     if (int rc = apply_c_dev(ctx, in, out, MO_ED_FP64, ctx->scratch_a.p, ctx->scratch_b.p, pm, iorb,
                              ispin))
         return rc;
-    MOED_CUDA(ctx, cudaMemcpyAsync(vec_out, ctx->scratch_b.p, bout, cudaMemcpyDeviceToHost,
-                                   ctx->stream));
+    if (int rc = download_padded(ctx, out, ctx->scratch_b.p, vec_out, sizeof(double))) return rc;
     MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return MO_ED_OK;
 }

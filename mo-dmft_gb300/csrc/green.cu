@@ -24,23 +24,25 @@ namespace moed {
 // element with the operator's sign; zero where the operator annihilates the
 // state (ed_operators.F90:44-58).
 template <typename T>
-__global__ void k_apply_c_up(const T *__restrict__ x, T *__restrict__ y, int nu_out, int nd, int nu_in,
-                             const int *__restrict__ out_words, const int *__restrict__ in_rank,
+__global__ void k_apply_c_up(const T *__restrict__ x, T *__restrict__ y, int nu_out, int ld_out, int nd,
+                             int ld_in, const int *__restrict__ out_words, const int *__restrict__ in_rank,
                              int bit, int pm)
 {
-    const long long n = (long long)nu_out * nd;
+    const long long n = (long long)ld_out * nd;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
-        const int u = (int)(i % nu_out);
-        const long long d = i / nu_out;
-        const unsigned w = (unsigned)out_words[u];
-        const bool occ = (w >> bit) & 1u;
+        const int u = (int)(i % ld_out);
+        const long long d = i / ld_out;
         T v = T(0);
-        if ((pm == 1) == occ) {
-            const int sgn = __popc(w & ((1u << bit) - 1u)) & 1;
-            const int j = in_rank[w ^ (1u << bit)];
-            const T src = x[d * nu_in + j];
-            v = sgn ? -src : src;
+        if (u < nu_out) {
+            const unsigned w = (unsigned)out_words[u];
+            const bool occ = (w >> bit) & 1u;
+            if ((pm == 1) == occ) {
+                const int sgn = __popc(w & ((1u << bit) - 1u)) & 1;
+                const int j = in_rank[w ^ (1u << bit)];
+                const T src = x[d * ld_in + j];
+                v = sgn ? -src : src;
+            }
         }
         y[i] = v;
     }
@@ -49,22 +51,22 @@ __global__ void k_apply_c_up(const T *__restrict__ x, T *__restrict__ y, int nu_
 // spin down: the sign also counts every up-spin bit (bitidx = nsite + iorb - 1),
 // i.e. a factor (-1)^(N_up) on top of the down-word parity.
 template <typename T>
-__global__ void k_apply_c_dn(const T *__restrict__ x, T *__restrict__ y, int nu, int nd_out,
+__global__ void k_apply_c_dn(const T *__restrict__ x, T *__restrict__ y, int nu, int ld, int nd_out,
                              const int *__restrict__ out_words, const int *__restrict__ in_rank,
                              int bit, int pm, int up_parity)
 {
-    const long long n = (long long)nu * nd_out;
+    const long long n = (long long)ld * nd_out;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
-        const int u = (int)(i % nu);
-        const int d = (int)(i / nu);
+        const int u = (int)(i % ld);
+        const int d = (int)(i / ld);
         const unsigned w = (unsigned)out_words[d];
         const bool occ = (w >> bit) & 1u;
         T v = T(0);
-        if ((pm == 1) == occ) {
+        if (u < nu && (pm == 1) == occ) {
             const int sgn = (__popc(w & ((1u << bit) - 1u)) + up_parity) & 1;
             const int j = in_rank[w ^ (1u << bit)];
-            const T src = x[(long long)j * nu + u];
+            const T src = x[(long long)j * ld + u];
             v = sgn ? -src : src;
         }
         y[i] = v;
@@ -74,26 +76,26 @@ __global__ void k_apply_c_dn(const T *__restrict__ x, T *__restrict__ y, int nu,
 int apply_c_dev(mo_ed_ctx *ctx, const Sector &in, const Sector &out, int prec, const void *x, void *y,
                 int pm, int iorb, int ispin)
 {
-    const long long n = out.D();
+    const long long n = out.Dpad();
     if (n <= 0) return MO_ED_OK;
     const int T = 256;
     const int g = (int)std::max(1LL, std::min((n + T - 1) / T, (long long)ctx->num_sms * 8));
     const int bit = iorb - 1;
     if (ispin == 1) {
         if (prec == MO_ED_FP32)
-            k_apply_c_up<float><<<g, T, 0, ctx->stream>>>((const float *)x, (float *)y, out.up->n, out.dn->n,
-                                                         in.up->n, out.up->words, in.up->rank, bit, pm);
+            k_apply_c_up<float><<<g, T, 0, ctx->stream>>>((const float *)x, (float *)y, out.up->n, out.ld(),
+                                                         out.dn->n, in.ld(), out.up->words, in.up->rank, bit, pm);
         else
-            k_apply_c_up<double><<<g, T, 0, ctx->stream>>>((const double *)x, (double *)y, out.up->n, out.dn->n,
-                                                          in.up->n, out.up->words, in.up->rank, bit, pm);
+            k_apply_c_up<double><<<g, T, 0, ctx->stream>>>((const double *)x, (double *)y, out.up->n, out.ld(),
+                                                          out.dn->n, in.ld(), out.up->words, in.up->rank, bit, pm);
     } else {
         const int upar = out.ne_up & 1;
         if (prec == MO_ED_FP32)
-            k_apply_c_dn<float><<<g, T, 0, ctx->stream>>>((const float *)x, (float *)y, out.up->n, out.dn->n,
-                                                         out.dn->words, in.dn->rank, bit, pm, upar);
+            k_apply_c_dn<float><<<g, T, 0, ctx->stream>>>((const float *)x, (float *)y, out.up->n, out.ld(),
+                                                         out.dn->n, out.dn->words, in.dn->rank, bit, pm, upar);
         else
-            k_apply_c_dn<double><<<g, T, 0, ctx->stream>>>((const double *)x, (double *)y, out.up->n, out.dn->n,
-                                                          out.dn->words, in.dn->rank, bit, pm, upar);
+            k_apply_c_dn<double><<<g, T, 0, ctx->stream>>>((const double *)x, (double *)y, out.up->n, out.ld(),
+                                                          out.dn->n, out.dn->words, in.dn->rank, bit, pm, upar);
     }
     MOED_CHECK_LAUNCH(ctx);
     return MO_ED_OK;
@@ -379,25 +381,35 @@ int mo_ed_diag(mo_ed_ctx *ctx, int ne_up, int ne_down, int nev, double *eigval, 
     if (int rc = diag_sector(ctx, s, nev, vals, eigvec ? &vecs : nullptr)) return rc;
     for (int i = 0; i < nev; ++i) eigval[i] = vals[i];
     if (eigvec) {
-        const long long D = s.D();
+        const long long D = s.D(), Dp = s.Dpad();
         DevBuf tmp;
         if (ctx->opt.precision == MO_ED_FP32)
-            if (int rc = dev_alloc(ctx, tmp, sizeof(double) * D)) return rc;
+            if (int rc = dev_alloc(ctx, tmp, sizeof(double) * Dp)) return rc;
         for (int i = 0; i < nev; ++i) {
             double *dst = eigvec + (size_t)i * D;
             if (i >= (int)vecs.size()) {
                 memset(dst, 0, sizeof(double) * D);
                 continue;
             }
+            const void *src = vecs[i].p;
             if (ctx->opt.precision == MO_ED_FP32) {
-                if (int rc = convert_f32_to_f64(ctx, (const float *)vecs[i].p, (double *)tmp.p, D)) return rc;
-                MOED_CUDA(ctx, cudaMemcpyAsync(dst, tmp.p, sizeof(double) * D, cudaMemcpyDeviceToHost, ctx->stream));
-            } else {
-                MOED_CUDA(ctx, cudaMemcpyAsync(dst, vecs[i].p, sizeof(double) * D, cudaMemcpyDeviceToHost, ctx->stream));
+                if (int rc = convert_f32_to_f64(ctx, (const float *)vecs[i].p, (double *)tmp.p, Dp)) return rc;
+                src = tmp.p;
             }
+            if (int rc = download_padded(ctx, s, src, dst, sizeof(double))) return rc;
             MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         }
     }
+    return MO_ED_OK;
+}
+
+int mo_ed_diag_stats(mo_ed_ctx *ctx, int *cycles, long long *matvecs, double *res_est, double *res_true)
+{
+    if (!ctx) return MO_ED_ERR_ARG;
+    if (cycles) *cycles = ctx->diag_cycles;
+    if (matvecs) *matvecs = ctx->diag_matvecs;
+    if (res_est) *res_est = ctx->diag_res_est;
+    if (res_true) *res_true = ctx->diag_res_true;
     return MO_ED_OK;
 }
 

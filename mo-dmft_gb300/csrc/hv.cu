@@ -1,31 +1,41 @@
 // hv.cu -- matrix-free Kanamori H*v on a (Nup, Ndn) sector.
 //
-// Replaces multiply_H (ed_hamiltonian.F90:88-191).  For output row index
-// (d, u) (down rank d, up rank u, element X[d][u]) the reference sums
-//   diagonal   onsite + dens_dens                      (:112-141)
-//   hybridisation  V c+_o c_k and V c+_k c_o, both spins (:146-161)
-//   spin-flip  -J c+_{i up} c_{i dn} c+_{j dn} c_{j up}  (:163-174)
-//   pair hop   -J c+_{i up} c+_{i dn} c_{j up} c_{j dn}  (:176-187)
+// Replaces multiply_H (ed_hamiltonian.F90:88-191).  For output element
+// (d, u) (down rank d, up rank u, X[d][u]) the reference sums
+//   diagonal       onsite + dens_dens                      (:112-141)
+//   hybridisation  V c+_o c_k and V c+_k c_o, both spins     (:146-161)
+//   spin-flip      -J c+_{i up} c_{i dn} c+_{j dn} c_{j up}  (:163-174)
+//   pair hop       -J c+_{i up} c+_{i dn} c_{j up} c_{j dn}  (:176-187)
 // gathering A at the state each operator maps row (d, u) to.  Here:
 //   * diagonal = Dup[u] + Ddn[d] + Cross[imp(u)][imp(d)] (tables.cu);
-//   * up-spin hops read X[d][u'] for the <= hw precomputed (u', +-V) of u;
-//   * down-spin hops read whole rows X[d'][*] -- coalesced AXPYs;
-//   * spin-flip / pair-hop factor into an up-spin transfer T_{i<-j}(u) and a
-//     down-spin transfer (T_{j<-i}(d) resp. T_{i<-j}(d)) with coefficient
-//     +J t_up t_dn (the reordering of the four operators gives -1 which
-//     cancels the -J), both transfers staying inside their bath group.
-// A work item is R consecutive rows of one job; a CTA sweeps all columns u of
-// the item, loading the up-hop entries of u once for the R rows.  The kernel
-// walks a batch of jobs (vectors of possibly different sectors) so that all
-// excitation vectors of a Lanczos step share one launch.  Optionally each
-// item writes sum_{its rows} x*y (FP64) for the Lanczos alpha.
+//   * up-spin hops gather X[d][u'] for the precomputed moves (u', +-V) of u;
+//   * down-spin hops are whole-row AXPYs from rows d';
+//   * spin-flip / pair hop factor into an up-spin transfer T_{i<-j}(u) and a
+//     down-spin transfer (T_{j<-i}(d) for spin-flip, T_{i<-j}(d) for pair
+//     hopping) with coefficient +J t_up t_dn: reordering the four operators
+//     of ed_operators.F90:183-213 / 236-266 gives a factor -1 that cancels
+//     the -J.  Both transfers stay inside a bath group (rank offsets that
+//     depend only on the impurity bits).
+//
+// Work decomposition.  An item is up to R rows made of whole down-spin bath
+// groups, so the partner rows of spin-flip / pair hopping are in the item.
+// Items are ordered by the bath occupations of the conserved subsystems, so
+// the down-spin neighbours of the rows in flight stay L2-resident.  A CTA
+// stages its rows in shared memory transposed, S[u][r]: one shared load of
+// S[u'] serves the up-spin move u -> u' for all rows of the item, and the
+// partner rows are shared-memory reads too.  Each thread owns 4 consecutive
+// columns: 16-byte aligned global loads for the down-spin row AXPYs and
+// 16-byte stores of y (rows are padded to a 128-byte stride); its column
+// moves come from a chunk-major table, one contiguous block per slot.  The
+// kernel walks a batch of jobs (vectors of possibly different sectors) so that
+// all excitation vectors of a Lanczos step share one launch; optionally each
+// item writes the FP64 partial of x*y for the Lanczos alpha.
 #include <algorithm>
 
 #include "internal.h"
 
 namespace moed {
 
-constexpr int kHvThreads = 256;
 constexpr int kMaxJobs = 24;
 
 template <typename TA>
@@ -34,25 +44,107 @@ struct HvBatch {
     HvJobT<TA> job[kMaxJobs];
 };
 
-template <typename TX, typename TA, typename TY, int R>
-__global__ void __launch_bounds__(kHvThreads)
+template <typename T>
+struct alignas(16) Vec4 {
+    T v[4];
+};
+
+template <typename T, int R>
+struct alignas(8) RowVec {
+    T v[R];
+};
+
+template <typename T>
+__device__ __forceinline__ Vec4<T> ldg4(const T *p)
+{
+    Vec4<T> r;
+    if constexpr (sizeof(T) == 4) {
+        const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
+        r.v[0] = a.x;
+        r.v[1] = a.y;
+        r.v[2] = a.z;
+        r.v[3] = a.w;
+    } else {
+        const double2 a = __ldg(reinterpret_cast<const double2 *>(p));
+        const double2 b = __ldg(reinterpret_cast<const double2 *>(p) + 1);
+        r.v[0] = a.x;
+        r.v[1] = a.y;
+        r.v[2] = b.x;
+        r.v[3] = b.y;
+    }
+    return r;
+}
+
+__device__ __forceinline__ int4 ldg_i4(const int *p) { return __ldg(reinterpret_cast<const int4 *>(p)); }
+
+template <typename T>
+__device__ __forceinline__ void stg4(T *p, const T (&v)[4])
+{
+    if constexpr (sizeof(T) == 4) {
+        *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    } else {
+        reinterpret_cast<double2 *>(p)[0] = make_double2(v[0], v[1]);
+        reinterpret_cast<double2 *>(p)[1] = make_double2(v[2], v[3]);
+    }
+}
+
+// the 4 moves of slot s of one 4-column chunk
+template <typename TA>
+__device__ __forceinline__ void ld_moves(const HopEnt<TA> *p, HopEnt<TA> (&e)[4])
+{
+    if constexpr (sizeof(TA) == 4) {
+        const int4 a = __ldg(reinterpret_cast<const int4 *>(p));
+        const int4 b = __ldg(reinterpret_cast<const int4 *>(p) + 1);
+        e[0].t = a.x;
+        e[0].v = __int_as_float(a.y);
+        e[1].t = a.z;
+        e[1].v = __int_as_float(a.w);
+        e[2].t = b.x;
+        e[2].v = __int_as_float(b.y);
+        e[3].t = b.z;
+        e[3].v = __int_as_float(b.w);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int4 a = __ldg(reinterpret_cast<const int4 *>(p + k));
+            e[k].t = a.x;
+            e[k].v = __hiloint2double(a.w, a.z);
+        }
+    }
+}
+
+template <typename TX, typename TA, typename TY, int R, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
 k_hv(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict__ mdl)
 {
-    __shared__ int s_t4[kMaxPair * kMaxImp];
-    __shared__ TA s_cross[kMaxImp * kMaxImp];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int npair = mdl->npair, nimp = mdl->nimp;
+    int ldmax = 0;
+    for (int i = 0; i < batch.njobs; ++i) ldmax = max(ldmax, batch.job[i].ld);
+    // dynamic shared memory: staged rows transposed, S[u] = row values of
+    // column u; then the interspecies diagonal and the 4-operator table
+    RowVec<TX, R> *S = reinterpret_cast<RowVec<TX, R> *>(smem_raw);
+    TA *s_cross = reinterpret_cast<TA *>(smem_raw + ((sizeof(RowVec<TX, R>) * (size_t)ldmax + 15) & ~(size_t)15));
+    int *s_t4 = reinterpret_cast<int *>(s_cross + nimp * nimp);
+
+    __shared__ unsigned s_pmask[kMaxImp];
     __shared__ int s_d[R], s_id[R], s_dcnt[R];
     __shared__ TA s_ddiag[R];
     __shared__ int s_dtgt[R][kMaxHop];
     __shared__ TA s_dval[R][kMaxHop];
-    __shared__ unsigned s_sfmask[R], s_phmask[R];
-    __shared__ int s_sfoff[R][kMaxPair], s_phoff[R][kMaxPair];
+    // per (row, pair): spin-flip / pair-hop partner as an item slot (>= 0) or
+    // as -(1 + global row) when the partner row is not staged, and the
+    // coefficient +-J; s_rowmask[p]: bit r spin-flip valid, bit 16+r pair hop
+    __shared__ unsigned s_rowmask[kMaxPair];
+    __shared__ unsigned s_itemmask;
+    __shared__ int s_sfsrc[R][kMaxPair], s_phsrc[R][kMaxPair];
     __shared__ TA s_sfc[R][kMaxPair], s_phc[R][kMaxPair];
-    __shared__ double s_red[kHvThreads / 32];
+    __shared__ double s_red[NT / 32];
 
     const int tid = threadIdx.x;
-    const int npair = mdl->npair, nimp = mdl->nimp, impmask = nimp - 1;
-    for (int i = tid; i < npair * nimp; i += kHvThreads) s_t4[i] = mdl->t4[i];
-    for (int i = tid; i < nimp * nimp; i += kHvThreads) s_cross[i] = (TA)mdl->cross[i];
+    for (int i = tid; i < npair * nimp; i += NT) s_t4[i] = mdl->t4[i];
+    for (int i = tid; i < nimp; i += NT) s_pmask[i] = mdl->pairmask[i];
+    for (int i = tid; i < nimp * nimp; i += NT) s_cross[i] = (TA)mdl->cross[i];
     const TA Jc = (TA)mdl->J;
 
     for (int item = blockIdx.x; item < batch.total_items; item += gridDim.x) {
@@ -61,109 +153,157 @@ k_hv(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict__ mdl
         const HvJobT<TA> &jb = batch.job[j];
         if (jb.active && *jb.active == 0) continue;
         const int it = item - jb.item0;
-        const int d0 = it * R;
-        const int nr = min(R, jb.nd - d0);
-        const int nu = jb.nu, nd = jb.nd;
+        const int nd = jb.nd, ld = jb.ld, nchunk = ld >> 2;
         const TX *__restrict__ x = (const TX *)jb.x;
         TY *__restrict__ y = (TY *)jb.y;
 
-        __syncthreads();  // previous item finished with the row tables
+        __syncthreads();  // the previous item is done with S and the row tables
         if (tid < R) {
-            int r = tid;
-            if (r < nr) {
-                int d = d0 + r;
+            const int r = tid;
+            const int d = jb.items[it * R + r];
+            if (d >= 0) {
+                const int inf = jb.dn_info[d];
                 s_d[r] = d;
-                s_id[r] = jb.dn_words[d] & impmask;
+                s_id[r] = (inf >> 8) & 0xff;
+                s_dcnt[r] = inf & 0xff;
                 s_ddiag[r] = jb.dn_diag[d];
-                s_dcnt[r] = jb.dn_cnt[d];
             } else {
-                s_d[r] = d0;
+                s_d[r] = -1;
                 s_id[r] = 0;
-                s_ddiag[r] = TA(0);
                 s_dcnt[r] = 0;
+                s_ddiag[r] = TA(0);
             }
-            s_sfmask[r] = 0u;
-            s_phmask[r] = 0u;
         }
+        for (int p = tid; p < kMaxPair; p += NT) s_rowmask[p] = 0u;
+        if (tid == 0) s_itemmask = 0u;
         __syncthreads();
-        for (int i = tid; i < R * jb.dn_maxcnt; i += kHvThreads) {
-            int r = i / jb.dn_maxcnt, s = i - r * jb.dn_maxcnt;
-            if (r < nr && s < s_dcnt[r]) {
+        for (int i = tid; i < R * jb.dn_maxcnt; i += NT) {
+            const int r = i / jb.dn_maxcnt, s = i - r * jb.dn_maxcnt;
+            if (s < s_dcnt[r]) {
                 s_dtgt[r][s] = jb.dn_tgt[(size_t)s * nd + s_d[r]];
                 s_dval[r][s] = jb.dn_val[(size_t)s * nd + s_d[r]];
             }
         }
         if (tid < R * npair) {
-            int r = tid / npair, p = tid - r * npair;
-            if (r < nr) {
-                // spin-flip: down transfer j <- i, i.e. table of the reversed pair
-                int esf = s_t4[mdl->pair_rev[p] * nimp + s_id[r]];
-                int eph = s_t4[p * nimp + s_id[r]];
+            const int r = tid / npair, p = tid - r * npair;
+            if (s_d[r] >= 0) {
+                const int esf = s_t4[mdl->pair_rev[p] * nimp + s_id[r]];   // spin-flip: T_{j<-i}(d)
+                const int eph = s_t4[p * nimp + s_id[r]];                  // pair hop:  T_{i<-j}(d)
                 if (esf < 0) {
-                    s_sfoff[r][p] = (int)(short)(esf & 0xffff);
+                    const int off = (int)(short)(esf & 0xffff), dp = s_d[r] + off, rp = r + off;
+                    s_sfsrc[r][p] = (rp >= 0 && rp < R && s_d[rp] == dp) ? rp : -(1 + dp);
                     s_sfc[r][p] = (esf & 0x40000000) ? -Jc : Jc;
-                    atomicOr(&s_sfmask[r], 1u << p);
+                    atomicOr(&s_rowmask[p], 1u << r);
+                    atomicOr(&s_itemmask, 1u << p);
                 }
                 if (eph < 0) {
-                    s_phoff[r][p] = (int)(short)(eph & 0xffff);
+                    const int off = (int)(short)(eph & 0xffff), dp = s_d[r] + off, rp = r + off;
+                    s_phsrc[r][p] = (rp >= 0 && rp < R && s_d[rp] == dp) ? rp : -(1 + dp);
                     s_phc[r][p] = (eph & 0x40000000) ? -Jc : Jc;
-                    atomicOr(&s_phmask[r], 1u << p);
+                    atomicOr(&s_rowmask[p], 1u << (16 + r));
+                    atomicOr(&s_itemmask, 1u << p);
                 }
+            }
+        }
+        // stage the rows, transposed (pad rows staged as zeros)
+        for (int c = tid; c < nchunk; c += NT) {
+            Vec4<TX> v[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int d = jb.items[it * R + r];
+                if (d >= 0) {
+                    v[r] = ldg4(x + (size_t)d * ld + 4 * c);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) v[r].v[k] = TX(0);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                RowVec<TX, R> t;
+#pragma unroll
+                for (int r = 0; r < R; ++r) t.v[r] = v[r].v[k];
+                S[4 * c + k] = t;
             }
         }
         __syncthreads();
 
+        const unsigned imask = s_itemmask;
         double dacc = 0.0;
-        for (int u = tid; u < nu; u += kHvThreads) {
-            const int iu = jb.up_words[u] & impmask;
-            const TA ud = jb.up_diag[u];
-            TA acc[R];
-            TX xs[R];
+        for (int c = tid; c < nchunk; c += NT) {
+            const int u0 = 4 * c;
+            const int4 inf4 = ldg_i4(jb.up_info + u0);
+            const int inf[4] = {inf4.x, inf4.y, inf4.z, inf4.w};
+            const Vec4<TA> ud = ldg4(jb.up_diag + u0);
+            TA acc[4][R];
+            TX xs[4][R];
+            int cnt[4], iu[4];
+            int maxc = 0;
+            // diagonal
 #pragma unroll
-            for (int r = 0; r < R; ++r) {
-                if (r < nr) {
-                    xs[r] = __ldg(x + (size_t)s_d[r] * nu + u);
-                    acc[r] = (ud + s_ddiag[r] + s_cross[iu * nimp + s_id[r]]) * (TA)xs[r];
-                } else {
-                    xs[r] = TX(0);
-                    acc[r] = TA(0);
+            for (int k = 0; k < 4; ++k) {
+                iu[k] = (inf[k] >> 8) & 0xff;
+                cnt[k] = inf[k] & 0xff;
+                maxc = max(maxc, cnt[k]);
+                const RowVec<TX, R> sx = S[u0 + k];
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    xs[k][r] = sx.v[r];
+                    acc[k][r] = (ud.v[k] + s_ddiag[r] + s_cross[iu[k] * nimp + s_id[r]]) * (TA)sx.v[r];
                 }
             }
-            // up-spin hybridisation: in-row gathers
-            const int cnt = jb.up_cnt[u];
-            for (int s = 0; s < cnt; ++s) {
-                const int t = __ldg(jb.up_tgt + (size_t)s * nu + u);
-                const TA v = __ldg(jb.up_val + (size_t)s * nu + u);
+            // up-spin hybridisation: shared-memory gathers, all rows at once
+            const HopEnt<TA> *tab = jb.up_tab + (size_t)c * jb.up_hw * 4;
+            for (int s = 0; s < maxc; ++s) {
+                HopEnt<TA> e[4];
+                ld_moves<TA>(tab + (size_t)s * 4, e);
 #pragma unroll
-                for (int r = 0; r < R; ++r)
-                    if (r < nr) acc[r] += v * (TA)__ldg(x + (size_t)s_d[r] * nu + t);
-            }
-            // down-spin hybridisation: row AXPYs
+                for (int k = 0; k < 4; ++k) {
+                    if (s < cnt[k]) {
+                        const RowVec<TX, R> g = S[e[k].t];
 #pragma unroll
-            for (int r = 0; r < R; ++r) {
-                if (r < nr) {
-                    const int c = s_dcnt[r];
-                    for (int s = 0; s < c; ++s)
-                        acc[r] += s_dval[r][s] * (TA)__ldg(x + (size_t)s_dtgt[r][s] * nu + u);
+                        for (int r = 0; r < R; ++r) acc[k][r] += e[k].v * (TA)g.v[r];
+                    }
                 }
             }
-            // spin-flip and pair hopping
-            for (int p = 0; p < npair; ++p) {
-                const int e = s_t4[p * nimp + iu];
-                if (e < 0) {
-                    const int uu = u + (int)(short)(e & 0xffff);
+            // down-spin hybridisation: row AXPYs (16-byte loads)
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int n = s_dcnt[r];
+#pragma unroll 4
+                for (int s = 0; s < n; ++s) {
+                    const TA v = s_dval[r][s];
+                    const Vec4<TX> g = ldg4(x + (size_t)s_dtgt[r][s] * ld + u0);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) acc[k][r] += v * (TA)g.v[k];
+                }
+            }
+            // spin-flip and pair hopping: pairs valid for this column and for
+            // some row of the item; partner rows read from the stage
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                unsigned pm = s_pmask[iu[k]] & imask;
+                while (pm) {
+                    const int p = __ffs(pm) - 1;
+                    pm &= pm - 1;
+                    const int e = s_t4[p * nimp + iu[k]];
+                    const int uu = u0 + k + (int)(short)(e & 0xffff);
                     const bool neg = (e & 0x40000000) != 0;
+                    const unsigned rm = s_rowmask[p];
+                    const TX *su = reinterpret_cast<const TX *>(&S[uu]);
 #pragma unroll
                     for (int r = 0; r < R; ++r) {
-                        if (r < nr) {
-                            if ((s_sfmask[r] >> p) & 1u) {
-                                TA c = neg ? -s_sfc[r][p] : s_sfc[r][p];
-                                acc[r] += c * (TA)__ldg(x + (size_t)(s_d[r] + s_sfoff[r][p]) * nu + uu);
-                            }
-                            if ((s_phmask[r] >> p) & 1u) {
-                                TA c = neg ? -s_phc[r][p] : s_phc[r][p];
-                                acc[r] += c * (TA)__ldg(x + (size_t)(s_d[r] + s_phoff[r][p]) * nu + uu);
-                            }
+                        if ((rm >> r) & 1u) {
+                            const int src = s_sfsrc[r][p];
+                            const TX xv = src >= 0 ? su[src] : __ldg(x + (size_t)(-1 - src) * ld + uu);
+                            const TA cf = neg ? -s_sfc[r][p] : s_sfc[r][p];
+                            acc[k][r] += cf * (TA)xv;
+                        }
+                        if ((rm >> (16 + r)) & 1u) {
+                            const int src = s_phsrc[r][p];
+                            const TX xv = src >= 0 ? su[src] : __ldg(x + (size_t)(-1 - src) * ld + uu);
+                            const TA cf = neg ? -s_phc[r][p] : s_phc[r][p];
+                            acc[k][r] += cf * (TA)xv;
                         }
                     }
                 }
@@ -171,10 +311,14 @@ k_hv(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict__ mdl
             TA part = TA(0);
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                if (r < nr) {
-                    TY o = (TY)acc[r];
-                    y[(size_t)s_d[r] * nu + u] = o;
-                    part += (TA)xs[r] * (TA)o;
+                if (s_d[r] >= 0) {
+                    TY o[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        o[k] = (TY)acc[k][r];
+                        part += (TA)xs[k][r] * (TA)o[k];
+                    }
+                    stg4(y + (size_t)s_d[r] * ld + u0, o);
                 }
             }
             dacc += (double)part;
@@ -185,42 +329,51 @@ k_hv(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict__ mdl
             __syncthreads();
             if (tid == 0) {
                 double t = 0.0;
-                for (int w = 0; w < kHvThreads / 32; ++w) t += s_red[w];
+                for (int w = 0; w < NT / 32; ++w) t += s_red[w];
                 jb.dot_partial[it] = t;
             }
         }
     }
 }
 
-int hv_rows_per_item(int kind) { return kind == HV_F32 ? 4 : 2; }
+template <typename TX, typename TA, int R>
+static size_t dyn_smem_bytes(int ld, const ModelDev &m)
+{
+    return ((sizeof(RowVec<TX, R>) * (size_t)ld + 15) & ~(size_t)15) + sizeof(TA) * (size_t)m.nimp * m.nimp +
+           sizeof(int) * (size_t)m.npair * m.nimp;
+}
+
+// rows per item: FP32 vectors R = 6 (two 3-row bath groups of a 3-orbital
+// impurity), FP64 / mixed R = 3
+int hv_rows_per_item(int kind) { return kind == HV_F32 ? 6 : 3; }
 
 template <typename TA>
 void hv_fill_job(const mo_ed_ctx *ctx, const Sector &s, int kind, const void *x, void *y,
                  HvJobT<TA> &j)
 {
-    (void)ctx;
     const bool f32 = sizeof(TA) == 4;
+    (void)ctx;
     j.x = x;
     j.y = y;
     j.dot_partial = nullptr;
     j.active = nullptr;
     j.nu = s.up->n;
     j.nd = s.dn->n;
+    j.ld = s.ld();
     const int R = hv_rows_per_item(kind);
-    j.nitems = (j.nd + R - 1) / R;
+    auto it = s.dn->items.find(R);
+    j.items = it != s.dn->items.end() ? it->second : nullptr;
+    j.nitems = it != s.dn->items.end() ? s.dn->nitems.at(R) : 0;
     j.item0 = 0;
-    j.up_words = s.up->words;
-    j.up_cnt = s.up->hop_cnt;
-    j.up_tgt = s.up->hop_tgt;
-    j.up_val = f32 ? (const TA *)s.up->hop_val_f : (const TA *)s.up->hop_val_d;
+    j.up_info = s.up->info;
+    j.up_tab = f32 ? (const HopEnt<TA> *)s.up->tab_f : (const HopEnt<TA> *)s.up->tab_d;
     j.up_diag = f32 ? (const TA *)s.up->diag_f : (const TA *)s.up->diag_d;
-    j.dn_words = s.dn->words;
-    j.dn_cnt = s.dn->hop_cnt;
+    j.up_hw = s.up->hw;
+    j.up_maxcnt = s.up->max_cnt;
+    j.dn_info = s.dn->info;
     j.dn_tgt = s.dn->hop_tgt;
     j.dn_val = f32 ? (const TA *)s.dn->hop_val_f : (const TA *)s.dn->hop_val_d;
     j.dn_diag = f32 ? (const TA *)s.dn->diag_f : (const TA *)s.dn->diag_d;
-    j.up_hw = s.up->hw;
-    j.dn_hw = s.dn->hw;
     j.dn_maxcnt = s.dn->max_cnt;
     j.pad = 0;
 }
@@ -229,12 +382,23 @@ template void hv_fill_job<float>(const mo_ed_ctx *, const Sector &, int, const v
 template void hv_fill_job<double>(const mo_ed_ctx *, const Sector &, int, const void *, void *,
                                   HvJobT<double> &);
 
-template <typename TX, typename TA, typename TY, int R>
+template <typename TX, typename TA, typename TY, int R, int NT, int MINB>
 static int launch_batch(mo_ed_ctx *ctx, const HvBatch<TA> &b)
 {
     if (b.total_items <= 0) return MO_ED_OK;
-    int grid = std::min(b.total_items, ctx->num_sms * 8);
-    k_hv<TX, TA, TY, R><<<grid, kHvThreads, 0, ctx->stream>>>(b, ctx->d_mdl);
+    int ldmax = 0;
+    for (int i = 0; i < b.njobs; ++i) {
+        ldmax = std::max(ldmax, b.job[i].ld);
+        if (!b.job[i].items) return fail(ctx, MO_ED_ERR_STATE, "H*v item table missing");
+    }
+    const size_t smem = dyn_smem_bytes<TX, TA, R>(ldmax, ctx->mdl);
+    auto kern = k_hv<TX, TA, TY, R, NT, MINB>;
+    MOED_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    MOED_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem));
+    if (per_sm < 1) return fail(ctx, MO_ED_ERR_ARG, "sector rows too long for the shared-memory stage");
+    const int grid = std::min(b.total_items, ctx->num_sms * per_sm);
+    kern<<<grid, NT, smem, ctx->stream>>>(b, ctx->d_mdl);
     MOED_CHECK_LAUNCH(ctx);
     return MO_ED_OK;
 }
@@ -244,10 +408,10 @@ static int launch_kind(mo_ed_ctx *ctx, int kind, const HvBatch<TA> &b)
 {
     if constexpr (sizeof(TA) == 4) {
         (void)kind;
-        return launch_batch<float, float, float, 4>(ctx, b);
+        return launch_batch<float, float, float, 6, 512, 1>(ctx, b);
     } else {
-        if (kind == HV_F64) return launch_batch<double, double, double, 2>(ctx, b);
-        return launch_batch<float, double, double, 2>(ctx, b);
+        if (kind == HV_F64) return launch_batch<double, double, double, 3, 256, 1>(ctx, b);
+        return launch_batch<float, double, double, 3, 256, 1>(ctx, b);
     }
 }
 
@@ -281,8 +445,16 @@ int hv_launch_f64(mo_ed_ctx *ctx, int kind, const HvJobT<double> *jobs, int njob
     return hv_run_jobs<double>(ctx, kind, jobs, njobs);
 }
 
+int hv_prepare(mo_ed_ctx *ctx, const Sector &s, int kind)
+{
+    const int *items;
+    int n;
+    return species_items(ctx, s.dn, hv_rows_per_item(kind), &items, &n);
+}
+
 int hv_single(mo_ed_ctx *ctx, const Sector &s, int kind, const void *x, void *y)
 {
+    if (int rc = hv_prepare(ctx, s, kind)) return rc;
     if (kind == HV_F32) {
         HvJobT<float> j;
         hv_fill_job<float>(ctx, s, kind, x, y, j);

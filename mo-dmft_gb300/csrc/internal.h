@@ -1,11 +1,14 @@
 // internal.h -- shared declarations of the GB300 ED solver (sm_103a).
 //
 // Data layout in HBM
-//   A sector vector X of dimension D = nup*ndown is stored as ndown rows of
-//   nup contiguous elements: X[idown][iup] (row index iup + idown*nup,
-//   0-based) -- the reference's row order (ed_basis.F90:120-123,137-138).
-//   Every H*v term that moves only up-spin electrons stays inside a row;
-//   down-spin moves are whole-row AXPYs.
+//   A sector vector X of dimension D = nup*ndown is stored on the device as
+//   ndown rows of nup elements, X[idown][iup] -- the reference's row order
+//   (ed_basis.F90:120-123,137-138: row index iup + (idown-1)*nup) -- with the
+//   row stride padded to ld = roundup(nup, 32) so that every row starts on a
+//   128-byte boundary (pad elements are zero).  Host entry points convert to
+//   and from the unpadded reference layout with one 2D copy.  Every H*v term
+//   that moves only up-spin electrons stays inside a row; down-spin moves are
+//   whole-row AXPYs.
 //
 //   Per spin species (nsite sites, N electrons) the device holds
 //     words[n]          ascending state words (colex unrank),
@@ -49,30 +52,60 @@ struct ModelDev {
     // pair p=(i,j): bit31 valid, bit30 negative sign, low 16 bits signed rank delta
     int t4[kMaxPair * kMaxImp];
     int pair_rev[kMaxPair];       // index of (j,i) for p=(i,j)
+    unsigned pairmask[kMaxImp];   // bit p set iff T_p(I) is valid
+    double cval[kMaxHop];         // nonzero couplings V in the reference loop order
     double cross[kMaxImp * kMaxImp];  // interspecies diagonal U n_i^up n_i^dn + (U-2J) n_i^up n_j^dn
 };
 
 // ---------------------------------------------------------------------------
 // spin species tables
 // ---------------------------------------------------------------------------
+template <typename T>
+struct HopEnt;                    // one up-spin move of a column: target rank and signed coupling
+template <>
+struct alignas(8) HopEnt<float> {
+    int t;
+    float v;
+};
+template <>
+struct alignas(16) HopEnt<double> {
+    int t, pad;
+    double v;
+};
+
 struct Species {
     int nsite = 0, N = 0, n = 0, hw = 0;
+    int n_pad = 0;                // roundup(n, 32): row stride when this species is the up spin
     int *words = nullptr;
     int *rank = nullptr;
     int *hop_cnt = nullptr;
-    int *hop_tgt = nullptr;
-    double *hop_val_d = nullptr;
+    int *hop_tgt = nullptr;       // [hw][n]
+    double *hop_val_d = nullptr;  // [hw][n]
     float *hop_val_f = nullptr;
-    double *diag_d = nullptr;
+    int *info = nullptr;          // [n_pad]: hop count | impurity bits << 8 (pads: 0)
+    double *diag_d = nullptr;     // [n_pad] (pads: 0)
     float *diag_f = nullptr;
+    // column move tables, chunk-major: entry (chunk c = u/4, slot s, u%4) at
+    // (c*hw + s)*4 + u%4, so one thread reads the slot-s moves of its four
+    // columns as one contiguous 32-byte (FP32) / 64-byte (FP64) block
+    HopEnt<float> *tab_f = nullptr;
+    HopEnt<double> *tab_d = nullptr;
     int max_cnt = 0;              // largest hop_cnt over words
+    int max_group = 0;            // largest bath group (words sharing their bath bits)
+    // row items for a given rows-per-item R: whole bath groups packed into
+    // items of <= R rows (rank order inside a group), items sorted by the
+    // bath-occupation counts of the conserved subsystems; -1 pads
+    std::map<int, int *> items;   // R -> [nitems][R]
+    std::map<int, int> nitems;
     ~Species();
 };
 
 struct Sector {
     int ne_up, ne_down;
     Species *up, *dn;
-    long long D() const { return (long long)up->n * dn->n; }
+    long long D() const { return (long long)up->n * dn->n; }     // dimension
+    int ld() const { return up->n_pad; }                           // device row stride
+    long long Dpad() const { return (long long)up->n_pad * dn->n; } // device elements
 };
 
 // ---------------------------------------------------------------------------
@@ -80,17 +113,22 @@ struct Sector {
 // ---------------------------------------------------------------------------
 template <typename TA>
 struct HvJobT {
-    const void *x;            // input vector (TX)
-    void *y;                  // output vector (TY)
+    const void *x;            // input vector (TX), device layout
+    void *y;                  // output vector (TY), device layout
     double *dot_partial;      // optional [nitems]: sum over the item of x*y
-    int nu, nd;
-    int item0, nitems;
-    const int *up_words, *up_cnt, *up_tgt;
-    const TA *up_val, *up_diag;
-    const int *dn_words, *dn_cnt, *dn_tgt;
-    const TA *dn_val, *dn_diag;
-    int up_hw, dn_hw, dn_maxcnt, pad;
     const int *active;        // optional device flag: job skipped when *active == 0
+    int nu, nd, ld;
+    int item0, nitems;
+    const int *items;         // [nitems][R] rows of each item (-1 pads)
+    const int *up_info;       // [ld]: move count | impurity bits << 8
+    const HopEnt<TA> *up_tab; // chunk-major column moves
+    const TA *up_diag;        // [ld]
+    int up_hw, up_maxcnt;
+    const int *dn_info;       // [nd]
+    const int *dn_tgt;        // [hw][nd]
+    const TA *dn_val;         // [hw][nd]
+    const TA *dn_diag;        // [nd]
+    int dn_maxcnt, pad;
 };
 
 // ---------------------------------------------------------------------------
@@ -156,7 +194,13 @@ struct mo_ed_ctx {
     moed::ModelDev *d_mdl = nullptr;
     std::vector<int> cpl_orb, cpl_bath;  // nonzero couplings in reference loop order
     std::vector<double> cpl_val;
+    std::vector<int> site_subsys;  // conserved subsystem (orbital + coupled bath levels) of each site
     std::map<int, std::unique_ptr<moed::Species>> species;  // by N
+
+    // statistics of the last eigensolve (mo_ed_diag_stats)
+    int diag_cycles = 0;
+    long long diag_matvecs = 0;
+    double diag_res_est = 0.0, diag_res_true = 0.0;
 
     // sectors / omega
     std::vector<int> nelec, nup;
@@ -189,6 +233,10 @@ int cuda_fail(mo_ed_ctx *ctx, cudaError_t e, const char *what);
 
 int dev_alloc(mo_ed_ctx *ctx, DevBuf &b, size_t bytes);
 int ensure(mo_ed_ctx *ctx, DevBuf &b, size_t bytes);
+// host vector in the reference layout (D contiguous) <-> device vector in the
+// padded layout (ndown rows of stride ld, zero pads); es = element size.
+int upload_padded(mo_ed_ctx *ctx, const Sector &s, const void *host, void *dev, size_t es);
+int download_padded(mo_ed_ctx *ctx, const Sector &s, const void *dev, void *host, size_t es);
 
 // ---- tables (tables.cu) ----------------------------------------------------
 long long binom(int n, int k);
@@ -210,7 +258,11 @@ void hv_fill_job(const mo_ed_ctx *ctx, const Sector &s, int kind, const void *x,
 // passed to the kernel by value, so the call can be captured in a CUDA graph.
 int hv_launch_f32(mo_ed_ctx *ctx, const HvJobT<float> *jobs, int njobs);
 int hv_launch_f64(mo_ed_ctx *ctx, int kind, const HvJobT<double> *jobs, int njobs);
+// rows per item of a kind, and the item table of a down species for it
 int hv_rows_per_item(int kind);
+int species_items(mo_ed_ctx *ctx, Species *sp, int R, const int **items, int *nitems);
+// build the item table H*v of `kind` needs for sector s
+int hv_prepare(mo_ed_ctx *ctx, const Sector &s, int kind);
 // Convenience: one vector, jobs staged through scratch.
 int hv_single(mo_ed_ctx *ctx, const Sector &s, int kind, const void *x, void *y);
 

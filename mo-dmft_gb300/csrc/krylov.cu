@@ -55,18 +55,11 @@ __global__ void k_dot_part(const TX *__restrict__ x, const TY *__restrict__ y, l
     double acc = 0.0;
     const long long stride = (long long)gridDim.x * blockDim.x;
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    // products and sums in FP64 (an FP32 x FP32 product is exact in FP64)
     for (; i + 3 * stride < n; i += 4 * stride) {
-        double p = (double)x[i] * (double)y[i];
-        if (sizeof(TX) == 4 && sizeof(TY) == 4) {
-            float q = (float)x[i] * (float)y[i] + (float)x[i + stride] * (float)y[i + stride] +
-                      (float)x[i + 2 * stride] * (float)y[i + 2 * stride] +
-                      (float)x[i + 3 * stride] * (float)y[i + 3 * stride];
-            acc += (double)q;
-        } else {
-            acc += p + (double)x[i + stride] * (double)y[i + stride] +
-                   (double)x[i + 2 * stride] * (double)y[i + 2 * stride] +
-                   (double)x[i + 3 * stride] * (double)y[i + 3 * stride];
-        }
+        acc += (double)x[i] * (double)y[i] + (double)x[i + stride] * (double)y[i + stride] +
+               (double)x[i + 2 * stride] * (double)y[i + 2 * stride] +
+               (double)x[i + 3 * stride] * (double)y[i + 3 * stride];
     }
     for (; i < n; i += stride) acc += (double)x[i] * (double)y[i];
     double t = block_sum(acc, sred);
@@ -247,7 +240,7 @@ int lz_setup(mo_ed_ctx *ctx, LzBatch &b, const std::vector<Sector> &secs, int pr
     const size_t es = prec == MO_ED_FP32 ? sizeof(float) : sizeof(double);
     for (int r = 0; r < nrun; ++r)
         for (int k = 0; k < 4; ++k)
-            if (int rc = dev_alloc(ctx, b.vecs[4 * r + k], es * (size_t)secs[r].D())) return rc;
+            if (int rc = dev_alloc(ctx, b.vecs[4 * r + k], es * (size_t)secs[r].Dpad())) return rc;
     if (int rc = dev_alloc(ctx, b.coef, sizeof(double) * 2 * (nstep + 1) * nrun)) return rc;
     if (int rc = dev_alloc(ctx, b.flags, sizeof(int) * 2 * nrun)) return rc;
     MOED_CUDA(ctx, cudaMemsetAsync(b.coef.p, 0, b.coef.bytes, ctx->stream));
@@ -263,13 +256,14 @@ int lz_setup(mo_ed_ctx *ctx, LzBatch &b, const std::vector<Sector> &secs, int pr
     b.hv_item0.resize(nrun);
     b.hv_nitems.resize(nrun);
     b.upd_total = b.hv_total = 0;
-    const int R = hv_rows_per_item(prec == MO_ED_FP32 ? HV_F32 : HV_F64);
+    const int kind = prec == MO_ED_FP32 ? HV_F32 : HV_F64;
     for (int r = 0; r < nrun; ++r) {
+        if (int rc = hv_prepare(ctx, secs[r], kind)) return rc;
         b.upd_item0[r] = b.upd_total;
-        b.upd_nitems[r] = (int)((secs[r].D() + kVecChunk - 1) / kVecChunk);
+        b.upd_nitems[r] = (int)((secs[r].Dpad() + kVecChunk - 1) / kVecChunk);
         b.upd_total += b.upd_nitems[r];
         b.hv_item0[r] = b.hv_total;
-        b.hv_nitems[r] = (secs[r].dn->n + R - 1) / R;
+        b.hv_nitems[r] = secs[r].dn->nitems.at(hv_rows_per_item(kind));
         b.hv_total += b.hv_nitems[r];
     }
     if (int rc = dev_alloc(ctx, b.upd_part, sizeof(double) * std::max(1, b.upd_total))) return rc;
@@ -289,7 +283,7 @@ static void lz_fill_dev(LzBatch &b, LzBatchDev &d)
         LzRunDev &R = d.run[r];
         for (int k = 0; k < 3; ++k) R.u[k] = b.vecs[4 * r + k].p;
         R.w = b.vecs[4 * r + 3].p;
-        R.D = b.sec[r].D();
+        R.D = b.sec[r].Dpad();
         R.upd_item0 = b.upd_item0[r];
         R.upd_nitems = b.upd_nitems[r];
         R.hv_item0 = b.hv_item0[r];
@@ -370,17 +364,15 @@ int lanczos_reference(mo_ed_ctx *ctx, const Sector &s, const double *h_vec, int 
     LzBatch lb;
     const int prec = ctx->opt.precision;
     if (int rc = lz_setup(ctx, lb, {s}, prec, nstep)) return rc;
-    const long long D = s.D();
+    const long long Dp = s.Dpad();
     if (prec == MO_ED_FP32) {
-        if (int rc = ensure(ctx, ctx->scratch_a, sizeof(double) * D)) return rc;
-        MOED_CUDA(ctx, cudaMemcpyAsync(ctx->scratch_a.p, h_vec, sizeof(double) * D,
-                                       cudaMemcpyHostToDevice, ctx->stream));
+        if (int rc = ensure(ctx, ctx->scratch_a, sizeof(double) * Dp)) return rc;
+        if (int rc = upload_padded(ctx, s, h_vec, ctx->scratch_a.p, sizeof(double))) return rc;
         if (int rc = convert_f64_to_f32(ctx, (const double *)ctx->scratch_a.p,
-                                        (float *)lz_start_vector(lb, 0), D))
+                                        (float *)lz_start_vector(lb, 0), Dp))
             return rc;
     } else {
-        MOED_CUDA(ctx, cudaMemcpyAsync(lz_start_vector(lb, 0), h_vec, sizeof(double) * D,
-                                       cudaMemcpyHostToDevice, ctx->stream));
+        if (int rc = upload_padded(ctx, s, h_vec, lz_start_vector(lb, 0), sizeof(double))) return rc;
     }
     std::vector<std::vector<double>> A, B;
     std::vector<int> nc;
@@ -514,12 +506,33 @@ __global__ void k_scale_copy(const T *__restrict__ in, T *__restrict__ out, long
         out[i] = in[i] * s;
 }
 
-// deterministic pseudo-random start vector in [-1, 1)
+// partial sums of ||y - theta x||^2 (x of type T, y FP64)
 template <typename T>
-__global__ void k_random(T *x, long long n, unsigned long long seed)
+__global__ void k_resid_part(const T *__restrict__ x, const double *__restrict__ y, const double *theta,
+                             long long n, double *part)
+{
+    __shared__ double sred[32];
+    const double th = *theta;
+    double acc = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double r = y[i] - th * (double)x[i];
+        acc += r * r;
+    }
+    double t = block_sum(acc, sred);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// deterministic pseudo-random start vector in [-1, 1) (zero in the row pads)
+template <typename T>
+__global__ void k_random(T *x, long long n, int ld, int nu, unsigned long long seed)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
+        if ((int)(i % ld) >= nu) {
+            x[i] = T(0);
+            continue;
+        }
         unsigned long long z = (unsigned long long)i + seed * 0x9E3779B97F4A7C15ull;
         z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
         z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
@@ -666,6 +679,71 @@ __global__ void k_jacobi(const double *__restrict__ Hp, int ldh, int m, int kk,
     }
 }
 
+// Generalized symmetric problem P c = lambda S c (k x k, column-major, upper
+// triangles of P and S filled): S = L L^T (Cholesky), A = L^-1 P L^-T.  One
+// thread; k is the number of Ritz vectors.  flag = 1 if S is not positive.
+__global__ void k_gen_eig_prep(const double *P, const double *S, int k, double *A, double *L, double *flag)
+{
+    flag[0] = 0.0;
+    for (int j = 0; j < k; ++j)
+        for (int i = 0; i < k; ++i) L[(size_t)j * k + i] = 0.0;
+    for (int j = 0; j < k; ++j) {
+        double d = S[(size_t)j * k + j];
+        for (int t = 0; t < j; ++t) d -= L[(size_t)t * k + j] * L[(size_t)t * k + j];
+        if (!(d > 0.0)) {
+            flag[0] = 1.0;
+            return;
+        }
+        const double ljj = sqrt(d);
+        L[(size_t)j * k + j] = ljj;
+        for (int i = j + 1; i < k; ++i) {
+            double v = S[(size_t)i * k + j];   // S(j,i), upper triangle
+            for (int t = 0; t < j; ++t) v -= L[(size_t)t * k + i] * L[(size_t)t * k + j];
+            L[(size_t)j * k + i] = v / ljj;
+        }
+    }
+    // B = L^-1 Psym (column by column), then A = L^-1 B^T
+    for (int c = 0; c < k; ++c) {
+        for (int i = 0; i < k; ++i) {
+            const double pic = 0.5 * (P[(size_t)c * k + i] + P[(size_t)i * k + c]);
+            double v = pic;
+            for (int t = 0; t < i; ++t) v -= L[(size_t)t * k + i] * A[(size_t)c * k + t];
+            A[(size_t)c * k + i] = v / L[(size_t)i * k + i];
+        }
+    }
+    // A currently holds B = L^-1 Psym; form L^-1 B^T in place via a copy
+    for (int r = 0; r < k; ++r)
+        for (int c = r + 1; c < k; ++c) {
+            const double t = A[(size_t)c * k + r];
+            A[(size_t)c * k + r] = A[(size_t)r * k + c];
+            A[(size_t)r * k + c] = t;
+        }
+    for (int c = 0; c < k; ++c) {
+        for (int i = 0; i < k; ++i) {
+            double v = A[(size_t)c * k + i];
+            for (int t = 0; t < i; ++t) v -= L[(size_t)t * k + i] * A[(size_t)c * k + t];
+            A[(size_t)c * k + i] = v / L[(size_t)i * k + i];
+        }
+    }
+    for (int r = 0; r < k; ++r)   // symmetrize
+        for (int c = r + 1; c < k; ++c) {
+            const double v = 0.5 * (A[(size_t)c * k + r] + A[(size_t)r * k + c]);
+            A[(size_t)c * k + r] = v;
+            A[(size_t)r * k + c] = v;
+        }
+}
+
+// C = L^-T W (back substitution per column)
+__global__ void k_gen_eig_post(const double *L, const double *W, int k, double *C)
+{
+    for (int c = 0; c < k; ++c)
+        for (int i = k - 1; i >= 0; --i) {
+            double v = W[(size_t)c * k + i];
+            for (int t = i + 1; t < k; ++t) v -= L[(size_t)i * k + t] * C[(size_t)c * k + t];
+            C[(size_t)c * k + i] = v / L[(size_t)i * k + i];
+        }
+}
+
 template <typename T>
 static VPtrs<T> make_ptrs(const std::vector<DevBuf *> &v, int n)
 {
@@ -698,7 +776,8 @@ template <typename T>
 static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<double> &vals,
                      std::vector<DevBuf> *vecs)
 {
-    const long long D = s.D();
+    const long long D = s.D();          // dimension
+    const long long Dp = s.Dpad();      // device elements (row pads are zero)
     const int prec = sizeof(T) == 4 ? MO_ED_FP32 : MO_ED_FP64;
     const int kind = sizeof(T) == 4 ? HV_F32 : HV_F64;
     const int nwant = (int)std::min<long long>(nev, D);
@@ -707,8 +786,12 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
     if (ncv < nwant) return fail(ctx, MO_ED_ERR_ARG, "gs_ncv smaller than nev");
     int kkeep = std::min(ncv - 1, nwant + (ncv - nwant) / 2);
     if (kkeep < nwant) kkeep = nwant;
-    const double tol = ctx->opt.gs_tol > 0 ? ctx->opt.gs_tol : (prec == MO_ED_FP32 ? 2e-6 : 1e-11);
-    const size_t vb = sizeof(T) * (size_t)D;
+    // Residual tolerance relative to ||H||.  FP32 vectors carry a noise floor
+    // near eps_32*||H||; the stagnation test below accepts Ritz pairs that
+    // stop improving there.
+    const double tol = ctx->opt.gs_tol > 0 ? ctx->opt.gs_tol : (prec == MO_ED_FP32 ? 1e-7 : 1e-11);
+    std::vector<double> res_hist;
+    const size_t vb = sizeof(T) * (size_t)Dp;
 
     std::vector<DevBuf> store(ncv + 2 + kkeep);
     for (auto &b : store)
@@ -719,7 +802,7 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
     std::vector<DevBuf *> spare(kkeep);
     for (int i = 0; i < kkeep; ++i) spare[i] = &store[ncv + 2 + i];
 
-    const int G = (int)std::max(1LL, std::min((D + kVecThreads - 1) / kVecThreads, (long long)ctx->num_sms * 4));
+    const int G = (int)std::max(1LL, std::min((Dp + kVecThreads - 1) / kVecThreads, (long long)ctx->num_sms * 4));
     const int n2 = ncv + 2;
     DevBuf dHp, dh1, dh2, dpart, dnorm, dbeta, dA, dVj, devals, devecs, dtheta, dsc;
     if (int rc = dev_alloc(ctx, dHp, sizeof(double) * (size_t)n2 * n2)) return rc;
@@ -738,23 +821,27 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
     double *Hp = (double *)dHp.p;
     const int ldh = n2;
 
-    auto hv = [&](const void *x, void *y) -> int { return hv_single(ctx, s, kind, x, y); };
+    long long matvecs = 0;
+    auto hv = [&](const void *x, void *y) -> int {
+        ++matvecs;
+        return hv_single(ctx, s, kind, x, y);
+    };
     auto normalize_into = [&](T *src, DevBuf *dst) -> int {
         // dst = src / ||src||
-        if (int rc = dot_dev(ctx, prec, src, prec, src, D, (double *)dsc.p)) return rc;
+        if (int rc = dot_dev(ctx, prec, src, prec, src, Dp, (double *)dsc.p)) return rc;
         double nrm2;
         MOED_CUDA(ctx, cudaMemcpyAsync(&nrm2, dsc.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
         MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         double inv = nrm2 > 0 ? 1.0 / std::sqrt(nrm2) : 0.0;
         MOED_CUDA(ctx, cudaMemcpyAsync((double *)dsc.p + 1, &inv, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-        k_scale_copy<T><<<G, kVecThreads, 0, ctx->stream>>>(src, (T *)dst->p, D, (double *)dsc.p + 1);
+        k_scale_copy<T><<<G, kVecThreads, 0, ctx->stream>>>(src, (T *)dst->p, Dp, (double *)dsc.p + 1);
         MOED_CHECK_LAUNCH(ctx);
         return MO_ED_OK;
     };
 
     // start vector
     unsigned long long seed = 0x5eedULL + 977ULL * (unsigned)s.ne_up + 131ULL * (unsigned)s.ne_down;
-    k_random<T><<<G, kVecThreads, 0, ctx->stream>>>((T *)W->p, D, seed);
+    k_random<T><<<G, kVecThreads, 0, ctx->stream>>>((T *)W->p, Dp, s.ld(), s.up->n, seed);
     MOED_CHECK_LAUNCH(ctx);
     if (int rc = normalize_into((T *)W->p, V[0])) return rc;
 
@@ -768,7 +855,7 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
         m = ncv;
         for (int j = k; j < ncv; ++j) {
             if (int rc = hv(V[j]->p, W->p)) return rc;
-            if (int rc = orthogonalize<T>(ctx, V, j + 1, (T *)W->p, D, (double *)dh1.p, (double *)dh2.p,
+            if (int rc = orthogonalize<T>(ctx, V, j + 1, (T *)W->p, Dp, (double *)dh1.p, (double *)dh2.p,
                                           (double *)dpart.p, (double *)dnorm.p, G))
                 return rc;
             k_cgs_finish<<<1, 256, 0, ctx->stream>>>((const double *)dh1.p, (const double *)dh2.p, j + 1,
@@ -789,14 +876,15 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
                 // invariant subspace: continue from a fresh random direction
                 double zero = 0.0;
                 MOED_CUDA(ctx, cudaMemcpyAsync(Hp + (size_t)j * ldh + j + 1, &zero, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-                k_random<T><<<G, kVecThreads, 0, ctx->stream>>>((T *)W->p, D, seed + 7919ULL * (cycle * kMaxNcv + j + 1));
+                k_random<T><<<G, kVecThreads, 0, ctx->stream>>>((T *)W->p, Dp, s.ld(), s.up->n,
+                                                                seed + 7919ULL * (cycle * kMaxNcv + j + 1));
                 MOED_CHECK_LAUNCH(ctx);
-                if (int rc = orthogonalize<T>(ctx, V, j + 1, (T *)W->p, D, (double *)dh1.p, (double *)dh2.p,
+                if (int rc = orthogonalize<T>(ctx, V, j + 1, (T *)W->p, Dp, (double *)dh1.p, (double *)dh2.p,
                                               (double *)dpart.p, (double *)dnorm.p, G))
                     return rc;
                 if (int rc = normalize_into((T *)W->p, V[j + 1])) return rc;
             } else {
-                k_scale_copy<T><<<G, kVecThreads, 0, ctx->stream>>>((const T *)W->p, (T *)V[j + 1]->p, D,
+                k_scale_copy<T><<<G, kVecThreads, 0, ctx->stream>>>((const T *)W->p, (T *)V[j + 1]->p, Dp,
                                                                     (double *)dbeta.p + 1);
                 MOED_CHECK_LAUNCH(ctx);
             }
@@ -815,12 +903,18 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
             MOED_CUDA(ctx, cudaMemcpyAsync(&beta_m, Hp + (size_t)(m - 1) * ldh + m, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
         MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         int nconv = 0;
+        double maxres = 0.0;
         for (int i = 0; i < nwant; ++i) {
             double res = std::fabs(beta_m * evecs_h[(size_t)i * m + (m - 1)]);
-            if (res <= tol * std::max(anorm, 1.0)) ++nconv;
-            else break;
+            maxres = std::max(maxres, res);
+            if (res <= tol * std::max(anorm, 1.0) && nconv == i) ++nconv;
         }
-        if (nconv >= nwant || m >= D) {
+        res_hist.push_back(maxres);
+        ctx->diag_res_est = maxres;
+        const size_t h = res_hist.size();
+        const bool stalled = prec == MO_ED_FP32 && h >= 6 && maxres <= 1e-6 * std::max(anorm, 1.0) &&
+                             maxres > 0.9 * res_hist[h - 6];
+        if (nconv >= nwant || m >= D || stalled) {
             done = true;
             break;
         }
@@ -831,7 +925,7 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
             const int nc = std::min(8, kk - c0);
             std::vector<DevBuf *> outs(spare.begin() + c0, spare.begin() + c0 + nc);
             VPtrs<T> X = make_ptrs<T>(outs, nc);
-            k_rotate<T, 8><<<G, kVecThreads, 0, ctx->stream>>>(P, m, (const double *)devecs.p, m, c0, nc, X, D);
+            k_rotate<T, 8><<<G, kVecThreads, 0, ctx->stream>>>(P, m, (const double *)devecs.p, m, c0, nc, X, Dp);
             MOED_CHECK_LAUNCH(ctx);
         }
         for (int i = 0; i < kk; ++i) std::swap(V[i], spare[i]);
@@ -841,12 +935,18 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
     }
     if (!done) return fail(ctx, MO_ED_ERR_NOCONV, "eigensolver did not converge");
 
-    // Ritz vectors and FP64 Rayleigh quotients
+    // Ritz vectors, then an FP64-accurate Rayleigh-Ritz on their span:
+    // P = X^T H X with H applied in FP64 accumulation, S = X^T X (X in the
+    // vector precision), P c = lambda S c.  Eigenvalues of a cluster of
+    // near-degenerate states are then accurate to ~res^2 / (gap to the rest
+    // of the spectrum), whatever the mixing inside the cluster.
     vals.assign(nev, DBL_MAX);
     const int nout = nwant;
-    std::vector<DevBuf> X(nout);
+    std::vector<DevBuf> X(nout), HX(nout);
     for (auto &b : X)
         if (int rc = dev_alloc(ctx, b, vb)) return rc;
+    for (auto &b : HX)
+        if (int rc = dev_alloc(ctx, b, sizeof(double) * (size_t)Dp)) return rc;
     {
         VPtrs<T> P = make_ptrs<T>(V, m);
         for (int c0 = 0; c0 < nout; c0 += 8) {
@@ -854,26 +954,95 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
             std::vector<DevBuf *> outs;
             for (int c = 0; c < nc; ++c) outs.push_back(&X[c0 + c]);
             VPtrs<T> Xp = make_ptrs<T>(outs, nc);
-            k_rotate<T, 8><<<G, kVecThreads, 0, ctx->stream>>>(P, m, (const double *)devecs.p, m, c0, nc, Xp, D);
+            k_rotate<T, 8><<<G, kVecThreads, 0, ctx->stream>>>(P, m, (const double *)devecs.p, m, c0, nc, Xp, Dp);
             MOED_CHECK_LAUNCH(ctx);
         }
     }
-    DevBuf Y;
-    if (int rc = dev_alloc(ctx, Y, sizeof(double) * (size_t)D)) return rc;
+    const int hk = prec == MO_ED_FP32 ? HV_MIXED : HV_F64;
     for (int i = 0; i < nout; ++i) {
-        const int hk = prec == MO_ED_FP32 ? HV_MIXED : HV_F64;
-        if (int rc = hv_single(ctx, s, hk, X[i].p, Y.p)) return rc;
-        if (int rc = dot_dev(ctx, prec, X[i].p, MO_ED_FP64, Y.p, D, (double *)dsc.p)) return rc;
-        if (int rc = dot_dev(ctx, prec, X[i].p, prec, X[i].p, D, (double *)dsc.p + 1)) return rc;
-        double r[2];
-        MOED_CUDA(ctx, cudaMemcpyAsync(r, dsc.p, sizeof(r), cudaMemcpyDeviceToHost, ctx->stream));
-        MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        vals[i] = r[0] / r[1];
+        if (int rc = hv_single(ctx, s, hk, X[i].p, HX[i].p)) return rc;
+        ++matvecs;
     }
+    DevBuf dPS, dRR;
+    if (int rc = dev_alloc(ctx, dPS, sizeof(double) * 2 * (size_t)nout * nout)) return rc;
+    const size_t k2 = (size_t)nout * nout, kp2 = (size_t)(nout + 1) * (nout + 1);
+    if (int rc = dev_alloc(ctx, dRR, sizeof(double) * (4 * k2 + 2 * kp2 + nout + 4))) return rc;
+    double *dP = (double *)dPS.p, *dS = dP + (size_t)nout * nout;
+    for (int i = 0; i < nout; ++i)
+        for (int j = 0; j < nout; ++j) {
+            if (int rc = dot_dev(ctx, prec, X[i].p, MO_ED_FP64, HX[j].p, Dp, dP + (size_t)j * nout + i)) return rc;
+            if (j >= i)
+                if (int rc = dot_dev(ctx, prec, X[i].p, prec, X[j].p, Dp, dS + (size_t)j * nout + i)) return rc;
+        }
+    double *rr = (double *)dRR.p;
+    double *dGA = rr, *dL = dGA + k2, *dW = dL + k2, *dC = dW + k2;
+    double *dJa = dC + k2, *dJv = dJa + kp2;          // Jacobi work (n x n, n = k rounded up to even)
+    double *dEv = dJv + kp2, *dFlag = dEv + nout;
+    k_gen_eig_prep<<<1, 1, 0, ctx->stream>>>(dP, dS, nout, dGA, dL, dFlag);
+    MOED_CHECK_LAUNCH(ctx);
+    k_jacobi<<<1, 256, 0, ctx->stream>>>(dGA, nout, nout, 0, dEv, dJa, dJv, dEv, dW, 60);
+    MOED_CHECK_LAUNCH(ctx);
+    k_gen_eig_post<<<1, 1, 0, ctx->stream>>>(dL, dW, nout, dC);
+    MOED_CHECK_LAUNCH(ctx);
+    std::vector<double> ev(nout);
+    double flag = 0.0;
+    MOED_CUDA(ctx, cudaMemcpyAsync(ev.data(), dEv, sizeof(double) * nout, cudaMemcpyDeviceToHost, ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpyAsync(&flag, dFlag, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (flag != 0.0) return fail(ctx, MO_ED_ERR_NOCONV, "Ritz vectors numerically dependent");
+    // refined vectors X C and their images (H X) C
+    std::vector<DevBuf> X2(nout), HX2(nout);
+    for (auto &b : X2)
+        if (int rc = dev_alloc(ctx, b, vb)) return rc;
+    for (auto &b : HX2)
+        if (int rc = dev_alloc(ctx, b, sizeof(double) * (size_t)Dp)) return rc;
+    {
+        std::vector<DevBuf *> xin, hin;
+        for (int i = 0; i < nout; ++i) {
+            xin.push_back(&X[i]);
+            hin.push_back(&HX[i]);
+        }
+        VPtrs<T> Px = make_ptrs<T>(xin, nout);
+        VPtrs<double> Ph = make_ptrs<double>(hin, nout);
+        for (int c0 = 0; c0 < nout; c0 += 8) {
+            const int nc = std::min(8, nout - c0);
+            std::vector<DevBuf *> ox, oh;
+            for (int c = 0; c < nc; ++c) {
+                ox.push_back(&X2[c0 + c]);
+                oh.push_back(&HX2[c0 + c]);
+            }
+            VPtrs<T> Ox = make_ptrs<T>(ox, nc);
+            VPtrs<double> Oh = make_ptrs<double>(oh, nc);
+            k_rotate<T, 8><<<G, kVecThreads, 0, ctx->stream>>>(Px, nout, dC, nout, c0, nc, Ox, Dp);
+            MOED_CHECK_LAUNCH(ctx);
+            k_rotate<double, 8><<<G, kVecThreads, 0, ctx->stream>>>(Ph, nout, dC, nout, c0, nc, Oh, Dp);
+            MOED_CHECK_LAUNCH(ctx);
+        }
+    }
+    double res_true = 0.0;
+    for (int i = 0; i < nout; ++i) {
+        vals[i] = ev[i];
+        // true residual ||H x - E x|| / ||x|| in FP64
+        double th = ev[i];
+        MOED_CUDA(ctx, cudaMemcpyAsync((double *)dsc.p + 2, &th, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        k_resid_part<T><<<G, kVecThreads, 0, ctx->stream>>>((const T *)X2[i].p, (const double *)HX2[i].p,
+                                                            (const double *)dsc.p + 2, Dp, (double *)dnorm.p);
+        MOED_CHECK_LAUNCH(ctx);
+        k_sum_parts<<<1, kVecThreads, 0, ctx->stream>>>((const double *)dnorm.p, G, (double *)dsc.p + 3);
+        MOED_CHECK_LAUNCH(ctx);
+        if (int rc = dot_dev(ctx, prec, X2[i].p, prec, X2[i].p, Dp, (double *)dsc.p + 1)) return rc;
+        double rr2[3];
+        MOED_CUDA(ctx, cudaMemcpyAsync(rr2, (double *)dsc.p + 1, sizeof(double) * 3, cudaMemcpyDeviceToHost, ctx->stream));
+        MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        res_true = std::max(res_true, std::sqrt(rr2[2] / rr2[0]));
+    }
+    ctx->diag_cycles = cycle + 1;
+    ctx->diag_matvecs = matvecs;
+    ctx->diag_res_true = res_true;
     if (vecs) {
         vecs->clear();
         vecs->resize(nout);
-        for (int i = 0; i < nout; ++i) std::swap((*vecs)[i], X[i]);
+        for (int i = 0; i < nout; ++i) std::swap((*vecs)[i], X2[i]);
     }
     return MO_ED_OK;
 }

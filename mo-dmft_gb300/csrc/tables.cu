@@ -45,8 +45,12 @@ Species::~Species()
     cudaFree(hop_tgt);
     cudaFree(hop_val_d);
     cudaFree(hop_val_f);
+    cudaFree(info);
     cudaFree(diag_d);
     cudaFree(diag_f);
+    cudaFree(tab_f);
+    cudaFree(tab_d);
+    for (auto &kv : items) cudaFree(kv.second);
 }
 
 // ---------------------------------------------------------------------------
@@ -103,11 +107,15 @@ struct CplList {
 // signs (parity of occupied bits below the target bit), ed_operators.F90:292-348.
 // For the down species the reference also counts all up-spin bits below; that
 // parity appears once in each of the two operators and cancels.
-__global__ void k_hops(int n, CplList cpl, const int *words, const int *rank, int *cnt, int *tgt,
-                       double *vd, float *vf, int *max_cnt)
+__global__ void k_hops(int n, int n_pad, int impmask, CplList cpl, const int *words, const int *rank,
+                       int *cnt, int *tgt, double *vd, float *vf, int *info, int *max_cnt)
 {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= n) return;
+    if (r >= n_pad) return;
+    if (r >= n) {             // pad columns: no moves, impurity bits 0
+        info[r] = 0;
+        return;
+    }
     unsigned w = (unsigned)words[r];
     int c = 0;
     for (int i = 0; i < cpl.n; ++i) {
@@ -127,8 +135,10 @@ __global__ void k_hops(int n, CplList cpl, const int *words, const int *rank, in
         unsigned w1 = w & ~(1u << src);
         int s2 = parity_below(w1, dst);
         unsigned w2 = w1 | (1u << dst);
-        double v = cpl.val[i] * (((s1 ^ s2) & 1) ? -1.0 : 1.0);
-        tgt[(size_t)c * n + r] = rank[w2];
+        const int neg = (s1 ^ s2) & 1;
+        double v = cpl.val[i] * (neg ? -1.0 : 1.0);
+        const int t = rank[w2];
+        tgt[(size_t)c * n + r] = t;
         vd[(size_t)c * n + r] = v;
         vf[(size_t)c * n + r] = (float)v;
         ++c;
@@ -139,17 +149,45 @@ __global__ void k_hops(int n, CplList cpl, const int *words, const int *rank, in
         vf[(size_t)i * n + r] = 0.0f;
     }
     cnt[r] = c;
+    info[r] = c | ((int)(w & (unsigned)impmask) << 8);
     atomicMax(max_cnt, c);
+}
+
+// Chunk-major column move tables: entry (c, s, k) = move s of column 4c+k.
+// Slots beyond a column's count (and pad columns) hold (own rank, 0).
+__global__ void k_chunk_tables(int n, int n_pad, int hw, const int *cnt, const int *tgt, const double *vd,
+                               HopEnt<float> *tf, HopEnt<double> *td)
+{
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= (long long)n_pad * hw) return;
+    const int u = (int)(i % n_pad), s = (int)(i / n_pad);
+    const size_t o = ((size_t)(u >> 2) * hw + s) * 4 + (u & 3);
+    int t = u < n ? u : 0;
+    double v = 0.0;
+    if (u < n && s < cnt[u]) {
+        t = tgt[(size_t)s * n + u];
+        v = vd[(size_t)s * n + u];
+    }
+    tf[o].t = t;
+    tf[o].v = (float)v;
+    td[o].t = t;
+    td[o].pad = 0;
+    td[o].v = v;
 }
 
 // Species part of the diagonal: sum_site ek(site) n_site (onsite,
 // ed_operators.F90:68-84) + (U-3J) sum_{i<j} n_i n_j over impurity orbitals
 // (same-spin dens_dens, ed_operators.F90:157-159).
-__global__ void k_species_diag(int n, int nsite, int norb, const int *words, const double *ek,
+__global__ void k_species_diag(int n, int n_pad, int nsite, int norb, const int *words, const double *ek,
                                double Usame, double *dd, float *df)
 {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= n) return;
+    if (r >= n_pad) return;
+    if (r >= n) {
+        dd[r] = 0.0;
+        df[r] = 0.0f;
+        return;
+    }
     unsigned w = (unsigned)words[r];
     double s = 0.0;
     for (int i = 0; i < nsite; ++i)
@@ -261,11 +299,106 @@ int build_model(mo_ed_ctx *ctx)
                     if (i != j && ((Iu >> i) & 1) && ((Id >> j) & 1)) s += ctx->U - 2 * ctx->J;
             m.cross[Iu * m.nimp + Id] = s;
         }
+    for (int I = 0; I < m.nimp; ++I) {
+        unsigned mask = 0;
+        for (int pp = 0; pp < m.npair; ++pp)
+            if (m.t4[pp * m.nimp + I] < 0) mask |= 1u << pp;
+        m.pairmask[I] = mask;
+    }
+    for (int i = 0; i < m.ncpl; ++i) m.cval[i] = ctx->cpl_val[i];
+    // conserved subsystems: connected components of the orbital / bath-level
+    // coupling graph (union-find).  Hybridisation moves keep the electron
+    // count of each subsystem, so rows sorted by those counts form blocks
+    // closed under down-spin moves.
+    {
+        std::vector<int> par(m.nsite);
+        for (int i = 0; i < m.nsite; ++i) par[i] = i;
+        auto find = [&](int a) {
+            while (par[a] != a) a = par[a] = par[par[a]];
+            return a;
+        };
+        for (int i = 0; i < m.ncpl; ++i) par[find(ctx->cpl_orb[i])] = find(ctx->cpl_bath[i]);
+        std::vector<int> id(m.nsite, -1);
+        ctx->site_subsys.assign(m.nsite, 0);
+        int nsub = 0;
+        for (int i = 0; i < m.nsite; ++i) {
+            const int r = find(i);
+            if (id[r] < 0) id[r] = nsub++;
+            ctx->site_subsys[i] = id[r];
+        }
+    }
     if (!ctx->d_mdl) MOED_CUDA(ctx, cudaMalloc(&ctx->d_mdl, sizeof(ModelDev)));
     MOED_CUDA(ctx, cudaMemcpyAsync(ctx->d_mdl, &m, sizeof(m), cudaMemcpyHostToDevice, ctx->stream));
     MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     ctx->species.clear();
     return upload_binom(ctx);
+}
+
+// Row items of a species for R rows per item.  Words sharing their bath bits
+// (a bath group) are consecutive ranks; spin-flip / pair hopping map a row
+// into its own group, so whole groups are kept in one item when they fit.
+// Groups are ordered by the bath-electron counts of the conserved subsystems
+// (down-spin moves change those counts by one), then packed greedily.
+int species_items(mo_ed_ctx *ctx, Species *sp, int R, const int **items, int *nitems)
+{
+    auto it = sp->items.find(R);
+    if (it != sp->items.end()) {
+        *items = it->second;
+        *nitems = sp->nitems[R];
+        return MO_ED_OK;
+    }
+    const int nsite = sp->nsite, N = sp->N, norb = ctx->norb;
+    int nsub = 0;
+    for (int v : ctx->site_subsys) nsub = std::max(nsub, v + 1);
+    struct Group {
+        unsigned long long key;
+        int first, size;
+    };
+    std::vector<Group> groups;
+    int r = 0;
+    unsigned prev = ~0u;
+    for (unsigned w = 0; w < (1u << nsite); ++w) {
+        if (__builtin_popcount(w) != N) continue;
+        const unsigned bath = w >> norb;
+        if (groups.empty() || bath != prev) {
+            unsigned long long k = 0;
+            for (int sub = 0; sub < nsub; ++sub) {
+                int c = 0;
+                for (int i = norb; i < nsite; ++i)
+                    if (((w >> i) & 1) && ctx->site_subsys[i] == sub) ++c;
+                k = k * 16 + (unsigned)c;
+            }
+            groups.push_back({k, r, 0});
+            prev = bath;
+        }
+        groups.back().size++;
+        ++r;
+    }
+    std::stable_sort(groups.begin(), groups.end(),
+                     [](const Group &a, const Group &b) { return a.key < b.key; });
+    std::vector<int> tab;
+    int fill = R;
+    for (const Group &g : groups) {
+        for (int off = 0; off < g.size; off += R) {       // a group larger than R is split
+            const int len = std::min(R, g.size - off);
+            if (fill + len > R) {
+                tab.insert(tab.end(), R, -1);
+                fill = 0;
+            }
+            for (int i = 0; i < len; ++i) tab[tab.size() - R + fill + i] = g.first + off + i;
+            fill += len;
+        }
+    }
+    const int n_items = (int)(tab.size() / R);
+    int *d = nullptr;
+    MOED_CUDA(ctx, cudaMalloc(&d, sizeof(int) * std::max<size_t>(1, tab.size())));
+    MOED_CUDA(ctx, cudaMemcpyAsync(d, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice, ctx->stream));
+    MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    sp->items[R] = d;
+    sp->nitems[R] = n_items;
+    *items = d;
+    *nitems = n_items;
+    return MO_ED_OK;
 }
 
 int get_species(mo_ed_ctx *ctx, int N, Species **out)
@@ -280,8 +413,9 @@ int get_species(mo_ed_ctx *ctx, int N, Species **out)
     s->nsite = nsite;
     s->N = N;
     s->n = (int)binom(nsite, N);
+    s->n_pad = (s->n + 31) / 32 * 32;
     s->hw = std::max(ctx->mdl.ncpl, 1);
-    const int n = s->n;
+    const int n = s->n, np = s->n_pad;
     const size_t nh = (size_t)n * s->hw;
     MOED_CUDA(ctx, cudaMalloc(&s->words, sizeof(int) * n));
     MOED_CUDA(ctx, cudaMalloc(&s->rank, sizeof(int) << nsite));
@@ -289,8 +423,11 @@ int get_species(mo_ed_ctx *ctx, int N, Species **out)
     MOED_CUDA(ctx, cudaMalloc(&s->hop_tgt, sizeof(int) * nh));
     MOED_CUDA(ctx, cudaMalloc(&s->hop_val_d, sizeof(double) * nh));
     MOED_CUDA(ctx, cudaMalloc(&s->hop_val_f, sizeof(float) * nh));
-    MOED_CUDA(ctx, cudaMalloc(&s->diag_d, sizeof(double) * n));
-    MOED_CUDA(ctx, cudaMalloc(&s->diag_f, sizeof(float) * n));
+    MOED_CUDA(ctx, cudaMalloc(&s->tab_f, sizeof(HopEnt<float>) * (size_t)np * s->hw));
+    MOED_CUDA(ctx, cudaMalloc(&s->tab_d, sizeof(HopEnt<double>) * (size_t)np * s->hw));
+    MOED_CUDA(ctx, cudaMalloc(&s->info, sizeof(int) * np));
+    MOED_CUDA(ctx, cudaMalloc(&s->diag_d, sizeof(double) * np));
+    MOED_CUDA(ctx, cudaMalloc(&s->diag_f, sizeof(float) * np));
 
     const int T = 256;
     k_unrank<<<(n + T - 1) / T, T, 0, ctx->stream>>>(nsite, N, n, s->words);
@@ -312,22 +449,31 @@ int get_species(mo_ed_ctx *ctx, int N, Species **out)
     MOED_CUDA(ctx, cudaMemsetAsync(dmax.p, 0, sizeof(int), ctx->stream));
     MOED_CUDA(ctx, cudaMemcpyAsync(dek.p, ctx->ek.data(), sizeof(double) * nsite,
                                    cudaMemcpyHostToDevice, ctx->stream));
-    if (cl.n > 0) {
-        k_hops<<<(n + T - 1) / T, T, 0, ctx->stream>>>(n, cl, s->words, s->rank, s->hop_cnt,
-                                                       s->hop_tgt, s->hop_val_d, s->hop_val_f,
-                                                       (int *)dmax.p);
-        MOED_CHECK_LAUNCH(ctx);
-    } else {
+    if (cl.n == 0) {
         MOED_CUDA(ctx, cudaMemsetAsync(s->hop_cnt, 0, sizeof(int) * n, ctx->stream));
         MOED_CUDA(ctx, cudaMemsetAsync(s->hop_tgt, 0, sizeof(int) * nh, ctx->stream));
         MOED_CUDA(ctx, cudaMemsetAsync(s->hop_val_d, 0, sizeof(double) * nh, ctx->stream));
         MOED_CUDA(ctx, cudaMemsetAsync(s->hop_val_f, 0, sizeof(float) * nh, ctx->stream));
     }
-    k_species_diag<<<(n + T - 1) / T, T, 0, ctx->stream>>>(n, nsite, ctx->norb, s->words,
-                                                           (const double *)dek.p,
-                                                           ctx->U - 3 * ctx->J, s->diag_d,
-                                                           s->diag_f);
+    k_hops<<<(np + T - 1) / T, T, 0, ctx->stream>>>(n, np, ctx->mdl.nimp - 1, cl, s->words, s->rank,
+                                                    s->hop_cnt, s->hop_tgt, s->hop_val_d, s->hop_val_f,
+                                                    s->info, (int *)dmax.p);
     MOED_CHECK_LAUNCH(ctx);
+    {
+        const long long tot = (long long)np * s->hw;
+        k_chunk_tables<<<(unsigned)((tot + T - 1) / T), T, 0, ctx->stream>>>(n, np, s->hw, s->hop_cnt, s->hop_tgt,
+                                                                             s->hop_val_d, s->tab_f, s->tab_d);
+        MOED_CHECK_LAUNCH(ctx);
+    }
+    k_species_diag<<<(np + T - 1) / T, T, 0, ctx->stream>>>(n, np, nsite, ctx->norb, s->words,
+                                                            (const double *)dek.p, ctx->U - 3 * ctx->J,
+                                                            s->diag_d, s->diag_f);
+    MOED_CHECK_LAUNCH(ctx);
+    {   // largest bath group (words sharing their bath bits)
+        std::map<unsigned, int> gs;
+        for (unsigned w = 0; w < (1u << nsite); ++w)
+            if (__builtin_popcount(w) == N) s->max_group = std::max(s->max_group, ++gs[w >> ctx->norb]);
+    }
     MOED_CUDA(ctx, cudaMemcpyAsync(&s->max_cnt, dmax.p, sizeof(int), cudaMemcpyDeviceToHost,
                                    ctx->stream));
     MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

@@ -73,6 +73,7 @@ SIGNATURES = [
     ("mo_ed_set_omega", C.c_int, [C.c_void_p, C.c_int, _dp]),
     ("mo_ed_icom", C.c_longlong, [C.c_int, C.c_int]),
     ("mo_ed_sector_dims", C.c_int, [C.c_void_p, C.c_int, C.c_int, _ip, _ip, _llp]),
+    ("mo_ed_vector_layout", C.c_int, [C.c_void_p, C.c_int, C.c_int, _ip, _llp]),
     ("mo_ed_generate_basis", C.c_int, [C.c_void_p, C.c_int, C.c_int, _ip, _ip, _ip, _ip]),
     ("mo_ed_basis_get", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_longlong, _llp, _up]),
     ("mo_ed_basis_idx", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_longlong, _up, _llp]),
@@ -84,6 +85,7 @@ SIGNATURES = [
                                 C.c_longlong, _llp]),
     ("mo_ed_lanczos_iteration", C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _ip, _dp, _dp]),
     ("mo_ed_diag", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _dp]),
+    ("mo_ed_diag_stats", C.c_int, [C.c_void_p, _ip, _llp, _dp, _dp]),
     ("mo_ed_solve", C.c_int, [C.c_void_p, _ip, _dp, _dp, _ip, _ip, C.c_int]),
     ("mo_ed_calc_green_ftn", C.c_int, [C.c_void_p, _dp]),
     ("mo_ed_green_coeffs", C.c_int, [C.c_void_p, _ip, _ip, _dp, C.c_int]),
@@ -232,6 +234,12 @@ class EDSolver:
         self._chk(lib().mo_ed_sector_dims(self._ctx, ne_up, ne_down, C.byref(a), C.byref(b), C.byref(n)))
         return a.value, b.value, n.value
 
+    def vector_layout(self, ne_up, ne_down):
+        """(ld, nelem) of the device layout: ndown rows of stride ld (zero pads)."""
+        ld, n = C.c_int(), C.c_longlong()
+        self._chk(lib().mo_ed_vector_layout(self._ctx, ne_up, ne_down, C.byref(ld), C.byref(n)))
+        return ld.value, n.value
+
     def generate_basis(self, ne_up, ne_down):
         nup, ndn, _ = self.sector_dims(ne_up, ne_down)
         nw = 1 << self.nsite
@@ -272,7 +280,7 @@ class EDSolver:
         return B
 
     def multiply_H_dev(self, ne_up, ne_down, dA, dB, dtype=FP32):
-        """Device pointers (ints); no synchronization."""
+        """Device pointers (ints) in the device layout (vector_layout); no synchronization."""
         self._chk(lib().mo_ed_multiply_h_dev(self._ctx, ne_up, ne_down, dtype, C.c_void_p(dA), C.c_void_p(dB)))
 
     def multiply_H_mixed_dev(self, ne_up, ne_down, dA, dB):
@@ -307,6 +315,12 @@ class EDSolver:
         self._chk(lib().mo_ed_diag(self._ctx, ne_up, ne_down, nev, _d(ev),
                                    _d(vec) if vectors else _dp()))
         return ev, (vec.T.copy() if vectors else None)
+
+    def diag_stats(self):
+        """(cycles, matvecs, residual estimate, FP64 true residual) of the last eigensolve."""
+        c, m, a, b = C.c_int(), C.c_longlong(), C.c_double(), C.c_double()
+        self._chk(lib().mo_ed_diag_stats(self._ctx, C.byref(c), C.byref(m), C.byref(a), C.byref(b)))
+        return dict(cycles=c.value, matvecs=m.value, res_est=a.value, res_true=b.value)
 
     def ed_solve(self):
         """ed_solver.F90:28 -> list of eigval_t dicts (val, prob, sector, level; 1-based)."""

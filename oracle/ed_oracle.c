@@ -350,6 +350,19 @@ void or_multiply_H_omp(const or_model *m, const or_basis *b, const double *A, do
 #endif
 }
 
+void or_multiply_H_rows(const or_model *m, const or_basis *b, const double *A, double *B,
+                        int64_t row0, int64_t row1, int nthreads)
+{
+#ifdef _OPENMP
+    int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#pragma omp parallel for schedule(static) num_threads(nt)
+    for (int64_t i = row0 + 1; i <= row1; ++i) B[i - 1] = multiply_H_row(m, b, A, i);
+#else
+    (void)nthreads;
+    for (int64_t i = row0 + 1; i <= row1; ++i) B[i - 1] = multiply_H_row(m, b, A, i);
+#endif
+}
+
 int or_dense_H(const or_model *m, const or_basis *b, double *Hd)
 {
     int64_t n = b->ntot;

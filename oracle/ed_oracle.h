@@ -70,6 +70,10 @@ void or_multiply_H(const or_model *m, const or_basis *b, const double *A, double
  * split of ed_basis.F90:52-62 on one node).  nthreads <= 0: all cores. */
 void or_multiply_H_omp(const or_model *m, const or_basis *b, const double *A,
                        double *B, int nthreads);
+/* Rows [row0, row1) (0-based) of B = H*A with nthreads OpenMP threads: a
+ * bounded sample of one H*v for the CPU baseline. */
+void or_multiply_H_rows(const or_model *m, const or_basis *b, const double *A, double *B,
+                        int64_t row0, int64_t row1, int nthreads);
 /* Dense H of the sector (row-major ntot x ntot), built column by column
  * with or_multiply_H; for small sectors only. */
 int or_dense_H(const or_model *m, const or_basis *b, double *Hd);

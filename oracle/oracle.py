@@ -70,6 +70,8 @@ def lib():
             getattr(L, f).argtypes = [C.c_uint32, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_uint32)]
         L.or_multiply_H.argtypes = [C.POINTER(_Model), C.POINTER(_Basis), _dp, _dp]
         L.or_multiply_H_omp.argtypes = [C.POINTER(_Model), C.POINTER(_Basis), _dp, _dp, C.c_int]
+        L.or_multiply_H_rows.argtypes = [C.POINTER(_Model), C.POINTER(_Basis), _dp, _dp, C.c_int64,
+                                         C.c_int64, C.c_int]
         L.or_dense_H.argtypes = [C.POINTER(_Model), C.POINTER(_Basis), _dp]
         L.or_apply_c.argtypes = [C.POINTER(_Model), C.POINTER(_Basis), _dp, C.c_int, C.c_int,
                                  C.c_int, C.POINTER(_Basis), C.POINTER(_dp)]
@@ -167,6 +169,12 @@ def multiply_H(model: Model, basis: Basis, A, nthreads=0):
     m = model.c()
     lib().or_multiply_H_omp(C.byref(m), C.byref(basis.c), _d(A), _d(B), nthreads)
     return B
+
+
+def multiply_H_rows(model: Model, basis: Basis, A, B, row0, row1, nthreads=0):
+    """B[row0:row1] = (H*A)[row0:row1] (in place)."""
+    m = model.c()
+    lib().or_multiply_H_rows(C.byref(m), C.byref(basis.c), _d(A), _d(B), row0, row1, nthreads)
 
 
 def dense_H(model: Model, basis: Basis):
