@@ -258,6 +258,7 @@ def run_ours(args):
     assert np.array_equal(yn, y[:, :nu_].reshape(-1).cpu().numpy()), "e2e result differs from the device path"
 
 
+    tuning, chosen = s.hv_tuning(nup, ndn, pkg.FP32)
     lg = None
     if rank == 0 and not args.no_lanczos_g:
         lg = lanczos_g(pkg, args.lg_config, args.lg_nev)
@@ -280,6 +281,8 @@ def run_ours(args):
                     "h2d_bytes_per_step": D * 4, "d2h_bytes_per_step": D * 4,
                     "ms_per_step": round(t_e2e * 1e3, 4)},
             "gpu_launches": launches,
+            "hv_autotune": {"variants": [{"rows_per_item": v[0][0], "threads": v[0][1], "ctas_per_sm": v[0][2],
+                                          "ms": round(v[1], 4)} for v in tuning], "chosen": chosen},
             "clocks": clocks,
             "lanczos_g": lg,
         }

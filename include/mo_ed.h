@@ -134,6 +134,15 @@ int mo_ed_multiply_h_dev(mo_ed_ctx *ctx, int ne_up, int ne_down, int dtype, cons
 int mo_ed_multiply_h_mixed_dev(mo_ed_ctx *ctx, int ne_up, int ne_down, const float *dA,
                                double *dB);
 
+/* H*v tile-shape autotuner of a sector (no reference counterpart: the
+ * reference has one CPU loop).  The first H*v of each (precision, Nup, Ndn)
+ * times every variant on that sector and keeps the fastest; this call runs
+ * the tuning if needed and reports *nvariant variants: shape[3*i..3*i+2] =
+ * (rows per item, threads per CTA, CTAs per SM), ms[i] (negative: does not
+ * fit), and the *chosen index.  Arrays hold capacity variants. */
+int mo_ed_hv_tuning(mo_ed_ctx *ctx, int ne_up, int ne_down, int dtype, int capacity, int *nvariant,
+                    int *shape, float *ms, int *chosen);
+
 /* ---- a11: apply_c (ed_operators.F90:10-61) ------------------------------ */
 /* vec_out = c^dagger_(iorb,ispin) vec (pm = 1) or c_(iorb,ispin) vec (pm = 2).
  * The reference allocates vec_out; here the caller passes its capacity

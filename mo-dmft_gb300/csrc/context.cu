@@ -348,6 +348,17 @@ int mo_ed_multiply_h_mixed_dev(mo_ed_ctx *ctx, int ne_up, int ne_down, const flo
     return hv_single(ctx, s, HV_MIXED, dA, dB);
 }
 
+int mo_ed_hv_tuning(mo_ed_ctx *ctx, int ne_up, int ne_down, int dtype, int capacity, int *nvariant,
+                    int *shape, float *ms, int *chosen)
+{
+    CTX_CHECK(ctx);
+    if (!nvariant || !chosen || (dtype != MO_ED_FP32 && dtype != MO_ED_FP64))
+        return fail(ctx, MO_ED_ERR_ARG, "bad arguments");
+    Sector s;
+    if (int rc = get_sector(ctx, ne_up, ne_down, &s)) return rc;
+    return hv_tuning(ctx, s, dtype == MO_ED_FP32 ? HV_F32 : HV_F64, capacity, nvariant, shape, ms, chosen);
+}
+
 int mo_ed_apply_c(mo_ed_ctx *ctx, int ne_up, int ne_down, const double *vec, int pm, int iorb,
                   int ispin, double *vec_out, long long capacity, long long *ntot_out)
 {

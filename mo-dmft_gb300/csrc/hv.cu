@@ -54,6 +54,18 @@ struct alignas(8) RowVec {
     T v[R];
 };
 
+// Spin-flip / pair-hop terms of one (row, column impurity pattern) pair: at
+// most 2 for up to three orbitals.  Term t reads the staged partner row
+// src[t] at column u + du[t] with coefficient c[t] (+-J with both transfer
+// signs folded in).
+template <typename TA>
+struct alignas(16) Quad {
+    int cnt;
+    signed char du[2];
+    unsigned char src[2];
+    TA c[2];
+};
+
 template <typename T>
 __device__ __forceinline__ Vec4<T> ldg4(const T *p)
 {
@@ -128,15 +140,19 @@ k_hv(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict__ mdl
     int *s_t4 = reinterpret_cast<int *>(s_cross + nimp * nimp);
 
     __shared__ unsigned s_pmask[kMaxImp];
+    __shared__ RowVec<TA, R> s_crossT[kMaxImp];   // per item: cross[iu][id_r] for the R rows
     __shared__ int s_d[R], s_id[R], s_dcnt[R];
     __shared__ TA s_ddiag[R];
     __shared__ int s_dtgt[R][kMaxHop];
     __shared__ TA s_dval[R][kMaxHop];
     // per (row, pair): spin-flip / pair-hop partner as an item slot (>= 0) or
     // as -(1 + global row) when the partner row is not staged, and the
-    // coefficient +-J; s_rowmask[p]: bit r spin-flip valid, bit 16+r pair hop
-    __shared__ unsigned s_rowmask[kMaxPair];
+    // coefficient +-J; s_sfm[r] / s_phm[r]: pairs valid for row r
+    __shared__ unsigned s_sfm[R], s_phm[R];
+    __shared__ unsigned s_rowmask[kMaxPair];   // generic path: bit r spin-flip, bit 16+r pair hop
     __shared__ unsigned s_itemmask;
+    __shared__ Quad<TA> s_q[R * kMaxImp];      // fast path table
+    __shared__ int s_slow;                     // 1: an item needs the generic path
     __shared__ int s_sfsrc[R][kMaxPair], s_phsrc[R][kMaxPair];
     __shared__ TA s_sfc[R][kMaxPair], s_phc[R][kMaxPair];
     __shared__ double s_red[NT / 32];
@@ -173,10 +189,19 @@ k_hv(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict__ mdl
                 s_dcnt[r] = 0;
                 s_ddiag[r] = TA(0);
             }
+            s_sfm[r] = 0u;
+            s_phm[r] = 0u;
         }
         for (int p = tid; p < kMaxPair; p += NT) s_rowmask[p] = 0u;
-        if (tid == 0) s_itemmask = 0u;
+        if (tid == 0) {
+            s_itemmask = 0u;
+            s_slow = 0;
+        }
         __syncthreads();
+        for (int i = tid; i < nimp * R; i += NT) {
+            const int iu = i / R, r = i - iu * R;
+            s_crossT[iu].v[r] = s_cross[iu * nimp + s_id[r]];
+        }
         for (int i = tid; i < R * jb.dn_maxcnt; i += NT) {
             const int r = i / jb.dn_maxcnt, s = i - r * jb.dn_maxcnt;
             if (s < s_dcnt[r]) {
@@ -191,19 +216,65 @@ k_hv(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict__ mdl
                 const int eph = s_t4[p * nimp + s_id[r]];                  // pair hop:  T_{i<-j}(d)
                 if (esf < 0) {
                     const int off = (int)(short)(esf & 0xffff), dp = s_d[r] + off, rp = r + off;
-                    s_sfsrc[r][p] = (rp >= 0 && rp < R && s_d[rp] == dp) ? rp : -(1 + dp);
+                    const bool local = rp >= 0 && rp < R && s_d[rp] == dp;
+                    s_sfsrc[r][p] = local ? rp : -(1 + dp);
                     s_sfc[r][p] = (esf & 0x40000000) ? -Jc : Jc;
+                    atomicOr(&s_sfm[r], 1u << p);
                     atomicOr(&s_rowmask[p], 1u << r);
                     atomicOr(&s_itemmask, 1u << p);
+                    if (!local) s_slow = 1;
                 }
                 if (eph < 0) {
                     const int off = (int)(short)(eph & 0xffff), dp = s_d[r] + off, rp = r + off;
-                    s_phsrc[r][p] = (rp >= 0 && rp < R && s_d[rp] == dp) ? rp : -(1 + dp);
+                    const bool local = rp >= 0 && rp < R && s_d[rp] == dp;
+                    s_phsrc[r][p] = local ? rp : -(1 + dp);
                     s_phc[r][p] = (eph & 0x40000000) ? -Jc : Jc;
+                    atomicOr(&s_phm[r], 1u << p);
                     atomicOr(&s_rowmask[p], 1u << (16 + r));
                     atomicOr(&s_itemmask, 1u << p);
+                    if (!local) s_slow = 1;
                 }
             }
+        }
+        __syncthreads();
+        // fast-path table: terms of every (row, column impurity pattern)
+        for (int i = tid; i < R * nimp; i += NT) {
+            const int r = i / nimp, iu = i - r * nimp;
+            Quad<TA> q;
+            q.cnt = 0;
+#pragma unroll
+            for (int t = 0; t < 2; ++t) {
+                q.du[t] = 0;
+                q.src[t] = 0;
+                q.c[t] = TA(0);
+            }
+            if (s_d[r] >= 0) {
+                for (int p = 0; p < npair; ++p) {
+                    const int e = s_t4[p * nimp + iu];
+                    if (e >= 0) continue;
+                    const int du = (int)(short)(e & 0xffff);
+                    const TA tu = (e & 0x40000000) ? TA(-1) : TA(1);
+                    if ((s_sfm[r] >> p) & 1u) {
+                        if (q.cnt == 2) s_slow = 1;
+                        else {
+                            q.du[q.cnt] = (signed char)du;
+                            q.src[q.cnt] = (unsigned char)max(s_sfsrc[r][p], 0);
+                            q.c[q.cnt] = tu * s_sfc[r][p];
+                            ++q.cnt;
+                        }
+                    }
+                    if ((s_phm[r] >> p) & 1u) {
+                        if (q.cnt == 2) s_slow = 1;
+                        else {
+                            q.du[q.cnt] = (signed char)du;
+                            q.src[q.cnt] = (unsigned char)max(s_phsrc[r][p], 0);
+                            q.c[q.cnt] = tu * s_phc[r][p];
+                            ++q.cnt;
+                        }
+                    }
+                }
+            }
+            s_q[i] = q;
         }
         // stage the rows, transposed (pad rows staged as zeros)
         for (int c = tid; c < nchunk; c += NT) {
@@ -228,6 +299,15 @@ k_hv(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict__ mdl
         }
         __syncthreads();
 
+        // item-uniform row data in registers
+        TA ddiag[R];
+        bool live[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            ddiag[r] = s_ddiag[r];
+            live[r] = s_d[r] >= 0;
+        }
+        const bool slow = s_slow != 0;
         const unsigned imask = s_itemmask;
         double dacc = 0.0;
         for (int c = tid; c < nchunk; c += NT) {
@@ -246,10 +326,11 @@ k_hv(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict__ mdl
                 cnt[k] = inf[k] & 0xff;
                 maxc = max(maxc, cnt[k]);
                 const RowVec<TX, R> sx = S[u0 + k];
+                const RowVec<TA, R> cr = s_crossT[iu[k]];
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
                     xs[k][r] = sx.v[r];
-                    acc[k][r] = (ud.v[k] + s_ddiag[r] + s_cross[iu[k] * nimp + s_id[r]]) * (TA)sx.v[r];
+                    acc[k][r] = (ud.v[k] + ddiag[r] + cr.v[r]) * (TA)sx.v[r];
                 }
             }
             // up-spin hybridisation: shared-memory gathers, all rows at once
@@ -278,32 +359,46 @@ k_hv(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict__ mdl
                     for (int k = 0; k < 4; ++k) acc[k][r] += v * (TA)g.v[k];
                 }
             }
-            // spin-flip and pair hopping: pairs valid for this column and for
-            // some row of the item; partner rows read from the stage
+            // spin-flip and pair hopping (partner rows are in the stage)
+            if (!slow) {
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                unsigned pm = s_pmask[iu[k]] & imask;
-                while (pm) {
-                    const int p = __ffs(pm) - 1;
-                    pm &= pm - 1;
-                    const int e = s_t4[p * nimp + iu[k]];
-                    const int uu = u0 + k + (int)(short)(e & 0xffff);
-                    const bool neg = (e & 0x40000000) != 0;
-                    const unsigned rm = s_rowmask[p];
-                    const TX *su = reinterpret_cast<const TX *>(&S[uu]);
+                for (int k = 0; k < 4; ++k) {
 #pragma unroll
                     for (int r = 0; r < R; ++r) {
-                        if ((rm >> r) & 1u) {
-                            const int src = s_sfsrc[r][p];
-                            const TX xv = src >= 0 ? su[src] : __ldg(x + (size_t)(-1 - src) * ld + uu);
-                            const TA cf = neg ? -s_sfc[r][p] : s_sfc[r][p];
-                            acc[k][r] += cf * (TA)xv;
-                        }
-                        if ((rm >> (16 + r)) & 1u) {
-                            const int src = s_phsrc[r][p];
-                            const TX xv = src >= 0 ? su[src] : __ldg(x + (size_t)(-1 - src) * ld + uu);
-                            const TA cf = neg ? -s_phc[r][p] : s_phc[r][p];
-                            acc[k][r] += cf * (TA)xv;
+                        const Quad<TA> q = s_q[r * nimp + iu[k]];
+#pragma unroll
+                        for (int t = 0; t < 2; ++t)
+                            if (t < q.cnt)
+                                acc[k][r] += q.c[t] * (TA)reinterpret_cast<const TX *>(&S[u0 + k + q.du[t]])[q.src[t]];
+                    }
+                }
+            } else {
+                // generic: pairs valid for this column and for some row of the item
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    unsigned pm = s_pmask[iu[k]] & imask;
+                    while (pm) {
+                        const int p = __ffs(pm) - 1;
+                        pm &= pm - 1;
+                        const int e = s_t4[p * nimp + iu[k]];
+                        const int uu = u0 + k + (int)(short)(e & 0xffff);
+                        const bool neg = (e & 0x40000000) != 0;
+                        const unsigned rm = s_rowmask[p];
+                        const TX *su = reinterpret_cast<const TX *>(&S[uu]);
+#pragma unroll
+                        for (int r = 0; r < R; ++r) {
+                            if ((rm >> r) & 1u) {
+                                const int src = s_sfsrc[r][p];
+                                const TX xv = src >= 0 ? su[src] : __ldg(x + (size_t)(-1 - src) * ld + uu);
+                                const TA cf = neg ? -s_sfc[r][p] : s_sfc[r][p];
+                                acc[k][r] += cf * (TA)xv;
+                            }
+                            if ((rm >> (16 + r)) & 1u) {
+                                const int src = s_phsrc[r][p];
+                                const TX xv = src >= 0 ? su[src] : __ldg(x + (size_t)(-1 - src) * ld + uu);
+                                const TA cf = neg ? -s_phc[r][p] : s_phc[r][p];
+                                acc[k][r] += cf * (TA)xv;
+                            }
                         }
                     }
                 }
@@ -311,7 +406,7 @@ k_hv(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict__ mdl
             TA part = TA(0);
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                if (s_d[r] >= 0) {
+                if (live[r]) {
                     TY o[4];
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
@@ -343,13 +438,30 @@ static size_t dyn_smem_bytes(int ld, const ModelDev &m)
            sizeof(int) * (size_t)m.npair * m.nimp;
 }
 
-// rows per item: FP32 vectors R = 6 (two 3-row bath groups of a 3-orbital
-// impurity), FP64 / mixed R = 3
-int hv_rows_per_item(int kind) { return kind == HV_F32 ? 6 : 3; }
+// ---------------------------------------------------------------------------
+// tile-shape variants and the autotuner
+// ---------------------------------------------------------------------------
+// A variant fixes the rows per item R, the CTA size NT and the CTAs per SM the
+// register budget is cut for (MINB).  All variants compute every element with
+// the same sequence of operations, so their outputs are bit-identical; only
+// the speed differs.  The first H*v of a (kind, Nup, Ndn) shape times each
+// variant on that sector (scratch vectors, CUDA events on the context stream)
+// and keeps the fastest.
+struct HvVariant {
+    int R, NT, MINB;
+};
+static const HvVariant kVarF32[] = {{3, 512, 2}, {4, 256, 2}, {6, 512, 1}, {3, 256, 3}};
+static const HvVariant kVarF64[] = {{2, 256, 2}, {3, 256, 1}, {2, 512, 1}};
+static const int kNVarF32 = sizeof(kVarF32) / sizeof(kVarF32[0]);
+static const int kNVarF64 = sizeof(kVarF64) / sizeof(kVarF64[0]);
+
+static const HvVariant &variant(int kind, int v) { return kind == HV_F32 ? kVarF32[v] : kVarF64[v]; }
+static int nvariants(int kind) { return kind == HV_F32 ? kNVarF32 : kNVarF64; }
+
+static long long shape_key(int kind, const Sector &s) { return ((long long)kind << 32) | (s.ne_up << 16) | s.ne_down; }
 
 template <typename TA>
-void hv_fill_job(const mo_ed_ctx *ctx, const Sector &s, int kind, const void *x, void *y,
-                 HvJobT<TA> &j)
+void hv_fill_job(const mo_ed_ctx *ctx, const Sector &s, int R, const void *x, void *y, HvJobT<TA> &j)
 {
     const bool f32 = sizeof(TA) == 4;
     (void)ctx;
@@ -360,7 +472,6 @@ void hv_fill_job(const mo_ed_ctx *ctx, const Sector &s, int kind, const void *x,
     j.nu = s.up->n;
     j.nd = s.dn->n;
     j.ld = s.ld();
-    const int R = hv_rows_per_item(kind);
     auto it = s.dn->items.find(R);
     j.items = it != s.dn->items.end() ? it->second : nullptr;
     j.nitems = it != s.dn->items.end() ? s.dn->nitems.at(R) : 0;
@@ -377,10 +488,8 @@ void hv_fill_job(const mo_ed_ctx *ctx, const Sector &s, int kind, const void *x,
     j.dn_maxcnt = s.dn->max_cnt;
     j.pad = 0;
 }
-template void hv_fill_job<float>(const mo_ed_ctx *, const Sector &, int, const void *, void *,
-                                 HvJobT<float> &);
-template void hv_fill_job<double>(const mo_ed_ctx *, const Sector &, int, const void *, void *,
-                                  HvJobT<double> &);
+template void hv_fill_job<float>(const mo_ed_ctx *, const Sector &, int, const void *, void *, HvJobT<float> &);
+template void hv_fill_job<double>(const mo_ed_ctx *, const Sector &, int, const void *, void *, HvJobT<double> &);
 
 template <typename TX, typename TA, typename TY, int R, int NT, int MINB>
 static int launch_batch(mo_ed_ctx *ctx, const HvBatch<TA> &b)
@@ -394,6 +503,7 @@ static int launch_batch(mo_ed_ctx *ctx, const HvBatch<TA> &b)
     const size_t smem = dyn_smem_bytes<TX, TA, R>(ldmax, ctx->mdl);
     auto kern = k_hv<TX, TA, TY, R, NT, MINB>;
     MOED_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MOED_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     int per_sm = 0;
     MOED_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem));
     if (per_sm < 1) return fail(ctx, MO_ED_ERR_ARG, "sector rows too long for the shared-memory stage");
@@ -404,26 +514,40 @@ static int launch_batch(mo_ed_ctx *ctx, const HvBatch<TA> &b)
 }
 
 template <typename TA>
-static int launch_kind(mo_ed_ctx *ctx, int kind, const HvBatch<TA> &b)
+static int launch_variant(mo_ed_ctx *ctx, int kind, int v, const HvBatch<TA> &b)
 {
     if constexpr (sizeof(TA) == 4) {
         (void)kind;
-        return launch_batch<float, float, float, 6, 512, 1>(ctx, b);
+        switch (v) {
+        case 0: return launch_batch<float, float, float, 3, 512, 2>(ctx, b);
+        case 1: return launch_batch<float, float, float, 4, 256, 2>(ctx, b);
+        case 2: return launch_batch<float, float, float, 6, 512, 1>(ctx, b);
+        default: return launch_batch<float, float, float, 3, 256, 3>(ctx, b);
+        }
+    } else if (kind == HV_F64) {
+        switch (v) {
+        case 0: return launch_batch<double, double, double, 2, 256, 2>(ctx, b);
+        case 1: return launch_batch<double, double, double, 3, 256, 1>(ctx, b);
+        default: return launch_batch<double, double, double, 2, 512, 1>(ctx, b);
+        }
     } else {
-        if (kind == HV_F64) return launch_batch<double, double, double, 3, 256, 1>(ctx, b);
-        return launch_batch<float, double, double, 3, 256, 1>(ctx, b);
+        switch (v) {
+        case 0: return launch_batch<float, double, double, 2, 256, 2>(ctx, b);
+        case 1: return launch_batch<float, double, double, 3, 256, 1>(ctx, b);
+        default: return launch_batch<float, double, double, 2, 512, 1>(ctx, b);
+        }
     }
 }
 
 template <typename TA>
-static int hv_run_jobs(mo_ed_ctx *ctx, int kind, const HvJobT<TA> *jobs, int njobs)
+static int hv_run_jobs(mo_ed_ctx *ctx, int kind, int v, const HvJobT<TA> *jobs, int njobs)
 {
     HvBatch<TA> b;
     b.njobs = 0;
     b.total_items = 0;
     for (int i = 0; i < njobs; ++i) {
         if (b.njobs == kMaxJobs) {
-            if (int rc = launch_kind<TA>(ctx, kind, b)) return rc;
+            if (int rc = launch_variant<TA>(ctx, kind, v, b)) return rc;
             b.njobs = 0;
             b.total_items = 0;
         }
@@ -433,36 +557,128 @@ static int hv_run_jobs(mo_ed_ctx *ctx, int kind, const HvJobT<TA> *jobs, int njo
         b.njobs++;
     }
     if (b.njobs == 0) return MO_ED_OK;
-    return launch_kind<TA>(ctx, kind, b);
+    return launch_variant<TA>(ctx, kind, v, b);
 }
 
-int hv_launch_f32(mo_ed_ctx *ctx, const HvJobT<float> *jobs, int njobs)
+int hv_launch_f32(mo_ed_ctx *ctx, int v, const HvJobT<float> *jobs, int njobs)
 {
-    return hv_run_jobs<float>(ctx, HV_F32, jobs, njobs);
+    return hv_run_jobs<float>(ctx, HV_F32, v, jobs, njobs);
 }
-int hv_launch_f64(mo_ed_ctx *ctx, int kind, const HvJobT<double> *jobs, int njobs)
+int hv_launch_f64(mo_ed_ctx *ctx, int kind, int v, const HvJobT<double> *jobs, int njobs)
 {
-    return hv_run_jobs<double>(ctx, kind, jobs, njobs);
+    return hv_run_jobs<double>(ctx, kind, v, jobs, njobs);
 }
 
-int hv_prepare(mo_ed_ctx *ctx, const Sector &s, int kind)
+static int launch_one(mo_ed_ctx *ctx, const Sector &s, int kind, int v, const void *x, void *y)
+{
+    const int R = variant(kind, v).R;
+    if (kind == HV_F32) {
+        HvJobT<float> j;
+        hv_fill_job<float>(ctx, s, R, x, y, j);
+        return hv_launch_f32(ctx, v, &j, 1);
+    }
+    HvJobT<double> j;
+    hv_fill_job<double>(ctx, s, R, x, y, j);
+    return hv_launch_f64(ctx, kind, v, &j, 1);
+}
+
+// Time every variant once on sector s and keep the fastest.
+static int tune(mo_ed_ctx *ctx, const Sector &s, int kind, int *best)
+{
+    const size_t ex = kind == HV_F64 ? sizeof(double) : sizeof(float);
+    const size_t ey = kind == HV_F32 ? sizeof(float) : sizeof(double);
+    DevBuf dx, dy;
+    if (int rc = dev_alloc(ctx, dx, ex * (size_t)s.Dpad())) return rc;
+    if (int rc = dev_alloc(ctx, dy, ey * (size_t)s.Dpad())) return rc;
+    MOED_CUDA(ctx, cudaMemsetAsync(dx.p, 0, dx.bytes, ctx->stream));
+    cudaEvent_t e0, e1;
+    MOED_CUDA(ctx, cudaEventCreate(&e0));
+    MOED_CUDA(ctx, cudaEventCreate(&e1));
+    float tbest = 1e30f;
+    *best = -1;
+    std::vector<float> &times = ctx->hv_times[shape_key(kind, s)];
+    times.assign(nvariants(kind), -1.0f);
+    for (int v = 0; v < nvariants(kind); ++v) {
+        const int *items;
+        int n;
+        if (int rc = species_items(ctx, s.dn, variant(kind, v).R, &items, &n)) return rc;
+        if (launch_one(ctx, s, kind, v, dx.p, dy.p) != MO_ED_OK) {   // variant does not fit this sector
+            cudaGetLastError();
+            continue;
+        }
+        float tv = 1e30f;
+        for (int rep = 0; rep < 3; ++rep) {
+            MOED_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+            if (int rc = launch_one(ctx, s, kind, v, dx.p, dy.p)) return rc;
+            MOED_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+            MOED_CUDA(ctx, cudaEventSynchronize(e1));
+            float ms = 0.f;
+            MOED_CUDA(ctx, cudaEventElapsedTime(&ms, e0, e1));
+            tv = std::min(tv, ms);
+        }
+        times[v] = tv;
+        if (tv < tbest) {
+            tbest = tv;
+            *best = v;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (*best < 0) return fail(ctx, MO_ED_ERR_ARG, "no H*v tile shape fits this sector");
+    ctx->err.clear();
+    return MO_ED_OK;
+}
+
+int hv_prepare(mo_ed_ctx *ctx, const Sector &s, int kind, int *v_out, int *R_out)
+{
+    const long long key = shape_key(kind, s);
+    auto it = ctx->hv_choice.find(key);
+    int v;
+    if (it != ctx->hv_choice.end()) {
+        v = it->second;
+    } else {
+        if (int rc = tune(ctx, s, kind, &v)) return rc;
+        ctx->hv_choice[key] = v;
+    }
+    const int *items;
+    int n;
+    if (int rc = species_items(ctx, s.dn, variant(kind, v).R, &items, &n)) return rc;
+    if (v_out) *v_out = v;
+    if (R_out) *R_out = variant(kind, v).R;
+    return MO_ED_OK;
+}
+
+int hv_tuning(mo_ed_ctx *ctx, const Sector &s, int kind, int cap, int *nvar, int *shape, float *ms, int *chosen)
+{
+    int v;
+    if (int rc = hv_prepare(ctx, s, kind, &v, nullptr)) return rc;
+    const std::vector<float> &t = ctx->hv_times[shape_key(kind, s)];
+    *nvar = nvariants(kind);
+    *chosen = v;
+    for (int i = 0; i < *nvar && i < cap; ++i) {
+        const HvVariant &h = variant(kind, i);
+        if (shape) {
+            shape[3 * i] = h.R;
+            shape[3 * i + 1] = h.NT;
+            shape[3 * i + 2] = h.MINB;
+        }
+        if (ms) ms[i] = i < (int)t.size() ? t[i] : -1.0f;
+    }
+    return MO_ED_OK;
+}
+
+int hv_prepare_rows(mo_ed_ctx *ctx, const Sector &s, int R)
 {
     const int *items;
     int n;
-    return species_items(ctx, s.dn, hv_rows_per_item(kind), &items, &n);
+    return species_items(ctx, s.dn, R, &items, &n);
 }
 
 int hv_single(mo_ed_ctx *ctx, const Sector &s, int kind, const void *x, void *y)
 {
-    if (int rc = hv_prepare(ctx, s, kind)) return rc;
-    if (kind == HV_F32) {
-        HvJobT<float> j;
-        hv_fill_job<float>(ctx, s, kind, x, y, j);
-        return hv_launch_f32(ctx, &j, 1);
-    }
-    HvJobT<double> j;
-    hv_fill_job<double>(ctx, s, kind, x, y, j);
-    return hv_launch_f64(ctx, kind, &j, 1);
+    int v;
+    if (int rc = hv_prepare(ctx, s, kind, &v, nullptr)) return rc;
+    return launch_one(ctx, s, kind, v, x, y);
 }
 
 }  // namespace moed

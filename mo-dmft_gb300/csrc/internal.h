@@ -212,6 +212,10 @@ struct mo_ed_ctx {
 
     // scratch
     moed::DevBuf scratch_a, scratch_b, scratch_part;
+    // autotuned H*v tile shape per (kind, Nup, Ndn), and the timings (ms) of
+    // every shape measured when it was chosen (negative: did not fit)
+    std::map<long long, int> hv_choice;
+    std::map<long long, std::vector<float>> hv_times;
 };
 
 namespace moed {
@@ -250,19 +254,24 @@ int basis_idx_dev(mo_ed_ctx *ctx, const Sector &s, long long n, const unsigned *
 
 // ---- H*v (hv.cu) ------------------------------------------------------------
 enum HvKind { HV_F64 = 0, HV_F32 = 1, HV_MIXED = 2 };
-// Fill a job for sector s (x, y device pointers).  nitems computed for kind.
+// Fill a job for sector s (x, y device pointers) with R rows per item (the
+// item table for R must exist: hv_prepare / hv_prepare_rows).
 template <typename TA>
-void hv_fill_job(const mo_ed_ctx *ctx, const Sector &s, int kind, const void *x, void *y,
-                 HvJobT<TA> &job);
+void hv_fill_job(const mo_ed_ctx *ctx, const Sector &s, int R, const void *x, void *y, HvJobT<TA> &job);
 // Launch H*v over a host list of jobs (item0 is assigned here); jobs are
 // passed to the kernel by value, so the call can be captured in a CUDA graph.
-int hv_launch_f32(mo_ed_ctx *ctx, const HvJobT<float> *jobs, int njobs);
-int hv_launch_f64(mo_ed_ctx *ctx, int kind, const HvJobT<double> *jobs, int njobs);
-// rows per item of a kind, and the item table of a down species for it
-int hv_rows_per_item(int kind);
+// v = tile-shape variant (hv_prepare); all jobs use its rows per item.
+int hv_launch_f32(mo_ed_ctx *ctx, int v, const HvJobT<float> *jobs, int njobs);
+int hv_launch_f64(mo_ed_ctx *ctx, int kind, int v, const HvJobT<double> *jobs, int njobs);
 int species_items(mo_ed_ctx *ctx, Species *sp, int R, const int **items, int *nitems);
-// build the item table H*v of `kind` needs for sector s
-int hv_prepare(mo_ed_ctx *ctx, const Sector &s, int kind);
+// Tile-shape variant for sector s (autotuned on the first call per shape;
+// that first call allocates and synchronizes, so make it before any stream
+// capture) and its rows per item; builds the item table.
+int hv_prepare(mo_ed_ctx *ctx, const Sector &s, int kind, int *v, int *R);
+// autotuner record of a shape: per variant (R, NT, MINB) and time in ms
+int hv_tuning(mo_ed_ctx *ctx, const Sector &s, int kind, int cap, int *nvar, int *shape, float *ms, int *chosen);
+// item table for R rows per item (sectors batched with a tuned one)
+int hv_prepare_rows(mo_ed_ctx *ctx, const Sector &s, int R);
 // Convenience: one vector, jobs staged through scratch.
 int hv_single(mo_ed_ctx *ctx, const Sector &s, int kind, const void *x, void *y);
 

@@ -257,13 +257,18 @@ int lz_setup(mo_ed_ctx *ctx, LzBatch &b, const std::vector<Sector> &secs, int pr
     b.hv_nitems.resize(nrun);
     b.upd_total = b.hv_total = 0;
     const int kind = prec == MO_ED_FP32 ? HV_F32 : HV_F64;
+    // one tile shape for the whole batch: the one tuned for its largest sector
+    int big = 0;
+    for (int r = 1; r < nrun; ++r)
+        if (secs[r].D() > secs[big].D()) big = r;
+    if (int rc = hv_prepare(ctx, secs[big], kind, &b.hv_variant, &b.hv_rows)) return rc;
     for (int r = 0; r < nrun; ++r) {
-        if (int rc = hv_prepare(ctx, secs[r], kind)) return rc;
+        if (int rc = hv_prepare_rows(ctx, secs[r], b.hv_rows)) return rc;
         b.upd_item0[r] = b.upd_total;
         b.upd_nitems[r] = (int)((secs[r].Dpad() + kVecChunk - 1) / kVecChunk);
         b.upd_total += b.upd_nitems[r];
         b.hv_item0[r] = b.hv_total;
-        b.hv_nitems[r] = secs[r].dn->nitems.at(hv_rows_per_item(kind));
+        b.hv_nitems[r] = secs[r].dn->nitems.at(b.hv_rows);
         b.hv_total += b.hv_nitems[r];
     }
     if (int rc = dev_alloc(ctx, b.upd_part, sizeof(double) * std::max(1, b.upd_total))) return rc;
@@ -306,7 +311,7 @@ static int lz_steps(mo_ed_ctx *ctx, LzBatch &b, LzBatchDev &d)
     for (int k = 0; k < 3; ++k) {
         jobs[k].resize(nrun);
         for (int r = 0; r < nrun; ++r) {
-            hv_fill_job<T>(ctx, b.sec[r], kind, d.run[r].u[k], d.run[r].w, jobs[k][r]);
+            hv_fill_job<T>(ctx, b.sec[r], b.hv_rows, d.run[r].u[k], d.run[r].w, jobs[k][r]);
             jobs[k][r].dot_partial = d.run[r].hv_part;
             jobs[k][r].active = d.run[r].active;
         }
@@ -319,8 +324,9 @@ static int lz_steps(mo_ed_ctx *ctx, LzBatch &b, LzBatchDev &d)
             k_lz_update<T><<<gv, kVecThreads, 0, ctx->stream>>>(d, j);
         }
         MOED_CHECK_LAUNCH(ctx);
-        int rc = (sizeof(T) == 4) ? hv_launch_f32(ctx, (const HvJobT<float> *)jobs[j % 3].data(), nrun)
-                                  : hv_launch_f64(ctx, HV_F64, (const HvJobT<double> *)jobs[j % 3].data(), nrun);
+        int rc = (sizeof(T) == 4)
+                     ? hv_launch_f32(ctx, b.hv_variant, (const HvJobT<float> *)jobs[j % 3].data(), nrun)
+                     : hv_launch_f64(ctx, HV_F64, b.hv_variant, (const HvJobT<double> *)jobs[j % 3].data(), nrun);
         if (rc) return rc;
         k_lz_finalize<<<nrun, kVecThreads, 0, ctx->stream>>>(d, j, b.nstep);
         MOED_CHECK_LAUNCH(ctx);
