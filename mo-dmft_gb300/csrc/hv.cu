@@ -308,15 +308,21 @@ k_hv(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict__ mdl
             live[r] = s_d[r] >= 0;
         }
         const bool slow = s_slow != 0;
+        const bool want_dot = jb.dot_partial != nullptr;
         const unsigned imask = s_itemmask;
         double dacc = 0.0;
+        int4 nx_inf = tid < nchunk ? ldg_i4(jb.up_info + 4 * tid) : make_int4(0, 0, 0, 0);
+        Vec4<TA> nx_ud = tid < nchunk ? ldg4(jb.up_diag + 4 * tid) : Vec4<TA>{};
         for (int c = tid; c < nchunk; c += NT) {
             const int u0 = 4 * c;
-            const int4 inf4 = ldg_i4(jb.up_info + u0);
+            const int4 inf4 = nx_inf;
+            const Vec4<TA> ud = nx_ud;
+            if (c + NT < nchunk) {   // prefetch the next chunk's column data
+                nx_inf = ldg_i4(jb.up_info + u0 + 4 * NT);
+                nx_ud = ldg4(jb.up_diag + u0 + 4 * NT);
+            }
             const int inf[4] = {inf4.x, inf4.y, inf4.z, inf4.w};
-            const Vec4<TA> ud = ldg4(jb.up_diag + u0);
             TA acc[4][R];
-            TX xs[4][R];
             int cnt[4], iu[4];
             int maxc = 0;
             // diagonal
@@ -328,22 +334,29 @@ k_hv(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict__ mdl
                 const RowVec<TX, R> sx = S[u0 + k];
                 const RowVec<TA, R> cr = s_crossT[iu[k]];
 #pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    xs[k][r] = sx.v[r];
-                    acc[k][r] = (ud.v[k] + ddiag[r] + cr.v[r]) * (TA)sx.v[r];
-                }
+                for (int r = 0; r < R; ++r) acc[k][r] = (ud.v[k] + ddiag[r] + cr.v[r]) * (TA)sx.v[r];
             }
             // up-spin hybridisation: shared-memory gathers, all rows at once
+            // The moves of SB slots are loaded together so that their L2
+            // latencies overlap; a gather is issued only for a column's own
+            // moves (no shared-memory traffic for padded slots).
+            constexpr int SB = R > 4 ? 2 : 4;
             const HopEnt<TA> *tab = jb.up_tab + (size_t)c * jb.up_hw * 4;
-            for (int s = 0; s < maxc; ++s) {
-                HopEnt<TA> e[4];
-                ld_moves<TA>(tab + (size_t)s * 4, e);
+            for (int s0 = 0; s0 < maxc; s0 += SB) {
+                HopEnt<TA> e[SB][4];
 #pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    if (s < cnt[k]) {
-                        const RowVec<TX, R> g = S[e[k].t];
+                for (int t = 0; t < SB; ++t) {
+                    if (s0 + t < maxc) ld_moves<TA>(tab + (size_t)(s0 + t) * 4, e[t]);
+                }
 #pragma unroll
-                        for (int r = 0; r < R; ++r) acc[k][r] += e[k].v * (TA)g.v[r];
+                for (int t = 0; t < SB; ++t) {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        if (s0 + t < cnt[k]) {
+                            const RowVec<TX, R> g = S[e[t][k].t];
+#pragma unroll
+                            for (int r = 0; r < R; ++r) acc[k][r] += e[t][k].v * (TA)g.v[r];
+                        }
                     }
                 }
             }
@@ -403,20 +416,25 @@ k_hv(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict__ mdl
                     }
                 }
             }
-            TA part = TA(0);
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 if (live[r]) {
                     TY o[4];
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        o[k] = (TY)acc[k][r];
-                        part += (TA)xs[k][r] * (TA)o[k];
-                    }
+                    for (int k = 0; k < 4; ++k) o[k] = (TY)acc[k][r];
                     stg4(y + (size_t)s_d[r] * ld + u0, o);
                 }
             }
-            dacc += (double)part;
+            if (want_dot) {   // x (re-read from the stage) . y of this chunk
+                TA part = TA(0);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const RowVec<TX, R> sx = S[u0 + k];
+#pragma unroll
+                    for (int r = 0; r < R; ++r) part += (TA)sx.v[r] * (TA)(TY)acc[k][r];
+                }
+                dacc += (double)part;
+            }
         }
         if (jb.dot_partial) {
             for (int off = 16; off > 0; off >>= 1) dacc += __shfl_down_sync(0xffffffffu, dacc, off);
@@ -450,7 +468,7 @@ static size_t dyn_smem_bytes(int ld, const ModelDev &m)
 struct HvVariant {
     int R, NT, MINB;
 };
-static const HvVariant kVarF32[] = {{3, 512, 2}, {4, 256, 2}, {6, 512, 1}, {3, 256, 3}};
+static const HvVariant kVarF32[] = {{3, 512, 2}, {4, 256, 2}, {6, 512, 1}, {3, 256, 3}, {8, 512, 1}};
 static const HvVariant kVarF64[] = {{2, 256, 2}, {3, 256, 1}, {2, 512, 1}};
 static const int kNVarF32 = sizeof(kVarF32) / sizeof(kVarF32[0]);
 static const int kNVarF64 = sizeof(kVarF64) / sizeof(kVarF64[0]);
@@ -522,7 +540,8 @@ static int launch_variant(mo_ed_ctx *ctx, int kind, int v, const HvBatch<TA> &b)
         case 0: return launch_batch<float, float, float, 3, 512, 2>(ctx, b);
         case 1: return launch_batch<float, float, float, 4, 256, 2>(ctx, b);
         case 2: return launch_batch<float, float, float, 6, 512, 1>(ctx, b);
-        default: return launch_batch<float, float, float, 3, 256, 3>(ctx, b);
+        case 3: return launch_batch<float, float, float, 3, 256, 3>(ctx, b);
+        default: return launch_batch<float, float, float, 8, 512, 1>(ctx, b);
         }
     } else if (kind == HV_F64) {
         switch (v) {
