@@ -158,6 +158,25 @@ int mo_ed_apply_c(mo_ed_ctx *ctx, int ne_up, int ne_down, const double *vec, int
 int mo_ed_lanczos_iteration(mo_ed_ctx *ctx, int ne_up, int ne_down, const double *vec,
                             int *nstep_calc, double *a, double *b);
 
+/* No counterpart in the reference.  mo_ed_lanczos_iteration without device
+ * allocation, for hosts that own all of the GPU's memory through their own
+ * pool (a DMFT driver that reserves the device up front for the arrays of its
+ * self-consistency loop) or cannot afford the device-wide synchronisation of
+ * cudaFree inside their loop.  Same arguments and results; the Krylov vectors,
+ * coefficients and partial sums live in one fixed 32 MiB region that the
+ * library reserves statically on every GPU that loads it, held until the
+ * process exits.  Limits: sectors up to about 1.0e6 padded elements in FP64
+ * (2.0e6 in FP32, mo_ed_vector_layout gives the count); larger ones return
+ * MO_ED_ERR_CAPACITY.  The sector must have been prepared in the same
+ * precision by an earlier mo_ed_lanczos_iteration, mo_ed_multiply_h_dev or
+ * mo_ed_hv_tuning call (those build its tables and may allocate); otherwise
+ * MO_ED_ERR_STATE.  The first call on a device looks up the region's address;
+ * make it before any stream capture.  All calls share the region, which keeps
+ * the previous call's contents (this call clears what must start at zero);
+ * calls that overlap on the GPU race on it, so serialise them. */
+int mo_ed_lanczos_iteration_noalloc(mo_ed_ctx *ctx, int ne_up, int ne_down, const double *vec,
+                                    int *nstep_calc, double *a, double *b);
+
 /* ---- a13: diag (ed_solver.F90:107-191) ---------------------------------- */
 /* nev lowest eigenpairs of one sector (thick-restart Lanczos with full
  * reorthogonalisation; FP64 Rayleigh quotients).  eigval[nev] (unconverged /

@@ -693,6 +693,19 @@ int hv_prepare_rows(mo_ed_ctx *ctx, const Sector &s, int R)
     return species_items(ctx, s.dn, R, &items, &n);
 }
 
+int hv_lookup(mo_ed_ctx *ctx, const Sector &s, int kind, int *v_out, int *R_out)
+{
+    auto it = ctx->hv_choice.find(shape_key(kind, s));
+    if (it == ctx->hv_choice.end())
+        return fail(ctx, MO_ED_ERR_STATE, "H*v tile shape of this sector not chosen yet");
+    const int R = variant(kind, it->second).R;
+    if (s.dn->items.find(R) == s.dn->items.end())
+        return fail(ctx, MO_ED_ERR_STATE, "H*v item table of this sector not built yet");
+    if (v_out) *v_out = it->second;
+    if (R_out) *R_out = R;
+    return MO_ED_OK;
+}
+
 int hv_single(mo_ed_ctx *ctx, const Sector &s, int kind, const void *x, void *y)
 {
     int v;

@@ -247,6 +247,9 @@ long long binom(int n, int k);
 int build_model(mo_ed_ctx *ctx);
 int get_species(mo_ed_ctx *ctx, int N, Species **out);
 int get_sector(mo_ed_ctx *ctx, int ne_up, int ne_down, Sector *out);
+// Lookup only: MO_ED_ERR_STATE when the sector's tables were never built
+// (get_sector builds them, and allocates; this never allocates).
+int find_sector(mo_ed_ctx *ctx, int ne_up, int ne_down, Sector *out);
 int basis_get_dev(mo_ed_ctx *ctx, const Sector &s, long long n, const long long *d_idx,
                   unsigned *d_state);
 int basis_idx_dev(mo_ed_ctx *ctx, const Sector &s, long long n, const unsigned *d_state,
@@ -272,12 +275,21 @@ int hv_prepare(mo_ed_ctx *ctx, const Sector &s, int kind, int *v, int *R);
 int hv_tuning(mo_ed_ctx *ctx, const Sector &s, int kind, int cap, int *nvar, int *shape, float *ms, int *chosen);
 // item table for R rows per item (sectors batched with a tuned one)
 int hv_prepare_rows(mo_ed_ctx *ctx, const Sector &s, int R);
+// Lookup only: the tile shape and item table that hv_prepare left for this
+// sector and kind, or MO_ED_ERR_STATE if it never ran (never tunes or allocates).
+int hv_lookup(mo_ed_ctx *ctx, const Sector &s, int kind, int *v, int *R);
 // Convenience: one vector, jobs staged through scratch.
 int hv_single(mo_ed_ctx *ctx, const Sector &s, int kind, const void *x, void *y);
 
 // ---- Krylov (krylov.cu) -----------------------------------------------------
 int lanczos_reference(mo_ed_ctx *ctx, const Sector &s, const double *h_vec, int nstep,
                       int *nstep_calc, double *a, double *b);
+// The same recurrence with every device buffer carved from the caller's
+// region [scratch, scratch + cap) (256-byte aligned).  Needs hv_lookup to
+// succeed for the sector; allocates no device memory.  Bytes needed:
+size_t lanczos_region_bytes(const Sector &s, int prec, int nstep, int hv_rows);
+int lanczos_reference_in(mo_ed_ctx *ctx, const Sector &s, const double *h_vec, int nstep,
+                         int *nstep_calc, double *a, double *b, void *scratch, size_t cap);
 int diag_sector(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<double> &vals,
                 std::vector<DevBuf> *vecs);
 

@@ -391,6 +391,111 @@ int lanczos_reference(mo_ed_ctx *ctx, const Sector &s, const double *h_vec, int 
     return MO_ED_OK;
 }
 
+// The same recurrence inside a caller-provided device region.  Layout, each
+// part starting on a 256-byte boundary: a and nrm [nstep+1] each, the two
+// flags, the update and H*v partial sums, u_0, u_1 u_2 (adjacent; for FP32
+// runs they first hold the FP64 start vector before its conversion) and w.
+namespace {
+struct LzRegion {
+    size_t coef, flags, upd, hv, u0, u12, w, end;
+};
+
+size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+LzRegion lz_region(const Sector &s, int prec, int nstep, int hv_rows)
+{
+    const size_t es = prec == MO_ED_FP32 ? sizeof(float) : sizeof(double);
+    const size_t Dp = (size_t)s.Dpad();
+    const size_t upd_n = (Dp + kVecChunk - 1) / kVecChunk;
+    const size_t hv_n = (size_t)std::max(1, s.dn->nitems.at(hv_rows));
+    LzRegion r;
+    r.coef = 0;
+    r.flags = up256(r.coef + sizeof(double) * 2 * (size_t)(nstep + 1));
+    r.upd = up256(r.flags + sizeof(int) * 2);
+    r.hv = up256(r.upd + sizeof(double) * upd_n);
+    r.u0 = up256(r.hv + sizeof(double) * hv_n);
+    r.u12 = up256(r.u0 + es * Dp);
+    r.w = up256(r.u12 + std::max(2 * es * Dp, prec == MO_ED_FP32 ? sizeof(double) * Dp : 0));
+    r.end = up256(r.w + es * Dp);
+    return r;
+}
+
+// a = nrm = 0, active = 1, nstep_calc = 0 (the region keeps an earlier call's contents)
+__global__ void k_lz_reset(const __grid_constant__ LzBatchDev b, int nstep)
+{
+    const LzRunDev &R = b.run[blockIdx.x];
+    for (int j = threadIdx.x; j <= nstep; j += blockDim.x) {
+        R.a[j] = 0.0;
+        R.nrm[j] = 0.0;
+    }
+    if (threadIdx.x == 0) {
+        *R.active = 1;
+        *R.nstep_calc = 0;
+    }
+}
+}  // namespace
+
+size_t lanczos_region_bytes(const Sector &s, int prec, int nstep, int hv_rows)
+{
+    return lz_region(s, prec, nstep, hv_rows).end;
+}
+
+int lanczos_reference_in(mo_ed_ctx *ctx, const Sector &s, const double *h_vec, int nstep,
+                         int *nstep_calc, double *a, double *b, void *scratch, size_t cap)
+{
+    const int prec = ctx->opt.precision;
+    const int kind = prec == MO_ED_FP32 ? HV_F32 : HV_F64;
+    LzBatch lb;
+    lb.prec = prec;
+    lb.nstep = nstep;
+    lb.sec = {s};
+    if (int rc = hv_lookup(ctx, s, kind, &lb.hv_variant, &lb.hv_rows)) return rc;
+    const LzRegion g = lz_region(s, prec, nstep, lb.hv_rows);
+    if (g.end > cap || ((size_t)scratch & 255)) return fail(ctx, MO_ED_ERR_CAPACITY, "Lanczos region too small");
+    char *base = (char *)scratch;
+    const size_t es = prec == MO_ED_FP32 ? sizeof(float) : sizeof(double);
+    const long long Dp = s.Dpad();
+
+    LzBatchDev d;
+    memset(&d, 0, sizeof(d));
+    d.nrun = 1;
+    LzRunDev &R = d.run[0];
+    R.u[0] = base + g.u0;
+    R.u[1] = base + g.u12;
+    R.u[2] = base + g.u12 + es * (size_t)Dp;
+    R.w = base + g.w;
+    R.D = Dp;
+    R.upd_item0 = 0;
+    R.upd_nitems = (int)((Dp + kVecChunk - 1) / kVecChunk);
+    R.hv_item0 = 0;
+    R.hv_nitems = s.dn->nitems.at(lb.hv_rows);
+    R.a = (double *)(base + g.coef);
+    R.nrm = R.a + (nstep + 1);
+    R.active = (int *)(base + g.flags);
+    R.nstep_calc = R.active + 1;
+    R.upd_part = (double *)(base + g.upd);
+    R.hv_part = (double *)(base + g.hv);
+    d.total_items = R.upd_nitems;
+
+    k_lz_reset<<<1, kVecThreads, 0, ctx->stream>>>(d, nstep);
+    MOED_CHECK_LAUNCH(ctx);
+    if (prec == MO_ED_FP32) {
+        double *stage = (double *)(base + g.u12);
+        if (int rc = upload_padded(ctx, s, h_vec, stage, sizeof(double))) return rc;
+        if (int rc = convert_f64_to_f32(ctx, stage, (float *)R.u[0], Dp)) return rc;
+        if (int rc = lz_steps<float>(ctx, lb, d)) return rc;
+    } else {
+        if (int rc = upload_padded(ctx, s, h_vec, R.u[0], sizeof(double))) return rc;
+        if (int rc = lz_steps<double>(ctx, lb, d)) return rc;
+    }
+    MOED_CUDA(ctx, cudaMemcpyAsync(a, R.a, sizeof(double) * (nstep + 1), cudaMemcpyDeviceToHost, ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpyAsync(b, R.nrm, sizeof(double) * (nstep + 1), cudaMemcpyDeviceToHost, ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpyAsync(nstep_calc, R.nstep_calc, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    b[0] = 0.0;
+    return MO_ED_OK;
+}
+
 // ---------------------------------------------------------------------------
 // thick-restart Lanczos with full reorthogonalisation (diag replacement)
 // ---------------------------------------------------------------------------

@@ -495,6 +495,23 @@ int get_sector(mo_ed_ctx *ctx, int ne_up, int ne_down, Sector *out)
     return MO_ED_OK;
 }
 
+int find_sector(mo_ed_ctx *ctx, int ne_up, int ne_down, Sector *out)
+{
+    if (!ctx->have_model) return fail(ctx, MO_ED_ERR_STATE, "model not set");
+    if (ne_up < 0 || ne_up > ctx->nsite || ne_down < 0 || ne_down > ctx->nsite)
+        return fail(ctx, MO_ED_ERR_SECTOR, "sector (" + std::to_string(ne_up) + "," +
+                                               std::to_string(ne_down) + ") out of range");
+    auto iu = ctx->species.find(ne_up), id = ctx->species.find(ne_down);
+    if (iu == ctx->species.end() || id == ctx->species.end())
+        return fail(ctx, MO_ED_ERR_STATE, "sector (" + std::to_string(ne_up) + "," +
+                                              std::to_string(ne_down) + ") tables not built yet");
+    out->ne_up = ne_up;
+    out->ne_down = ne_down;
+    out->up = iu->second.get();
+    out->dn = id->second.get();
+    return MO_ED_OK;
+}
+
 int basis_get_dev(mo_ed_ctx *ctx, const Sector &s, long long n, const long long *d_idx,
                   unsigned *d_state)
 {

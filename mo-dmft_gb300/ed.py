@@ -86,6 +86,7 @@ SIGNATURES = [
     ("mo_ed_apply_c", C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, C.c_int, C.c_int, C.c_int, _dp,
                                 C.c_longlong, _llp]),
     ("mo_ed_lanczos_iteration", C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _ip, _dp, _dp]),
+    ("mo_ed_lanczos_iteration_noalloc", C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _ip, _dp, _dp]),
     ("mo_ed_diag", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _dp]),
     ("mo_ed_diag_stats", C.c_int, [C.c_void_p, _ip, _llp, _dp, _dp]),
     ("mo_ed_solve", C.c_int, [C.c_void_p, _ip, _dp, _dp, _ip, _ip, C.c_int]),
@@ -318,6 +319,16 @@ class EDSolver:
         a, b = np.zeros(n + 1), np.zeros(n + 1)
         nc = C.c_int()
         self._chk(lib().mo_ed_lanczos_iteration(self._ctx, ne_up, ne_down, _d(_f64(vec)), C.byref(nc), _d(a), _d(b)))
+        return nc.value, a, b
+
+    def lanczos_iteration_noalloc(self, ne_up, ne_down, vec):
+        """lanczos_iteration on the library's fixed device region (no device
+        allocation; the sector must be prepared by an earlier call)."""
+        n = self.opt.nstep
+        a, b = np.zeros(n + 1), np.zeros(n + 1)
+        nc = C.c_int()
+        self._chk(lib().mo_ed_lanczos_iteration_noalloc(self._ctx, ne_up, ne_down, _d(_f64(vec)), C.byref(nc),
+                                                        _d(a), _d(b)))
         return nc.value, a, b
 
     def diag(self, ne_up, ne_down, nev, vectors=True):
