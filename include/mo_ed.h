@@ -66,8 +66,9 @@ typedef struct {
     int gs_ncv;         /* Krylov basis size of the eigensolver per restart cycle (0: auto) */
     int gs_maxcycles;   /* restart cycles before MO_ED_ERR_NOCONV (default 200) */
     double gs_tol;      /* relative residual tolerance of converged Ritz pairs (0: auto) */
-    int green_reorth;   /* 0 (default): the reference recurrence without reorthogonalisation
-                           (ed_lanczos.F90:53-68); 1: full reorthogonalisation */
+    int green_reorth;   /* must be 0: the Green's-function Lanczos is the reference
+                           recurrence without reorthogonalisation (ed_lanczos.F90:53-68);
+                           other values are rejected with MO_ED_ERR_ARG */
     int reserved[8];
 } mo_ed_options;
 

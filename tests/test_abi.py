@@ -77,3 +77,21 @@ def test_no_device_fails_loudly(pkg, built):
         pytest.skip("a CUDA device is present")
     with pytest.raises(pkg.EDError):
         pkg.EDSolver(0)
+
+
+def test_fortran_bindings_match_header():
+    """Every bind(C) interface of the Fortran module names a declared entry
+    point and passes the same number of arguments."""
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    decl = {}
+    for name, args in re.findall(r"\b(mo_ed_\w+)\s*\(([^)]*)\)\s*;", txt):
+        decl[name] = 0 if args.strip() in ("", "void") else len(args.split(","))
+    f90 = open(os.path.join(ROOT, "mo-dmft_gb300", "fortran", "mo_ed_bind.f90")).read()
+    f90 = re.sub(r"&\s*\n\s*", "", f90)
+    found = re.findall(r"function\s+(mo_ed_\w+)\s*\(([^)]*)\)\s*bind\(C,\s*name=\"(mo_ed_\w+)\"\)", f90)
+    assert len(found) >= 20
+    for fname, args, cname in found:
+        assert fname == cname and cname in decl, cname
+        n = 0 if not args.strip() else len(args.split(","))
+        assert n == decl[cname], (cname, n, decl[cname])
