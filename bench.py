@@ -282,6 +282,7 @@ def run_ours(args):
                     "ms_per_step": round(t_e2e * 1e3, 4)},
             "gpu_launches": launches,
             "hv_autotune": {"variants": [{"rows_per_item": v[0][0], "threads": v[0][1], "ctas_per_sm": v[0][2],
+                                          "kernel": "k_hv_async" if v[0][3] else "k_hv",
                                           "ms": round(v[1], 4)} for v in tuning], "chosen": chosen},
             "clocks": clocks,
             "lanczos_g": lg,

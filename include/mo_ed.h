@@ -138,11 +138,17 @@ int mo_ed_multiply_h_mixed_dev(mo_ed_ctx *ctx, int ne_up, int ne_down, const flo
 /* H*v tile-shape autotuner of a sector (no reference counterpart: the
  * reference has one CPU loop).  The first H*v of each (precision, Nup, Ndn)
  * times every variant on that sector and keeps the fastest; this call runs
- * the tuning if needed and reports *nvariant variants: shape[3*i..3*i+2] =
- * (rows per item, threads per CTA, CTAs per SM), ms[i] (negative: does not
+ * the tuning if needed and reports *nvariant variants: shape[4*i..4*i+3] =
+ * (rows per item, threads per CTA, CTAs per SM, kernel: 0 k_hv, 1 the
+ * double-buffered staged k_hv_async), ms[i] (negative: does not
  * fit), and the *chosen index.  Arrays hold capacity variants. */
 int mo_ed_hv_tuning(mo_ed_ctx *ctx, int ne_up, int ne_down, int dtype, int capacity, int *nvariant,
                     int *shape, float *ms, int *chosen);
+/* Pin the H*v variant (index into the list mo_ed_hv_tuning reports) of a
+ * sector and precision, replacing the autotuner's choice.  Every variant
+ * computes the same sums; the order of the up-spin terms differs between
+ * the shared-memory schedules, so FP32 results agree to rounding. */
+int mo_ed_hv_set_variant(mo_ed_ctx *ctx, int ne_up, int ne_down, int dtype, int variant);
 
 /* ---- a11: apply_c (ed_operators.F90:10-61) ------------------------------ */
 /* vec_out = c^dagger_(iorb,ispin) vec (pm = 1) or c_(iorb,ispin) vec (pm = 2).

@@ -362,6 +362,15 @@ int mo_ed_hv_tuning(mo_ed_ctx *ctx, int ne_up, int ne_down, int dtype, int capac
     return hv_tuning(ctx, s, dtype == MO_ED_FP32 ? HV_F32 : HV_F64, capacity, nvariant, shape, ms, chosen);
 }
 
+int mo_ed_hv_set_variant(mo_ed_ctx *ctx, int ne_up, int ne_down, int dtype, int variant)
+{
+    CTX_CHECK(ctx);
+    if (dtype != MO_ED_FP32 && dtype != MO_ED_FP64) return fail(ctx, MO_ED_ERR_ARG, "bad dtype");
+    Sector s;
+    if (int rc = get_sector(ctx, ne_up, ne_down, &s)) return rc;
+    return hv_set_variant(ctx, s, dtype == MO_ED_FP32 ? HV_F32 : HV_F64, variant);
+}
+
 int mo_ed_apply_c(mo_ed_ctx *ctx, int ne_up, int ne_down, const double *vec, int pm, int iorb,
                   int ispin, double *vec_out, long long capacity, long long *ntot_out)
 {

@@ -457,19 +457,526 @@ static size_t dyn_smem_bytes(int ld, const ModelDev &m)
 }
 
 // ---------------------------------------------------------------------------
+// staged variant (k_hv_async)
+// ---------------------------------------------------------------------------
+// The same sum per element, organised for latency hiding and few instructions:
+//   * stage layout [tile][r][32]: column u of staged row r sits at
+//     ((u >> 5) * R + r) * 32 + (u & 31).  The R values of a column are 32
+//     elements apart, so one address serves every row (immediate offsets),
+//     and column u is in bank u mod 32 for every row;
+//   * the rows of the next item and its descriptor (the row data k_hv
+//     computes per item: row indices, down-spin moves, interspecies diagonal,
+//     spin-flip / pair-hop terms; built once by k_item_desc) are copied
+//     (cp.async, 16 bytes per thread, L2 only) into the second of two stage
+//     buffers while the current item is computed: two barriers per item;
+//   * warp w owns chunks c = w + NW * (kHvCh * i + q) (32 columns each, one
+//     column per lane), so every global load and store of a warp covers one
+//     128-byte line and the kHvCh chunks of an iteration share their address
+//     arithmetic (immediate offsets);
+//   * up-spin moves follow the conflict-free schedule (species_sched): the
+//     entries hold the stage offset of the target, one bank-conflict-free
+//     shared load per staged row and slot, no predication;
+//   * down-spin row AXPYs: one row offset per move serves the kHvCh chunks.
+constexpr int kHvCh = 2;
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all_but_newest() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+template <typename TA>
+__device__ __forceinline__ int hv_find_job(const HvBatch<TA> &b, int item)
+{
+    int j = 0;
+    while (j + 1 < b.njobs && item >= b.job[j + 1].item0) ++j;
+    return j;
+}
+
+// next item of this CTA at or after `from` (stride gridDim.x) whose job is active
+template <typename TA>
+__device__ __forceinline__ int hv_next_item(const HvBatch<TA> &b, int from)
+{
+    for (int item = from; item < b.total_items; item += gridDim.x) {
+        const HvJobT<TA> &jb = b.job[hv_find_job(b, item)];
+        if (!jb.active || *jb.active != 0) return item;
+    }
+    return -1;
+}
+
+// Item descriptor: the per-item row data of k_hv (row indices, impurity
+// patterns, down-spin moves, interspecies diagonal of the rows, spin-flip /
+// pair-hop terms), computed once per (down species, R, precision) by
+// k_item_desc and staged next to the rows.  Offsets are in 4-byte words.
+struct DescGeom {
+    int words, dm, nimp, npair;
+    int o_d, o_id, o_dcnt, o_flags, o_ddiag, o_dtgt, o_dval, o_cross, o_quad;
+    int o_sfsrc, o_phsrc, o_sfc, o_phc, o_rowmask;
+};
+
+template <typename TA, int R>
+static DescGeom desc_geom(int dm, const ModelDev &m)
+{
+    const int ts = sizeof(TA) / 4;
+    auto al = [](int w, int a) { return (w + a - 1) / a * a; };
+    DescGeom g;
+    g.dm = std::max(dm, 1);
+    g.nimp = m.nimp;
+    g.npair = std::max(m.npair, 1);
+    int w = 0;
+    g.o_d = w;       w += R;
+    g.o_id = w;      w += R;
+    g.o_dcnt = w;    w += R;
+    g.o_flags = w;   w += 2;            // slow, item pair mask
+    w = al(w, 2);
+    g.o_ddiag = w;   w += R * ts;
+    g.o_dtgt = w;    w += R * g.dm;
+    w = al(w, 2);
+    g.o_dval = w;    w += R * g.dm * ts;
+    g.o_cross = w;   w += g.nimp * R * ts;
+    w = al(w, 4);
+    g.o_quad = w;    w += R * g.nimp * (int)(sizeof(Quad<TA>) / 4);
+    g.o_sfsrc = w;   w += R * g.npair;
+    g.o_phsrc = w;   w += R * g.npair;
+    w = al(w, 2);
+    g.o_sfc = w;     w += R * g.npair * ts;
+    g.o_phc = w;     w += R * g.npair * ts;
+    g.o_rowmask = w; w += g.npair;
+    g.words = al(w, 4);
+    return g;
+}
+
+// one thread per item: the row data the k_hv setup computes per item
+template <typename TA, int R>
+__global__ void k_item_desc(int nitems, const int *__restrict__ items, const int *__restrict__ dn_info,
+                            const TA *__restrict__ dn_diag, const int *__restrict__ dn_tgt,
+                            const TA *__restrict__ dn_val, int nd, const ModelDev *__restrict__ mdl, DescGeom g,
+                            unsigned *__restrict__ out)
+{
+    const int it = blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= nitems) return;
+    unsigned *rec = out + (size_t)it * g.words;
+    for (int i = 0; i < g.words; ++i) rec[i] = 0u;
+    int *od = (int *)(rec + g.o_d), *oid = (int *)(rec + g.o_id), *ocnt = (int *)(rec + g.o_dcnt);
+    int *oflags = (int *)(rec + g.o_flags);
+    TA *oddiag = (TA *)(rec + g.o_ddiag);
+    int *odtgt = (int *)(rec + g.o_dtgt);
+    TA *odval = (TA *)(rec + g.o_dval);
+    TA *ocross = (TA *)(rec + g.o_cross);
+    Quad<TA> *oquad = (Quad<TA> *)(rec + g.o_quad);
+    int *osfsrc = (int *)(rec + g.o_sfsrc), *ophsrc = (int *)(rec + g.o_phsrc);
+    TA *osfc = (TA *)(rec + g.o_sfc), *ophc = (TA *)(rec + g.o_phc);
+    unsigned *orowmask = rec + g.o_rowmask;
+    const int nimp = mdl->nimp, npair = mdl->npair;
+    const TA Jc = (TA)mdl->J;
+    int d[R], id[R];
+    unsigned sfm[R], phm[R];
+    int slow = 0;
+    unsigned itemmask = 0u;
+    for (int r = 0; r < R; ++r) {
+        d[r] = items[it * R + r];
+        id[r] = 0;
+        sfm[r] = phm[r] = 0u;
+        int cnt = 0;
+        TA dg = TA(0);
+        if (d[r] >= 0) {
+            const int inf = dn_info[d[r]];
+            id[r] = (inf >> 8) & 0xff;
+            cnt = inf & 0xff;
+            dg = dn_diag[d[r]];
+            for (int s = 0; s < cnt; ++s) {
+                odtgt[r * g.dm + s] = dn_tgt[(size_t)s * nd + d[r]];
+                odval[r * g.dm + s] = dn_val[(size_t)s * nd + d[r]];
+            }
+        }
+        od[r] = d[r];
+        oid[r] = id[r];
+        ocnt[r] = cnt;
+        oddiag[r] = dg;
+    }
+    for (int iu = 0; iu < nimp; ++iu)
+        for (int r = 0; r < R; ++r) ocross[iu * R + r] = (TA)mdl->cross[iu * nimp + id[r]];
+    for (int r = 0; r < R; ++r) {
+        if (d[r] < 0) continue;
+        for (int p = 0; p < npair; ++p) {
+            const int esf = mdl->t4[mdl->pair_rev[p] * nimp + id[r]];   // spin-flip: T_{j<-i}(d)
+            const int eph = mdl->t4[p * nimp + id[r]];                  // pair hop:  T_{i<-j}(d)
+            if (esf < 0) {
+                const int off = (int)(short)(esf & 0xffff), dp = d[r] + off, rp = r + off;
+                const bool local = rp >= 0 && rp < R && d[rp] == dp;
+                osfsrc[r * g.npair + p] = local ? rp : -(1 + dp);
+                osfc[r * g.npair + p] = (esf & 0x40000000) ? -Jc : Jc;
+                sfm[r] |= 1u << p;
+                orowmask[p] |= 1u << r;
+                itemmask |= 1u << p;
+                if (!local) slow = 1;
+            }
+            if (eph < 0) {
+                const int off = (int)(short)(eph & 0xffff), dp = d[r] + off, rp = r + off;
+                const bool local = rp >= 0 && rp < R && d[rp] == dp;
+                ophsrc[r * g.npair + p] = local ? rp : -(1 + dp);
+                ophc[r * g.npair + p] = (eph & 0x40000000) ? -Jc : Jc;
+                phm[r] |= 1u << p;
+                orowmask[p] |= 1u << (16 + r);
+                itemmask |= 1u << p;
+                if (!local) slow = 1;
+            }
+        }
+    }
+    for (int r = 0; r < R; ++r)
+        for (int iu = 0; iu < nimp; ++iu) {
+            Quad<TA> q;
+            q.cnt = 0;
+            for (int t = 0; t < 2; ++t) {
+                q.du[t] = 0;
+                q.src[t] = 0;
+                q.c[t] = TA(0);
+            }
+            if (d[r] >= 0) {
+                for (int p = 0; p < npair; ++p) {
+                    const int e = mdl->t4[p * nimp + iu];
+                    if (e >= 0) continue;
+                    const int du = (int)(short)(e & 0xffff);
+                    const TA tu = (e & 0x40000000) ? TA(-1) : TA(1);
+                    if ((sfm[r] >> p) & 1u) {
+                        if (q.cnt == 2) slow = 1;
+                        else {
+                            q.du[q.cnt] = (signed char)du;
+                            q.src[q.cnt] = (unsigned char)max(osfsrc[r * g.npair + p], 0);
+                            q.c[q.cnt] = tu * osfc[r * g.npair + p];
+                            ++q.cnt;
+                        }
+                    }
+                    if ((phm[r] >> p) & 1u) {
+                        if (q.cnt == 2) slow = 1;
+                        else {
+                            q.du[q.cnt] = (signed char)du;
+                            q.src[q.cnt] = (unsigned char)max(ophsrc[r * g.npair + p], 0);
+                            q.c[q.cnt] = tu * ophc[r * g.npair + p];
+                            ++q.cnt;
+                        }
+                    }
+                }
+            }
+            oquad[r * nimp + iu] = q;
+        }
+    oflags[0] = slow;
+    oflags[1] = (int)itemmask;
+}
+
+// all threads: copy the rows and the descriptor of `item` into a stage
+// buffer and its descriptor buffer, and commit the group
+template <typename TX, typename TA, int R, int NT>
+__device__ __forceinline__ void hv_stage_item(const HvBatch<TA> &b, int item, TX *stage, unsigned *desc,
+                                              int dwords)
+{
+    const HvJobT<TA> &jb = b.job[hv_find_job(b, item)];
+    const int it = item - jb.item0;
+    const int ld = jb.ld;
+    constexpr int EPV = 16 / sizeof(TX);   // elements per 16-byte copy
+    const int nv = ld / EPV;
+    const TX *x = (const TX *)jb.x;
+    const unsigned *src_desc = jb.desc + (size_t)it * dwords;
+    for (int q = threadIdx.x; q < dwords / 4; q += NT) cp_async16(desc + 4 * q, src_desc + 4 * q);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int d = jb.items[it * R + r];
+        if (d < 0) continue;
+        const TX *src = x + (size_t)d * ld;
+        for (int q = threadIdx.x; q < nv; q += NT) {
+            const int u = q * EPV;
+            cp_async16(stage + ((u >> 5) * R + r) * 32 + (u & 31), src + u);
+        }
+    }
+    cp_async_commit();
+}
+
+template <typename TX, typename TA, typename TY, int R, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+k_hv_async(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict__ mdl, const DescGeom g)
+{
+    extern __shared__ __align__(16) unsigned char smem_async[];
+    const int nimp = mdl->nimp;
+    int ldmax = 0;
+    for (int i = 0; i < batch.njobs; ++i) ldmax = max(ldmax, batch.job[i].ld);
+    const int stage_elems = R * ldmax;
+    TX *stage0 = reinterpret_cast<TX *>(smem_async);
+    TX *stage1 = stage0 + stage_elems;
+    unsigned *desc0 = reinterpret_cast<unsigned *>(smem_async + ((2 * (size_t)stage_elems * sizeof(TX) + 15) & ~(size_t)15));
+    unsigned *desc1 = desc0 + g.words;
+    int *s_t4 = reinterpret_cast<int *>(desc1 + g.words);
+    __shared__ unsigned s_pmask[kMaxImp];
+    __shared__ double s_red[NT / 32];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NW = NT / 32;
+    for (int i = tid; i < mdl->npair * nimp; i += NT) s_t4[i] = mdl->t4[i];
+    for (int i = tid; i < nimp; i += NT) s_pmask[i] = mdl->pairmask[i];
+    __syncthreads();
+
+    int cur = hv_next_item(batch, (int)blockIdx.x);
+    if (cur >= 0) hv_stage_item<TX, TA, R, NT>(batch, cur, stage0, desc0, g.words);
+    int k = 0;
+    while (cur >= 0) {
+        const int buf = k & 1;
+        const int nxt = hv_next_item(batch, cur + (int)gridDim.x);
+        // buffers (k+1)&1 were released by the barrier that ended item k-1;
+        // one commit group per iteration either way
+        if (nxt >= 0) hv_stage_item<TX, TA, R, NT>(batch, nxt, buf ? stage0 : stage1, buf ? desc0 : desc1, g.words);
+        else cp_async_commit();
+
+        const HvJobT<TA> &jb = batch.job[hv_find_job(batch, cur)];
+        const int it = cur - jb.item0;
+        const int ld = jb.ld, nch = ld >> 5;
+        const TX *__restrict__ x = (const TX *)jb.x;
+        TY *__restrict__ y = (TY *)jb.y;
+        cp_async_wait_all_but_newest();   // this thread's copies of the current item
+        __syncthreads();                  // everyone's
+        const TX *S = buf ? stage1 : stage0;
+        const unsigned *dsc = buf ? desc1 : desc0;
+        const int *s_d = (const int *)(dsc + g.o_d);
+        const int *s_dcnt = (const int *)(dsc + g.o_dcnt);
+        const int *s_dtgt = (const int *)(dsc + g.o_dtgt);
+        const TA *s_dval = (const TA *)(dsc + g.o_dval);
+        const TA *s_crossT = (const TA *)(dsc + g.o_cross);
+        const Quad<TA> *s_q = (const Quad<TA> *)(dsc + g.o_quad);
+        const int *s_sfsrc = (const int *)(dsc + g.o_sfsrc), *s_phsrc = (const int *)(dsc + g.o_phsrc);
+        const TA *s_sfc = (const TA *)(dsc + g.o_sfc), *s_phc = (const TA *)(dsc + g.o_phc);
+        const unsigned *s_rowmask = dsc + g.o_rowmask;
+        const bool slow = ((const int *)(dsc + g.o_flags))[0] != 0;
+        const unsigned imask = (unsigned)((const int *)(dsc + g.o_flags))[1];
+        const int dm = g.dm, npr = g.npair;
+
+        TA ddiag[R];
+        bool live[R];
+        int dcnt[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            ddiag[r] = ((const TA *)(dsc + g.o_ddiag))[r];
+            live[r] = s_d[r] >= 0;
+            dcnt[r] = s_dcnt[r];
+        }
+        const bool want_dot = jb.dot_partial != nullptr;
+        double dacc = 0.0;
+        constexpr int SB = 4;
+        constexpr int DB = 4;
+        for (int cb = warp; cb < nch; cb += NW * kHvCh) {
+            // chunks cb + NW*q, q < kHvCh; column of this lane in chunk q: ub + 32*NW*q
+            const int ub = 32 * cb + lane;
+            bool has[kHvCh];
+            int iu[kHvCh];
+            int2 h[kHvCh];
+            TA acc[kHvCh][R];
+#pragma unroll
+            for (int q = 0; q < kHvCh; ++q) {
+                has[q] = cb + NW * q < nch;
+                h[q] = has[q] ? __ldg(jb.up_sched_hdr + cb + NW * q) : make_int2(0, 0);
+            }
+            // the first DB down-spin moves of every row: loads in flight early
+            TX gd[R][DB][kHvCh];
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+#pragma unroll
+                for (int t = 0; t < DB; ++t) {
+                    const bool mv = t < dcnt[r];
+                    const TX *xr = x + (size_t)s_dtgt[r * dm + (mv ? t : 0)] * ld + ub;
+#pragma unroll
+                    for (int q = 0; q < kHvCh; ++q) gd[r][t][q] = (mv && has[q]) ? __ldg(xr + 32 * NW * q) : TX(0);
+                }
+            // first SB schedule entries of every chunk
+            HopEnt<TA> e0[kHvCh][SB];
+#pragma unroll
+            for (int q = 0; q < kHvCh; ++q)
+#pragma unroll
+                for (int t = 0; t < SB; ++t)
+                    e0[q][t] = (t < h[q].y) ? jb.up_sched[h[q].x + 32 * t + lane] : HopEnt<TA>{};
+            // diagonal
+#pragma unroll
+            for (int q = 0; q < kHvCh; ++q) {
+                const int u = ub + 32 * NW * q;
+                int inf = 0;
+                TA ud = TA(0);
+                if (has[q]) {
+                    inf = __ldg(jb.up_info + u);
+                    ud = __ldg(jb.up_diag + u);
+                }
+                iu[q] = (inf >> 8) & 0xff;
+#pragma unroll
+                for (int r = 0; r < R; ++r) acc[q][r] = TA(0);
+                if (has[q]) {
+                    const TX *so = S + ((u >> 5) * R) * 32 + (u & 31);
+#pragma unroll
+                    for (int r = 0; r < R; ++r)
+                        acc[q][r] = (ud + ddiag[r] + s_crossT[iu[q] * R + r]) * (TA)so[32 * r];
+                }
+            }
+            // up-spin hybridisation: scheduled conflict-free gathers
+#pragma unroll
+            for (int q = 0; q < kHvCh; ++q) {
+                const int ns = h[q].y;
+                const HopEnt<TA> *tab = jb.up_sched + h[q].x + lane;
+                HopEnt<TA> e[SB];
+#pragma unroll
+                for (int t = 0; t < SB; ++t) e[t] = e0[q][t];
+                for (int s0 = 0; s0 < ns; s0 += SB) {
+                    HopEnt<TA> f[SB];
+#pragma unroll
+                    for (int t = 0; t < SB; ++t) f[t] = (s0 + SB + t < ns) ? tab[32 * (s0 + SB + t)] : HopEnt<TA>{};
+#pragma unroll
+                    for (int t = 0; t < SB; ++t) {
+                        if (s0 + t < ns) {
+                            const TX *st = S + e[t].t;
+#pragma unroll
+                            for (int r = 0; r < R; ++r) acc[q][r] += e[t].v * (TA)st[32 * r];
+                        }
+                    }
+#pragma unroll
+                    for (int t = 0; t < SB; ++t) e[t] = f[t];
+                }
+            }
+            // spin-flip and pair hopping (partner rows staged)
+#pragma unroll
+            for (int q = 0; q < kHvCh; ++q) {
+                if (!has[q]) continue;
+                const int u = ub + 32 * NW * q;
+                if (!slow) {
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        const Quad<TA> qd = s_q[r * nimp + iu[q]];
+                        if (qd.cnt > 0) {
+#pragma unroll
+                            for (int t = 0; t < 2; ++t) {
+                                if (t < qd.cnt) {
+                                    const int w = u + qd.du[t];
+                                    acc[q][r] += qd.c[t] * (TA)S[((w >> 5) * R + qd.src[t]) * 32 + (w & 31)];
+                                }
+                            }
+                        }
+                    }
+                } else {
+                    unsigned pm = s_pmask[iu[q]] & imask;
+                    while (pm) {
+                        const int p = __ffs(pm) - 1;
+                        pm &= pm - 1;
+                        const int e = s_t4[p * nimp + iu[q]];
+                        const int w = u + (int)(short)(e & 0xffff);
+                        const bool neg = (e & 0x40000000) != 0;
+                        const unsigned rm = s_rowmask[p];
+#pragma unroll
+                        for (int r = 0; r < R; ++r) {
+                            if ((rm >> r) & 1u) {
+                                const int src = s_sfsrc[r * npr + p];
+                                const TX xv = src >= 0 ? S[((w >> 5) * R + src) * 32 + (w & 31)]
+                                                       : __ldg(x + (size_t)(-1 - src) * ld + w);
+                                const TA cf = neg ? -s_sfc[r * npr + p] : s_sfc[r * npr + p];
+                                acc[q][r] += cf * (TA)xv;
+                            }
+                            if ((rm >> (16 + r)) & 1u) {
+                                const int src = s_phsrc[r * npr + p];
+                                const TX xv = src >= 0 ? S[((w >> 5) * R + src) * 32 + (w & 31)]
+                                                       : __ldg(x + (size_t)(-1 - src) * ld + w);
+                                const TA cf = neg ? -s_phc[r * npr + p] : s_phc[r * npr + p];
+                                acc[q][r] += cf * (TA)xv;
+                            }
+                        }
+                    }
+                }
+            }
+            // down-spin hybridisation: the early loads, then the remaining moves
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+#pragma unroll
+                for (int t = 0; t < DB; ++t) {
+                    if (t < dcnt[r]) {
+                        const TA v = s_dval[r * dm + t];
+#pragma unroll
+                        for (int q = 0; q < kHvCh; ++q) acc[q][r] += v * (TA)gd[r][t][q];
+                    }
+                }
+                for (int t0 = DB; t0 < dcnt[r]; t0 += DB) {
+                    TX g2[DB][kHvCh];
+#pragma unroll
+                    for (int t = 0; t < DB; ++t) {
+                        const bool mv = t0 + t < dcnt[r];
+                        const TX *xr = x + (size_t)s_dtgt[r * dm + (mv ? t0 + t : t0)] * ld + ub;
+#pragma unroll
+                        for (int q = 0; q < kHvCh; ++q) g2[t][q] = (mv && has[q]) ? __ldg(xr + 32 * NW * q) : TX(0);
+                    }
+#pragma unroll
+                    for (int t = 0; t < DB; ++t) {
+                        if (t0 + t < dcnt[r]) {
+                            const TA v = s_dval[r * dm + t0 + t];
+#pragma unroll
+                            for (int q = 0; q < kHvCh; ++q) acc[q][r] += v * (TA)g2[t][q];
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                if (!live[r]) continue;
+                TY *yr = y + (size_t)s_d[r] * ld + ub;
+#pragma unroll
+                for (int q = 0; q < kHvCh; ++q)
+                    if (has[q]) yr[32 * NW * q] = (TY)acc[q][r];
+            }
+            if (want_dot) {
+                TA part = TA(0);
+#pragma unroll
+                for (int q = 0; q < kHvCh; ++q) {
+                    if (!has[q]) continue;
+                    const int u = ub + 32 * NW * q;
+                    const TX *so = S + ((u >> 5) * R) * 32 + (u & 31);
+#pragma unroll
+                    for (int r = 0; r < R; ++r)
+                        if (live[r]) part += (TA)so[32 * r] * (TA)(TY)acc[q][r];
+                }
+                dacc += (double)part;
+            }
+        }
+        if (want_dot) {
+            for (int off = 16; off > 0; off >>= 1) dacc += __shfl_down_sync(0xffffffffu, dacc, off);
+            if (lane == 0) s_red[warp] = dacc;
+        }
+        __syncthreads();   // item done: its buffers are free
+        if (want_dot && tid == 0) {
+            double t = 0.0;
+            for (int w = 0; w < NW; ++w) t += s_red[w];
+            jb.dot_partial[it] = t;
+        }
+        cur = nxt;
+        ++k;
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
+template <typename TX, typename TA, int R>
+static size_t dyn_smem_bytes_async(int ld, const ModelDev &m, const DescGeom &g)
+{
+    return ((2 * (size_t)R * ld * sizeof(TX) + 15) & ~(size_t)15) + sizeof(unsigned) * 2 * (size_t)g.words +
+           sizeof(int) * (size_t)m.npair * m.nimp;
+}
+
+// ---------------------------------------------------------------------------
 // tile-shape variants and the autotuner
 // ---------------------------------------------------------------------------
-// A variant fixes the rows per item R, the CTA size NT and the CTAs per SM the
-// register budget is cut for (MINB).  All variants compute every element with
-// the same sequence of operations, so their outputs are bit-identical; only
-// the speed differs.  The first H*v of a (kind, Nup, Ndn) shape times each
-// variant on that sector (scratch vectors, CUDA events on the context stream)
-// and keeps the fastest.
+// A variant fixes the kernel (k_hv or k_hv_async), the rows per item R, the CTA
+// size NT and the CTAs per SM the register budget is cut for (MINB).  The
+// k_hv variants compute every element with the same sequence of operations
+// (bit-identical outputs); k_hv_async adds the up-spin terms in the order of
+// the gather schedule, so FP32 outputs of the two kernels agree to rounding.
+// The first H*v of a (kind, Nup, Ndn) shape times each variant on that sector
+// (scratch vectors, CUDA events on the context stream) and keeps the fastest.
 struct HvVariant {
     int R, NT, MINB;
+    int staged; // 1: k_hv_async (double-buffered asynchronous stage), 0: k_hv
 };
-static const HvVariant kVarF32[] = {{3, 512, 2}, {4, 256, 2}, {6, 512, 1}, {3, 256, 3}, {8, 512, 1}};
-static const HvVariant kVarF64[] = {{2, 256, 2}, {3, 256, 1}, {2, 512, 1}};
+static const HvVariant kVarF32[] = {{3, 512, 2, 0}, {4, 256, 2, 0}, {6, 512, 1, 0}, {3, 256, 3, 0}, {8, 512, 1, 0},
+                                    {4, 512, 1, 1}, {3, 512, 1, 1}, {2, 512, 2, 1}, {2, 256, 2, 1}};
+static const HvVariant kVarF64[] = {{2, 256, 2, 0}, {3, 256, 1, 0}, {2, 512, 1, 0}, {2, 512, 1, 1}, {4, 512, 1, 1}};
 static const int kNVarF32 = sizeof(kVarF32) / sizeof(kVarF32[0]);
 static const int kNVarF64 = sizeof(kVarF64) / sizeof(kVarF64[0]);
 
@@ -505,6 +1012,19 @@ void hv_fill_job(const mo_ed_ctx *ctx, const Sector &s, int R, const void *x, vo
     j.dn_diag = f32 ? (const TA *)s.dn->diag_f : (const TA *)s.dn->diag_d;
     j.dn_maxcnt = s.dn->max_cnt;
     j.pad = 0;
+    j.up_sched_hdr = s.up->sched_hdr;
+    j.up_sched_ent = s.up->sched_ent;
+    {
+        auto dsc = s.dn->desc.find(R * 2 + (f32 ? 0 : 1));
+        j.desc = dsc != s.dn->desc.end() ? dsc->second : nullptr;
+    }
+    if (f32) {
+        auto sf = s.up->sched_rf.find(R);
+        j.up_sched = sf != s.up->sched_rf.end() ? (const HopEnt<TA> *)sf->second : nullptr;
+    } else {
+        auto sd = s.up->sched_rd.find(R);
+        j.up_sched = sd != s.up->sched_rd.end() ? (const HopEnt<TA> *)sd->second : nullptr;
+    }
 }
 template void hv_fill_job<float>(const mo_ed_ctx *, const Sector &, int, const void *, void *, HvJobT<float> &);
 template void hv_fill_job<double>(const mo_ed_ctx *, const Sector &, int, const void *, void *, HvJobT<double> &);
@@ -531,6 +1051,63 @@ static int launch_batch(mo_ed_ctx *ctx, const HvBatch<TA> &b)
     return MO_ED_OK;
 }
 
+template <typename TX, typename TA, typename TY, int R, int NT, int MINB = 1>
+static int launch_batch_async(mo_ed_ctx *ctx, const HvBatch<TA> &b)
+{
+    if (b.total_items <= 0) return MO_ED_OK;
+    int ldmax = 0;
+    for (int i = 0; i < b.njobs; ++i) {
+        ldmax = std::max(ldmax, b.job[i].ld);
+        if (!b.job[i].items || !b.job[i].up_sched_hdr || !b.job[i].up_sched || !b.job[i].desc)
+            return fail(ctx, MO_ED_ERR_STATE, "H*v tables missing");
+    }
+    const DescGeom g = desc_geom<TA, R>(ctx->mdl.ncpl, ctx->mdl);
+    const size_t smem = dyn_smem_bytes_async<TX, TA, R>(ldmax, ctx->mdl, g);
+    auto kern = k_hv_async<TX, TA, TY, R, NT, MINB>;
+    MOED_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MOED_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    int per_sm = 0;
+    MOED_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem));
+    if (per_sm < 1) return fail(ctx, MO_ED_ERR_ARG, "sector rows too long for the shared-memory stage");
+    const int grid = std::min(b.total_items, ctx->num_sms * per_sm);
+    kern<<<grid, NT, smem, ctx->stream>>>(b, ctx->d_mdl, g);
+    MOED_CHECK_LAUNCH(ctx);
+    return MO_ED_OK;
+}
+
+template <typename TA, int R>
+static int build_desc_r(mo_ed_ctx *ctx, Species *dn, unsigned **out)
+{
+    const DescGeom g = desc_geom<TA, R>(ctx->mdl.ncpl, ctx->mdl);
+    const int n = dn->nitems.at(R);
+    unsigned *p = nullptr;
+    MOED_CUDA(ctx, cudaMalloc(&p, sizeof(unsigned) * (size_t)g.words * std::max(n, 1)));
+    *out = p;
+    const bool f32 = sizeof(TA) == 4;
+    k_item_desc<TA, R><<<(n + 127) / 128, 128, 0, ctx->stream>>>(
+        n, dn->items.at(R), dn->info, f32 ? (const TA *)dn->diag_f : (const TA *)dn->diag_d, dn->hop_tgt,
+        f32 ? (const TA *)dn->hop_val_f : (const TA *)dn->hop_val_d, dn->n, ctx->d_mdl, g, p);
+    MOED_CHECK_LAUNCH(ctx);
+    return MO_ED_OK;
+}
+
+// item descriptors of the down species for R rows per item (k_hv_async)
+static int species_desc(mo_ed_ctx *ctx, Species *dn, int R, bool f32)
+{
+    const int key = R * 2 + (f32 ? 0 : 1);
+    if (dn->desc.count(key)) return MO_ED_OK;
+    unsigned *p = nullptr;
+    int rc;
+    switch (R) {
+    case 2: rc = f32 ? build_desc_r<float, 2>(ctx, dn, &p) : build_desc_r<double, 2>(ctx, dn, &p); break;
+    case 3: rc = f32 ? build_desc_r<float, 3>(ctx, dn, &p) : build_desc_r<double, 3>(ctx, dn, &p); break;
+    case 4: rc = f32 ? build_desc_r<float, 4>(ctx, dn, &p) : build_desc_r<double, 4>(ctx, dn, &p); break;
+    default: return fail(ctx, MO_ED_ERR_ARG, "no item descriptors for this rows-per-item");
+    }
+    if (p) dn->desc[key] = p;
+    return rc;
+}
+
 template <typename TA>
 static int launch_variant(mo_ed_ctx *ctx, int kind, int v, const HvBatch<TA> &b)
 {
@@ -541,19 +1118,27 @@ static int launch_variant(mo_ed_ctx *ctx, int kind, int v, const HvBatch<TA> &b)
         case 1: return launch_batch<float, float, float, 4, 256, 2>(ctx, b);
         case 2: return launch_batch<float, float, float, 6, 512, 1>(ctx, b);
         case 3: return launch_batch<float, float, float, 3, 256, 3>(ctx, b);
-        default: return launch_batch<float, float, float, 8, 512, 1>(ctx, b);
+        case 4: return launch_batch<float, float, float, 8, 512, 1>(ctx, b);
+        case 5: return launch_batch_async<float, float, float, 4, 512>(ctx, b);
+        case 6: return launch_batch_async<float, float, float, 3, 512>(ctx, b);
+        case 7: return launch_batch_async<float, float, float, 2, 512, 2>(ctx, b);
+        default: return launch_batch_async<float, float, float, 2, 256, 2>(ctx, b);
         }
     } else if (kind == HV_F64) {
         switch (v) {
         case 0: return launch_batch<double, double, double, 2, 256, 2>(ctx, b);
         case 1: return launch_batch<double, double, double, 3, 256, 1>(ctx, b);
-        default: return launch_batch<double, double, double, 2, 512, 1>(ctx, b);
+        case 2: return launch_batch<double, double, double, 2, 512, 1>(ctx, b);
+        case 3: return launch_batch_async<double, double, double, 2, 512>(ctx, b);
+        default: return launch_batch_async<double, double, double, 4, 512>(ctx, b);
         }
     } else {
         switch (v) {
         case 0: return launch_batch<float, double, double, 2, 256, 2>(ctx, b);
         case 1: return launch_batch<float, double, double, 3, 256, 1>(ctx, b);
-        default: return launch_batch<float, double, double, 2, 512, 1>(ctx, b);
+        case 2: return launch_batch<float, double, double, 2, 512, 1>(ctx, b);
+        case 3: return launch_batch_async<float, double, double, 2, 512>(ctx, b);
+        default: return launch_batch_async<float, double, double, 4, 512>(ctx, b);
         }
     }
 }
@@ -601,6 +1186,19 @@ static int launch_one(mo_ed_ctx *ctx, const Sector &s, int kind, int v, const vo
     return hv_launch_f64(ctx, kind, v, &j, 1);
 }
 
+// tables variant v of `kind` reads for sector s: the item table of its R,
+// and for the staged kernel the up-spin schedule and the item descriptors
+static int prepare_variant(mo_ed_ctx *ctx, const Sector &s, int kind, int v)
+{
+    const HvVariant &h = variant(kind, v);
+    const int *items;
+    int n;
+    if (int rc = species_items(ctx, s.dn, h.R, &items, &n)) return rc;
+    if (!h.staged) return MO_ED_OK;
+    if (int rc = species_sched(ctx, s.up, h.R)) return rc;
+    return species_desc(ctx, s.dn, h.R, kind == HV_F32);
+}
+
 // Time every variant once on sector s and keep the fastest.
 static int tune(mo_ed_ctx *ctx, const Sector &s, int kind, int *best)
 {
@@ -618,9 +1216,7 @@ static int tune(mo_ed_ctx *ctx, const Sector &s, int kind, int *best)
     std::vector<float> &times = ctx->hv_times[shape_key(kind, s)];
     times.assign(nvariants(kind), -1.0f);
     for (int v = 0; v < nvariants(kind); ++v) {
-        const int *items;
-        int n;
-        if (int rc = species_items(ctx, s.dn, variant(kind, v).R, &items, &n)) return rc;
+        if (int rc = prepare_variant(ctx, s, kind, v)) return rc;
         if (launch_one(ctx, s, kind, v, dx.p, dy.p) != MO_ED_OK) {   // variant does not fit this sector
             cudaGetLastError();
             continue;
@@ -659,9 +1255,7 @@ int hv_prepare(mo_ed_ctx *ctx, const Sector &s, int kind, int *v_out, int *R_out
         if (int rc = tune(ctx, s, kind, &v)) return rc;
         ctx->hv_choice[key] = v;
     }
-    const int *items;
-    int n;
-    if (int rc = species_items(ctx, s.dn, variant(kind, v).R, &items, &n)) return rc;
+    if (int rc = prepare_variant(ctx, s, kind, v)) return rc;
     if (v_out) *v_out = v;
     if (R_out) *R_out = variant(kind, v).R;
     return MO_ED_OK;
@@ -677,20 +1271,19 @@ int hv_tuning(mo_ed_ctx *ctx, const Sector &s, int kind, int cap, int *nvar, int
     for (int i = 0; i < *nvar && i < cap; ++i) {
         const HvVariant &h = variant(kind, i);
         if (shape) {
-            shape[3 * i] = h.R;
-            shape[3 * i + 1] = h.NT;
-            shape[3 * i + 2] = h.MINB;
+            shape[4 * i] = h.R;
+            shape[4 * i + 1] = h.NT;
+            shape[4 * i + 2] = h.MINB;
+            shape[4 * i + 3] = h.staged;
         }
         if (ms) ms[i] = i < (int)t.size() ? t[i] : -1.0f;
     }
     return MO_ED_OK;
 }
 
-int hv_prepare_rows(mo_ed_ctx *ctx, const Sector &s, int R)
+int hv_prepare_rows(mo_ed_ctx *ctx, const Sector &s, int kind, int v)
 {
-    const int *items;
-    int n;
-    return species_items(ctx, s.dn, R, &items, &n);
+    return prepare_variant(ctx, s, kind, v);
 }
 
 int hv_lookup(mo_ed_ctx *ctx, const Sector &s, int kind, int *v_out, int *R_out)
@@ -698,11 +1291,22 @@ int hv_lookup(mo_ed_ctx *ctx, const Sector &s, int kind, int *v_out, int *R_out)
     auto it = ctx->hv_choice.find(shape_key(kind, s));
     if (it == ctx->hv_choice.end())
         return fail(ctx, MO_ED_ERR_STATE, "H*v tile shape of this sector not chosen yet");
-    const int R = variant(kind, it->second).R;
-    if (s.dn->items.find(R) == s.dn->items.end())
-        return fail(ctx, MO_ED_ERR_STATE, "H*v item table of this sector not built yet");
+    const HvVariant &h = variant(kind, it->second);
+    const int R = h.R;
+    bool ready = s.dn->items.count(R) != 0;
+    if (h.staged)
+        ready = ready && s.up->sched_rf.count(R) && s.dn->desc.count(R * 2 + (kind == HV_F32 ? 0 : 1));
+    if (!ready) return fail(ctx, MO_ED_ERR_STATE, "H*v item table of this sector not built yet");
     if (v_out) *v_out = it->second;
     if (R_out) *R_out = R;
+    return MO_ED_OK;
+}
+
+int hv_set_variant(mo_ed_ctx *ctx, const Sector &s, int kind, int v)
+{
+    if (v < 0 || v >= nvariants(kind)) return fail(ctx, MO_ED_ERR_ARG, "H*v variant out of range");
+    if (int rc = prepare_variant(ctx, s, kind, v)) return rc;
+    ctx->hv_choice[shape_key(kind, s)] = v;
     return MO_ED_OK;
 }
 

@@ -90,12 +90,29 @@ struct Species {
     // columns as one contiguous 32-byte (FP32) / 64-byte (FP64) block
     HopEnt<float> *tab_f = nullptr;
     HopEnt<double> *tab_d = nullptr;
+    // conflict-free gather schedule of the up-spin moves: per 32-column chunk
+    // c, sched_hdr[c] = {first entry, slots}; entry (slot s, lane l) at
+    // first + 32*s + l is 0 (no move) or valid | neg << 22 | coupling << 16 |
+    // target rank.  Within a slot the 32 targets fall in 32 different
+    // shared-memory banks (target mod 32).
+    int2 *sched_hdr = nullptr;
+    unsigned *sched_ent = nullptr;
+    std::vector<int2> h_sched_hdr;    // host copies (per-R tables derive from them)
+    std::vector<unsigned> h_sched_ent;
+    int sched_slots_max = 0;
+    // per rows-per-item R: the schedule as {shared-memory offset of row 0 in
+    // the [tile][R][32] stage, signed coupling}; empty lanes read a bank that
+    // no other lane of the slot uses, with coupling 0
+    std::map<int, HopEnt<float> *> sched_rf;
+    std::map<int, HopEnt<double> *> sched_rd;
     int max_cnt = 0;              // largest hop_cnt over words
     int max_group = 0;            // largest bath group (words sharing their bath bits)
     // row items for a given rows-per-item R: whole bath groups packed into
     // items of <= R rows (rank order inside a group), items sorted by the
     // bath-occupation counts of the conserved subsystems; -1 pads
     std::map<int, int *> items;   // R -> [nitems][R]
+    // per-item descriptors of the staged H*v kernel, key R*2 + (FP64 ? 1 : 0)
+    std::map<int, unsigned *> desc;
     std::map<int, int> nitems;
     ~Species();
 };
@@ -129,6 +146,10 @@ struct HvJobT {
     const TA *dn_val;         // [hw][nd]
     const TA *dn_diag;        // [nd]
     int dn_maxcnt, pad;
+    const int2 *up_sched_hdr;      // conflict-free gather schedule (Species::sched_*)
+    const unsigned *up_sched_ent;
+    const HopEnt<TA> *up_sched;
+    const unsigned *desc;          // per-item descriptors (staged kernel)
 };
 
 // ---------------------------------------------------------------------------
@@ -273,11 +294,16 @@ int species_items(mo_ed_ctx *ctx, Species *sp, int R, const int **items, int *ni
 int hv_prepare(mo_ed_ctx *ctx, const Sector &s, int kind, int *v, int *R);
 // autotuner record of a shape: per variant (R, NT, MINB) and time in ms
 int hv_tuning(mo_ed_ctx *ctx, const Sector &s, int kind, int cap, int *nvar, int *shape, float *ms, int *chosen);
-// item table for R rows per item (sectors batched with a tuned one)
-int hv_prepare_rows(mo_ed_ctx *ctx, const Sector &s, int R);
+// tables of variant v (item table, schedule, descriptors) for a sector
+// batched with the one v was tuned on
+int hv_prepare_rows(mo_ed_ctx *ctx, const Sector &s, int kind, int v);
+// Per-R stage offsets of the up-spin gather schedule (built once per R).
+int species_sched(mo_ed_ctx *ctx, Species *sp, int R);
 // Lookup only: the tile shape and item table that hv_prepare left for this
 // sector and kind, or MO_ED_ERR_STATE if it never ran (never tunes or allocates).
 int hv_lookup(mo_ed_ctx *ctx, const Sector &s, int kind, int *v, int *R);
+// Pin the tile-shape variant of a sector and kind (instead of the autotuner's choice).
+int hv_set_variant(mo_ed_ctx *ctx, const Sector &s, int kind, int v);
 // Convenience: one vector, jobs staged through scratch.
 int hv_single(mo_ed_ctx *ctx, const Sector &s, int kind, const void *x, void *y);
 

@@ -125,6 +125,38 @@ int convert_f32_to_f64(mo_ed_ctx *ctx, const float *in, double *out, long long n
     return MO_ED_OK;
 }
 
+// 16-byte vector access to 4 consecutive elements (vectors are padded to a
+// multiple of 32 elements and 256-byte aligned)
+template <typename T>
+__device__ __forceinline__ void vload4(const T *p, T (&r)[4])
+{
+    if constexpr (sizeof(T) == 4) {
+        const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
+        r[0] = a.x;
+        r[1] = a.y;
+        r[2] = a.z;
+        r[3] = a.w;
+    } else {
+        const double2 a = __ldg(reinterpret_cast<const double2 *>(p));
+        const double2 b = __ldg(reinterpret_cast<const double2 *>(p) + 1);
+        r[0] = a.x;
+        r[1] = a.y;
+        r[2] = b.x;
+        r[3] = b.y;
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void vstore4(T *p, const T (&r)[4])
+{
+    if constexpr (sizeof(T) == 4) {
+        *reinterpret_cast<float4 *>(p) = make_float4(r[0], r[1], r[2], r[3]);
+    } else {
+        reinterpret_cast<double2 *>(p)[0] = make_double2(r[0], r[1]);
+        reinterpret_cast<double2 *>(p)[1] = make_double2(r[2], r[3]);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // reference recurrence, batched
 // ---------------------------------------------------------------------------
@@ -156,6 +188,8 @@ __global__ void k_lz_norm0(const __grid_constant__ LzBatchDev b)
 // step j >= 1: u_j = s (w - a_{j-1} u_{j-1}) - c u_{j-2},  s = 1/sqrt(b_{j-1}),
 // c = sqrt(b_{j-1}/b_{j-2}) -- ed_lanczos.F90:38 (j = 1) and :54 (j >= 2)
 // with the reference's normalized vectors written as scaled stored ones.
+// 4 consecutive elements per thread (16-byte accesses; run lengths are
+// multiples of 32 elements).
 template <typename T>
 __global__ void k_lz_update(const __grid_constant__ LzBatchDev b, int j)
 {
@@ -175,18 +209,21 @@ __global__ void k_lz_update(const __grid_constant__ LzBatchDev b, int j)
         const T *up = (const T *)R.u[(j + 1) % 3];   // (j-2) mod 3
         T *un = (T *)R.u[j % 3];
         double acc = 0.0;
-        if (j >= 2) {
-            for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-                T v = s * (w[i] - a * uc[i]) - c * up[i];
-                un[i] = v;
-                acc += (double)(v * v);
+        for (long long i = i0 + 4 * threadIdx.x; i < i1; i += 4 * blockDim.x) {
+            T wv[4], cv[4], pv[4], v[4];
+            vload4(w + i, wv);
+            vload4(uc + i, cv);
+            if (j >= 2) {
+                vload4(up + i, pv);
+            } else {
+                pv[0] = pv[1] = pv[2] = pv[3] = T(0);
             }
-        } else {
-            for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-                T v = s * (w[i] - a * uc[i]);
-                un[i] = v;
-                acc += (double)(v * v);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                v[e] = (j >= 2) ? s * (wv[e] - a * cv[e]) - c * pv[e] : s * (wv[e] - a * cv[e]);
+                acc += (double)(v[e] * v[e]);
             }
+            vstore4(un + i, v);
         }
         double t = block_sum(acc, sred);
         if (threadIdx.x == 0) R.upd_part[it] = t;
@@ -263,7 +300,7 @@ int lz_setup(mo_ed_ctx *ctx, LzBatch &b, const std::vector<Sector> &secs, int pr
         if (secs[r].D() > secs[big].D()) big = r;
     if (int rc = hv_prepare(ctx, secs[big], kind, &b.hv_variant, &b.hv_rows)) return rc;
     for (int r = 0; r < nrun; ++r) {
-        if (int rc = hv_prepare_rows(ctx, secs[r], b.hv_rows)) return rc;
+        if (int rc = hv_prepare_rows(ctx, secs[r], kind, b.hv_variant)) return rc;
         b.upd_item0[r] = b.upd_total;
         b.upd_nitems[r] = (int)((secs[r].Dpad() + kVecChunk - 1) / kVecChunk);
         b.upd_total += b.upd_nitems[r];
@@ -500,58 +537,74 @@ int lanczos_reference_in(mo_ed_ctx *ctx, const Sector &s, const double *h_vec, i
 // thick-restart Lanczos with full reorthogonalisation (diag replacement)
 // ---------------------------------------------------------------------------
 constexpr int kMaxNcv = 200;
-constexpr int kMdTile = 2048;      // elements per multi-dot tile
 
 template <typename T>
 struct VPtrs {
     const T *p[kMaxNcv + 1];
 };
 
-// part[b][l] = sum over block b's tiles of V_l . w
+template <typename T>
+struct alignas(16) V4Raw {
+    T v[4];
+};
+
+// part[b][l] = block b's share of V_l . w for l < nv.  Threads walk 4
+// consecutive elements at a time (16-byte loads), w once per pass, and keep
+// one accumulator per vector: up to kDotPass vectors per pass over w.
+// Products are summed in the vector precision over 8 quads (32 elements),
+// then in FP64; block sums in FP64 in a fixed order.
+constexpr int kDotPass = 24;
+
 template <typename T>
 __global__ void __launch_bounds__(kVecThreads)
 k_multidot(const __grid_constant__ VPtrs<T> V, int nv, const T *__restrict__ w, long long D,
            double *part)
 {
-    __shared__ T sw[kMdTile];
-    constexpr int kWarps = kVecThreads / 32;
-    constexpr int kPerWarp = (kMaxNcv + 1 + kWarps - 1) / kWarps;
-    double acc[kPerWarp];
-#pragma unroll
-    for (int i = 0; i < kPerWarp; ++i) acc[i] = 0.0;
+    __shared__ double sred[kVecThreads / 32][kDotPass];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const long long ntile = (D + kMdTile - 1) / kMdTile;
-    for (long long t = blockIdx.x; t < ntile; t += gridDim.x) {
-        const long long i0 = t * kMdTile;
-        const int len = (int)min((long long)kMdTile, D - i0);
-        __syncthreads();
-        for (int i = threadIdx.x; i < len; i += kVecThreads) sw[i] = w[i0 + i];
-        __syncthreads();
+    for (int l0 = 0; l0 < nv; l0 += kDotPass) {
+        const int np = min(kDotPass, nv - l0);
+        double acc[kDotPass];
+        T sacc[kDotPass];
 #pragma unroll
-        for (int k = 0; k < kPerWarp; ++k) {
-            const int l = wid + k * kWarps;
-            if (l < nv) {
-                const T *v = V.p[l] + i0;
-                T s = T(0);
-                double sd = 0.0;
-                int c = 0;
-                for (int i = lane; i < len; i += 32) {
-                    s += v[i] * sw[i];
-                    if (++c == 8) {
-                        sd += (double)s;
-                        s = T(0);
-                        c = 0;
-                    }
+        for (int l = 0; l < kDotPass; ++l) {
+            acc[l] = 0.0;
+            sacc[l] = T(0);
+        }
+        int cnt = 0;
+        for (long long i = 4 * (blockIdx.x * (long long)blockDim.x + threadIdx.x); i < D;
+             i += 4 * (long long)gridDim.x * blockDim.x) {
+            T x[4];
+            vload4(w + i, x);
+#pragma unroll
+            for (int l = 0; l < kDotPass; ++l) {
+                if (l < np) {
+                    T a[4];
+                    vload4(V.p[l0 + l] + i, a);
+                    sacc[l] += a[0] * x[0] + a[1] * x[1] + a[2] * x[2] + a[3] * x[3];
                 }
-                acc[k] += sd + (double)s;
+            }
+            if (++cnt == 8) {
+#pragma unroll
+                for (int l = 0; l < kDotPass; ++l) {
+                    acc[l] += (double)sacc[l];
+                    sacc[l] = T(0);
+                }
+                cnt = 0;
             }
         }
-    }
 #pragma unroll
-    for (int k = 0; k < kPerWarp; ++k) {
-        const int l = wid + k * kWarps;
-        double v = warp_sum(acc[k]);
-        if (lane == 0 && l < nv) part[(size_t)blockIdx.x * nv + l] = v;
+        for (int l = 0; l < kDotPass; ++l) {
+            const double v = warp_sum(acc[l] + (double)sacc[l]);
+            if (lane == 0) sred[wid][l] = v;
+        }
+        __syncthreads();
+        for (int l = threadIdx.x; l < np; l += blockDim.x) {
+            double t = 0.0;
+            for (int q = 0; q < kVecThreads / 32; ++q) t += sred[q][l];
+            part[(size_t)blockIdx.x * nv + l0 + l] = t;
+        }
+        __syncthreads();
     }
 }
 
@@ -565,24 +618,41 @@ __global__ void k_reduce_cols(const double *part, int G, int nv, double *out)
     }
 }
 
-// w -= sum_l V_l h_l ; optional partial of ||w||^2
+// w -= sum_l V_l h_l ; optional partial of ||w||^2.  4 consecutive elements
+// per thread, 4 vectors' loads in flight.
 template <typename T>
 __global__ void __launch_bounds__(kVecThreads)
 k_multiaxpy(const __grid_constant__ VPtrs<T> V, int nv, const double *__restrict__ h, T *w,
             long long D, double *norm_part)
 {
-    __shared__ T sh[kMaxNcv + 1];
+    __shared__ T sh[kMaxNcv + 4];
     __shared__ double sred[32];
-    for (int l = threadIdx.x; l < nv; l += blockDim.x) sh[l] = (T)h[l];
+    for (int l = threadIdx.x; l < nv + 4; l += blockDim.x) sh[l] = l < nv ? (T)h[l] : T(0);
     __syncthreads();
     double acc = 0.0;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < D;
-         i += (long long)gridDim.x * blockDim.x) {
-        T s = T(0);
-        for (int l = 0; l < nv; ++l) s += V.p[l][i] * sh[l];
-        T v = w[i] - s;
-        w[i] = v;
-        acc += (double)(v * v);
+    for (long long i = 4 * (blockIdx.x * (long long)blockDim.x + threadIdx.x); i < D;
+         i += 4 * (long long)gridDim.x * blockDim.x) {
+        T s[4] = {T(0), T(0), T(0), T(0)};
+        for (int l = 0; l < nv; l += 4) {
+            T a[4][4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (l + q < nv) vload4(V.p[l + q] + i, a[q]);
+                else a[q][0] = a[q][1] = a[q][2] = a[q][3] = T(0);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) s[e] += a[q][e] * sh[l + q];
+        }
+        T x[4];
+        vload4(w + i, x);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            x[e] -= s[e];
+            acc += (double)(x[e] * x[e]);
+        }
+        vstore4(w + i, x);
     }
     if (norm_part) {
         double t = block_sum(acc, sred);
@@ -652,31 +722,37 @@ __global__ void k_random(T *x, long long n, int ld, int nu, unsigned long long s
     }
 }
 
-// X_c = sum_l V_l Y[l][c] for c in [c0, c0+KC)
+// X_c = sum_l V_l Y[l][c] for c in [c0, c0+KC).  Accumulated in the vector
+// precision (FP32 vectors: FP32; GB300 runs FP64 at a small fraction of the
+// FP32 rate), coefficients from shared memory, 4 vectors' loads in flight.
 template <typename T, int KC>
 __global__ void __launch_bounds__(kVecThreads)
 k_rotate(const __grid_constant__ VPtrs<T> V, int nv, const double *__restrict__ Y, int ldy, int c0,
          int nc, const __grid_constant__ VPtrs<T> X, long long D)
 {
-    __shared__ double sy[kMaxNcv * KC];
-    for (int idx = threadIdx.x; idx < nv * KC; idx += blockDim.x) {
+    __shared__ __align__(16) T sy[(kMaxNcv + 4) * KC];
+    for (int idx = threadIdx.x; idx < (nv + 4) * KC; idx += blockDim.x) {
         int l = idx / KC, c = idx - l * KC;
-        sy[idx] = (c < nc) ? Y[(size_t)(c0 + c) * ldy + l] : 0.0;
+        sy[idx] = (c < nc && l < nv) ? (T)Y[(size_t)(c0 + c) * ldy + l] : T(0);
     }
     __syncthreads();
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < D;
          i += (long long)gridDim.x * blockDim.x) {
-        double acc[KC];
+        T acc[KC];
 #pragma unroll
-        for (int c = 0; c < KC; ++c) acc[c] = 0.0;
-        for (int l = 0; l < nv; ++l) {
-            const double v = (double)V.p[l][i];
+        for (int c = 0; c < KC; ++c) acc[c] = T(0);
+        for (int l = 0; l < nv; l += 4) {
+            T v[4];
 #pragma unroll
-            for (int c = 0; c < KC; ++c) acc[c] += v * sy[l * KC + c];
+            for (int q = 0; q < 4; ++q) v[q] = (l + q < nv) ? V.p[l + q][i] : T(0);
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+#pragma unroll
+                for (int c = 0; c < KC; ++c) acc[c] += v[q] * sy[(l + q) * KC + c];
         }
 #pragma unroll
         for (int c = 0; c < KC; ++c)
-            if (c < nc) const_cast<T *>(X.p[c])[i] = (T)acc[c];
+            if (c < nc) const_cast<T *>(X.p[c])[i] = acc[c];
     }
 }
 
@@ -870,7 +946,7 @@ static int orthogonalize(mo_ed_ctx *ctx, const std::vector<DevBuf *> &basis, int
                          int G)
 {
     VPtrs<T> P = make_ptrs<T>(basis, nv);
-    const int Gm = (int)std::max(1LL, std::min((D + kMdTile - 1) / kMdTile, (long long)ctx->num_sms * 2));
+    const int Gm = (int)std::max(1LL, std::min((D / 4 + kVecThreads - 1) / kVecThreads, (long long)ctx->num_sms * 4));
     for (int pass = 0; pass < 2; ++pass) {
         double *h = pass == 0 ? h1 : h2;
         k_multidot<T><<<Gm, kVecThreads, 0, ctx->stream>>>(P, nv, w, D, part);
@@ -919,7 +995,7 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
     if (int rc = dev_alloc(ctx, dHp, sizeof(double) * (size_t)n2 * n2)) return rc;
     if (int rc = dev_alloc(ctx, dh1, sizeof(double) * n2)) return rc;
     if (int rc = dev_alloc(ctx, dh2, sizeof(double) * n2)) return rc;
-    if (int rc = dev_alloc(ctx, dpart, sizeof(double) * (size_t)n2 * ctx->num_sms * 2)) return rc;
+    if (int rc = dev_alloc(ctx, dpart, sizeof(double) * (size_t)n2 * ctx->num_sms * 4)) return rc;
     if (int rc = dev_alloc(ctx, dnorm, sizeof(double) * G)) return rc;
     if (int rc = dev_alloc(ctx, dbeta, sizeof(double) * 2)) return rc;
     if (int rc = dev_alloc(ctx, dA, sizeof(double) * (size_t)n2 * n2)) return rc;

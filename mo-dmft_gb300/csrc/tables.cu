@@ -50,7 +50,12 @@ Species::~Species()
     cudaFree(diag_f);
     cudaFree(tab_f);
     cudaFree(tab_d);
+    cudaFree(sched_hdr);
+    cudaFree(sched_ent);
+    for (auto &kv : sched_rf) cudaFree(kv.second);
+    for (auto &kv : sched_rd) cudaFree(kv.second);
     for (auto &kv : items) cudaFree(kv.second);
+    for (auto &kv : desc) cudaFree(kv.second);
 }
 
 // ---------------------------------------------------------------------------
@@ -401,6 +406,201 @@ int species_items(mo_ed_ctx *ctx, Species *sp, int R, const int **items, int *ni
     return MO_ED_OK;
 }
 
+// Up-spin gather schedule.  The moves of the 32 columns of a chunk are the
+// edges of a bipartite multigraph between lanes (output columns) and shared-
+// memory banks (target mod 32).  A proper edge colouring with Delta colours
+// (Delta = the largest lane or bank degree; Koenig's theorem) gives Delta
+// slots in which every lane has at most one move and every bank at most one
+// reader: each slot is one conflict-free shared-memory access per staged row.
+// Colouring: for edge (l, b), take a colour a free at l and c free at b; if a
+// is also free at b use it, else swap a and c along the alternating path that
+// starts at b (it cannot reach l), which frees a at b.
+namespace {
+struct EdgeColouring {
+    int delta;
+    std::vector<int> at;   // [node][colour] -> edge or -1; nodes 0..31 lanes, 32..63 banks
+    std::vector<int> col;  // edge -> colour
+    explicit EdgeColouring(int d) : delta(d), at(64 * d, -1) {}
+    int free_colour(int node) const
+    {
+        for (int c = 0; c < delta; ++c)
+            if (at[node * delta + c] < 0) return c;
+        return -1;
+    }
+};
+}  // namespace
+
+static void colour_chunk(const std::vector<int> &lane, const std::vector<int> &bank, int delta,
+                         std::vector<int> &colour)
+{
+    const int ne = (int)lane.size();
+    EdgeColouring g(delta);
+    g.col.assign(ne, -1);
+    auto other = [&](int e, int node) { return node < 32 ? 32 + bank[e] : lane[e]; };
+    for (int e = 0; e < ne; ++e) {
+        const int l = lane[e], b = 32 + bank[e];
+        const int a = g.free_colour(l), c = g.free_colour(b);
+        if (g.at[b * delta + a] >= 0) {
+            // alternating a/c path from b: collect its edges, then swap their colours
+            std::vector<int> path;
+            int node = b, want = a;
+            while (true) {
+                const int pe = g.at[node * delta + want];
+                if (pe < 0) break;
+                path.push_back(pe);
+                node = other(pe, node);
+                want = (want == a) ? c : a;
+            }
+            for (int pe : path) {
+                const int pc = g.col[pe];
+                g.at[lane[pe] * delta + pc] = -1;
+                g.at[(32 + bank[pe]) * delta + pc] = -1;
+            }
+            for (int pe : path) {
+                const int nc = (g.col[pe] == a) ? c : a;
+                g.col[pe] = nc;
+                g.at[lane[pe] * delta + nc] = pe;
+                g.at[(32 + bank[pe]) * delta + nc] = pe;
+            }
+        }
+        g.col[e] = a;
+        g.at[l * delta + a] = e;
+        g.at[b * delta + a] = e;
+    }
+    colour = g.col;
+}
+
+static int build_up_schedule(mo_ed_ctx *ctx, Species *s)
+{
+    const int nsite = ctx->nsite, N = s->N, n = s->n, nch = s->n_pad / 32;
+    std::vector<int> words;
+    std::vector<int> rank((size_t)1 << nsite, -1);
+    for (unsigned w = 0; w < (1u << nsite); ++w)
+        if (__builtin_popcount(w) == N) {
+            rank[w] = (int)words.size();
+            words.push_back((int)w);
+        }
+    auto parity_below_h = [](unsigned w, int bit) { return __builtin_popcount(w & ((1u << bit) - 1u)) & 1; };
+    const int ncpl = ctx->mdl.ncpl;
+    std::vector<int2> hdr(nch);
+    std::vector<unsigned> ent;
+    std::vector<int> el, eb, colour;
+    std::vector<unsigned> ecode;
+    int smax = 0;
+    for (int c = 0; c < nch; ++c) {
+        el.clear();
+        eb.clear();
+        ecode.clear();
+        int deg_l[32] = {0}, deg_b[32] = {0};
+        for (int l = 0; l < 32; ++l) {
+            const int u = 32 * c + l;
+            if (u >= n) continue;
+            const unsigned w = (unsigned)words[u];
+            for (int i = 0; i < ncpl; ++i) {   // the move rule of k_hops
+                const int o = ctx->cpl_orb[i], k = ctx->cpl_bath[i];
+                const int ob = (w >> o) & 1, kb = (w >> k) & 1;
+                int src, dst;
+                if (kb && !ob) {
+                    src = k;
+                    dst = o;
+                } else if (ob && !kb) {
+                    src = o;
+                    dst = k;
+                } else {
+                    continue;
+                }
+                const int s1 = parity_below_h(w, src);
+                const unsigned w1 = w & ~(1u << src);
+                const int s2 = parity_below_h(w1, dst);
+                const int t = rank[w1 | (1u << dst)];
+                el.push_back(l);
+                eb.push_back(t & 31);
+                ecode.push_back(0x80000000u | ((unsigned)((s1 ^ s2) & 1) << 22) | ((unsigned)i << 16) |
+                                (unsigned)t);
+                deg_l[l]++;
+                deg_b[t & 31]++;
+            }
+        }
+        int delta = 0;
+        for (int q = 0; q < 32; ++q) delta = std::max(delta, std::max(deg_l[q], deg_b[q]));
+        hdr[c] = make_int2((int)ent.size(), delta);
+        if (delta == 0) continue;
+        colour_chunk(el, eb, delta, colour);
+        const size_t base = ent.size();
+        ent.resize(base + (size_t)32 * delta, 0u);
+        for (size_t e = 0; e < el.size(); ++e) {
+            unsigned &slot = ent[base + (size_t)32 * colour[e] + el[e]];
+            if (colour[e] < 0 || colour[e] >= delta || slot != 0u)
+                return fail(ctx, MO_ED_ERR_STATE, "gather schedule colouring failed");
+            slot = ecode[e];
+        }
+        smax = std::max(smax, delta);
+    }
+    s->sched_slots_max = smax;
+    if (ent.empty()) ent.push_back(0u);
+    MOED_CUDA(ctx, cudaMalloc(&s->sched_hdr, sizeof(int2) * std::max(nch, 1)));
+    MOED_CUDA(ctx, cudaMalloc(&s->sched_ent, sizeof(unsigned) * ent.size()));
+    if (nch > 0)
+        MOED_CUDA(ctx, cudaMemcpyAsync(s->sched_hdr, hdr.data(), sizeof(int2) * nch, cudaMemcpyHostToDevice,
+                                       ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpyAsync(s->sched_ent, ent.data(), sizeof(unsigned) * ent.size(),
+                                   cudaMemcpyHostToDevice, ctx->stream));
+    MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));   // before the host vectors move
+    s->h_sched_hdr = std::move(hdr);
+    s->h_sched_ent = std::move(ent);
+    return MO_ED_OK;
+}
+
+int species_sched(mo_ed_ctx *ctx, Species *sp, int R)
+{
+    if (sp->sched_rf.count(R)) return MO_ED_OK;
+    const std::vector<int2> &hdr = sp->h_sched_hdr;
+    const std::vector<unsigned> &ent = sp->h_sched_ent;
+    std::vector<HopEnt<float>> ef(ent.size());
+    std::vector<HopEnt<double>> ed(ent.size());
+    auto offset = [R](int t) { return ((t >> 5) * R) * 32 + (t & 31); };
+    for (size_t c = 0; c < hdr.size(); ++c) {
+        const int first = hdr[c].x, nslot = hdr[c].y;
+        for (int sl = 0; sl < nslot; ++sl) {
+            const unsigned *e = &ent[(size_t)first + (size_t)32 * sl];
+            unsigned used = 0u;
+            for (int l = 0; l < 32; ++l)
+                if (e[l] & 0x80000000u) used |= 1u << (e[l] & 31u);
+            for (int l = 0; l < 32; ++l) {
+                const size_t o = (size_t)first + (size_t)32 * sl + l;
+                int t;
+                double v;
+                if (e[l] & 0x80000000u) {
+                    t = (int)(e[l] & 0xffffu);
+                    v = ctx->cpl_val[(e[l] >> 16) & 63u];
+                    if (e[l] & (1u << 22)) v = -v;
+                } else {
+                    t = __builtin_ctz(~used);   // a bank no lane of this slot reads (column t of tile 0)
+                    used |= 1u << t;
+                    v = 0.0;
+                }
+                ef[o].t = offset(t);
+                ef[o].v = (float)v;
+                ed[o].t = offset(t);
+                ed[o].pad = 0;
+                ed[o].v = v;
+            }
+        }
+    }
+    HopEnt<float> *df = nullptr;
+    HopEnt<double> *dd = nullptr;
+    MOED_CUDA(ctx, cudaMalloc(&df, sizeof(HopEnt<float>) * ef.size()));
+    sp->sched_rf[R] = df;
+    MOED_CUDA(ctx, cudaMalloc(&dd, sizeof(HopEnt<double>) * ed.size()));
+    sp->sched_rd[R] = dd;
+    MOED_CUDA(ctx, cudaMemcpyAsync(df, ef.data(), sizeof(HopEnt<float>) * ef.size(), cudaMemcpyHostToDevice,
+                                   ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpyAsync(dd, ed.data(), sizeof(HopEnt<double>) * ed.size(), cudaMemcpyHostToDevice,
+                                   ctx->stream));
+    MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return MO_ED_OK;
+}
+
 int get_species(mo_ed_ctx *ctx, int N, Species **out)
 {
     auto it = ctx->species.find(N);
@@ -477,6 +677,7 @@ int get_species(mo_ed_ctx *ctx, int N, Species **out)
     MOED_CUDA(ctx, cudaMemcpyAsync(&s->max_cnt, dmax.p, sizeof(int), cudaMemcpyDeviceToHost,
                                    ctx->stream));
     MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (int rc = build_up_schedule(ctx, s.get())) return rc;
     *out = s.get();
     ctx->species[N] = std::move(s);
     return MO_ED_OK;

@@ -83,6 +83,7 @@ SIGNATURES = [
     ("mo_ed_multiply_h_mixed_dev", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     ("mo_ed_hv_tuning", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, _ip, _ip,
                                   C.POINTER(C.c_float), _ip]),
+    ("mo_ed_hv_set_variant", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]),
     ("mo_ed_apply_c", C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, C.c_int, C.c_int, C.c_int, _dp,
                                 C.c_longlong, _llp]),
     ("mo_ed_lanczos_iteration", C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _ip, _dp, _dp]),
@@ -289,16 +290,20 @@ class EDSolver:
     def multiply_H_mixed_dev(self, ne_up, ne_down, dA, dB):
         self._chk(lib().mo_ed_multiply_h_mixed_dev(self._ctx, ne_up, ne_down, C.c_void_p(dA), C.c_void_p(dB)))
 
+    def hv_set_variant(self, ne_up, ne_down, variant, dtype=FP32):
+        """Pin the H*v tile-shape variant (index of hv_tuning's list)."""
+        self._chk(lib().mo_ed_hv_set_variant(self._ctx, ne_up, ne_down, dtype, variant))
+
     def hv_tuning(self, ne_up, ne_down, dtype=FP32):
-        """Autotuner record: list of ((R, threads, CTAs/SM), ms) and the chosen index."""
+        """Autotuner record: list of ((R, threads, CTAs/SM, staged), ms) and the chosen index."""
         cap = 16
         nv, ch = C.c_int(), C.c_int()
-        shape = np.zeros(3 * cap, np.int32)
+        shape = np.zeros(4 * cap, np.int32)
         ms = np.zeros(cap, np.float32)
         self._chk(lib().mo_ed_hv_tuning(self._ctx, ne_up, ne_down, dtype, cap, C.byref(nv),
                                         shape.ctypes.data_as(_ip), ms.ctypes.data_as(C.POINTER(C.c_float)),
                                         C.byref(ch)))
-        return [(tuple(int(v) for v in shape[3 * i:3 * i + 3]), float(ms[i])) for i in range(nv.value)], ch.value
+        return [(tuple(int(v) for v in shape[4 * i:4 * i + 4]), float(ms[i])) for i in range(nv.value)], ch.value
 
     # ---- apply_c (ed_operators.F90:10) --------------------------------------
     def apply_c(self, ne_up, ne_down, vec, pm, iorb, ispin):

@@ -117,6 +117,30 @@ def test_multiply_h_fp32(setup, oracle, name):
         assert rel(y, oracle.multiply_H(m, b, x.astype(np.float64))) < 2e-6, (name, nu, nd)
 
 
+@pytest.mark.parametrize("name", ["3x6_block", "4x4_mixed", "5x2_dense"])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-13), ("fp32", 2e-6)])
+def test_multiply_h_every_variant(setup, oracle, pkg, name, precision, tol):
+    """Each tile-shape variant (k_hv and the bulk-copy staged k_hv_tma), pinned
+    in turn, against the oracle on several sectors."""
+    s, m = setup(name, precision=precision)
+    dt = pkg.FP32 if precision == "fp32" else pkg.FP64
+    ns = m.nsite
+    rng = np.random.default_rng(11)
+    for nu, nd in sectors_of(ns):
+        b = oracle.Basis(ns, nu, nd)
+        x = rng.standard_normal(b.ntot)
+        if precision == "fp32":
+            x = x.astype(np.float32)
+        ref = oracle.multiply_H(m, b, x.astype(np.float64))
+        variants, _ = s.hv_tuning(nu, nd, dt)
+        for v, (shape, ms) in enumerate(variants):
+            if ms < 0:
+                continue      # does not fit this sector
+            s.hv_set_variant(nu, nd, v, dt)
+            y = s.multiply_H(nu, nd, x)
+            assert rel(y, ref) < tol, (name, nu, nd, v, shape)
+
+
 def test_multiply_h_mixed(setup, oracle):
     import torch
     s, m = setup("3x6_block")
