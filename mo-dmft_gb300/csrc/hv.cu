@@ -983,6 +983,8 @@ static const int kNVarF64 = sizeof(kVarF64) / sizeof(kVarF64[0]);
 static const HvVariant &variant(int kind, int v) { return kind == HV_F32 ? kVarF32[v] : kVarF64[v]; }
 static int nvariants(int kind) { return kind == HV_F32 ? kNVarF32 : kNVarF64; }
 
+constexpr long long kTuneMinElems = 1ll << 18;   // smaller sectors take variant 0 untimed
+
 static long long shape_key(int kind, const Sector &s) { return ((long long)kind << 32) | (s.ne_up << 16) | s.ne_down; }
 
 template <typename TA>
@@ -1251,6 +1253,10 @@ int hv_prepare(mo_ed_ctx *ctx, const Sector &s, int kind, int *v_out, int *R_out
     int v;
     if (it != ctx->hv_choice.end()) {
         v = it->second;
+    } else if (s.Dpad() < kTuneMinElems) {
+        v = 0;   // small sector: timing the variants would cost more than it saves
+        ctx->hv_choice[key] = v;
+        ctx->hv_times[key].assign(nvariants(kind), -1.0f);
     } else {
         if (int rc = tune(ctx, s, kind, &v)) return rc;
         ctx->hv_choice[key] = v;

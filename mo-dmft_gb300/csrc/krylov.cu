@@ -340,7 +340,7 @@ static void lz_fill_dev(LzBatch &b, LzBatchDev &d)
 }
 
 template <typename T>
-static int lz_steps(mo_ed_ctx *ctx, LzBatch &b, LzBatchDev &d)
+static int lz_enqueue(mo_ed_ctx *ctx, LzBatch &b, LzBatchDev &d)
 {
     const int nrun = d.nrun;
     const int kind = sizeof(T) == 4 ? HV_F32 : HV_F64;
@@ -371,13 +371,43 @@ static int lz_steps(mo_ed_ctx *ctx, LzBatch &b, LzBatchDev &d)
     return MO_ED_OK;
 }
 
+// All nstep+1 steps of a batch (3 launches per step, no host round trip:
+// runs stop on the device through their active flags).  With `graph` the
+// launches are captured once into a CUDA graph and replayed as one launch;
+// a stream that is already being captured gets the plain launches.
+template <typename T>
+static int lz_steps(mo_ed_ctx *ctx, LzBatch &b, LzBatchDev &d, bool graph)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    MOED_CUDA(ctx, cudaStreamIsCapturing(ctx->stream, &cs));
+    if (!graph || cs != cudaStreamCaptureStatusNone) return lz_enqueue<T>(ctx, b, d);
+    MOED_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = lz_enqueue<T>(ctx, b, d);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    cudaGraphExec_t x = nullptr;
+    if (rc == MO_ED_OK && e == cudaSuccess) e = cudaGraphInstantiate(&x, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (rc != MO_ED_OK || e != cudaSuccess) {
+        // a capture the runtime refused: the same launches, issued directly
+        cudaGetLastError();
+        if (x) cudaGraphExecDestroy(x);
+        return lz_enqueue<T>(ctx, b, d);
+    }
+    e = cudaGraphLaunch(x, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaGraphExecDestroy(x);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphLaunch");
+    return MO_ED_OK;
+}
+
 int lz_run(mo_ed_ctx *ctx, LzBatch &b, std::vector<std::vector<double>> &a,
            std::vector<std::vector<double>> &bb, std::vector<int> &nstep_calc)
 {
     LzBatchDev d;
     lz_fill_dev(b, d);
     const int nrun = d.nrun;
-    int rc = (b.prec == MO_ED_FP32) ? lz_steps<float>(ctx, b, d) : lz_steps<double>(ctx, b, d);
+    int rc = (b.prec == MO_ED_FP32) ? lz_steps<float>(ctx, b, d, true) : lz_steps<double>(ctx, b, d, true);
     if (rc) return rc;
     std::vector<double> coef((size_t)2 * (b.nstep + 1) * nrun);
     std::vector<int> fl(2 * nrun);
@@ -520,10 +550,10 @@ int lanczos_reference_in(mo_ed_ctx *ctx, const Sector &s, const double *h_vec, i
         double *stage = (double *)(base + g.u12);
         if (int rc = upload_padded(ctx, s, h_vec, stage, sizeof(double))) return rc;
         if (int rc = convert_f64_to_f32(ctx, stage, (float *)R.u[0], Dp)) return rc;
-        if (int rc = lz_steps<float>(ctx, lb, d)) return rc;
+        if (int rc = lz_steps<float>(ctx, lb, d, false)) return rc;
     } else {
         if (int rc = upload_padded(ctx, s, h_vec, R.u[0], sizeof(double))) return rc;
-        if (int rc = lz_steps<double>(ctx, lb, d)) return rc;
+        if (int rc = lz_steps<double>(ctx, lb, d, false)) return rc;
     }
     MOED_CUDA(ctx, cudaMemcpyAsync(a, R.a, sizeof(double) * (nstep + 1), cudaMemcpyDeviceToHost, ctx->stream));
     MOED_CUDA(ctx, cudaMemcpyAsync(b, R.nrm, sizeof(double) * (nstep + 1), cudaMemcpyDeviceToHost, ctx->stream));
@@ -537,6 +567,7 @@ int lanczos_reference_in(mo_ed_ctx *ctx, const Sector &s, const double *h_vec, i
 // thick-restart Lanczos with full reorthogonalisation (diag replacement)
 // ---------------------------------------------------------------------------
 constexpr int kMaxNcv = 200;
+constexpr size_t kTrlPoolBytes = (size_t)64 << 20;   // largest pooled Krylov vector
 
 template <typename T>
 struct VPtrs {
@@ -980,9 +1011,13 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
     std::vector<double> res_hist;
     const size_t vb = sizeof(T) * (size_t)Dp;
 
-    std::vector<DevBuf> store(ncv + 2 + kkeep);
-    for (auto &b : store)
-        if (int rc = dev_alloc(ctx, b, vb)) return rc;
+    // Krylov vectors: sectors up to kTrlPoolBytes per vector reuse buffers kept
+    // in the context (many small sectors: no allocation per sector)
+    std::vector<DevBuf> local;
+    std::vector<DevBuf> &store = vb <= kTrlPoolBytes ? ctx->trl_pool : local;
+    if (store.size() < (size_t)(ncv + 2 + kkeep)) store.resize(ncv + 2 + kkeep);
+    for (int i = 0; i < ncv + 2 + kkeep; ++i)
+        if (int rc = ensure(ctx, store[i], vb)) return rc;
     std::vector<DevBuf *> V(ncv + 1);
     for (int i = 0; i <= ncv; ++i) V[i] = &store[i];
     DevBuf *W = &store[ncv + 1];
@@ -991,19 +1026,22 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
 
     const int G = (int)std::max(1LL, std::min((Dp + kVecThreads - 1) / kVecThreads, (long long)ctx->num_sms * 4));
     const int n2 = ncv + 2;
-    DevBuf dHp, dh1, dh2, dpart, dnorm, dbeta, dA, dVj, devals, devecs, dtheta, dsc;
-    if (int rc = dev_alloc(ctx, dHp, sizeof(double) * (size_t)n2 * n2)) return rc;
-    if (int rc = dev_alloc(ctx, dh1, sizeof(double) * n2)) return rc;
-    if (int rc = dev_alloc(ctx, dh2, sizeof(double) * n2)) return rc;
-    if (int rc = dev_alloc(ctx, dpart, sizeof(double) * (size_t)n2 * ctx->num_sms * 4)) return rc;
-    if (int rc = dev_alloc(ctx, dnorm, sizeof(double) * G)) return rc;
-    if (int rc = dev_alloc(ctx, dbeta, sizeof(double) * 2)) return rc;
-    if (int rc = dev_alloc(ctx, dA, sizeof(double) * (size_t)n2 * n2)) return rc;
-    if (int rc = dev_alloc(ctx, dVj, sizeof(double) * (size_t)n2 * n2)) return rc;
-    if (int rc = dev_alloc(ctx, devals, sizeof(double) * n2)) return rc;
-    if (int rc = dev_alloc(ctx, devecs, sizeof(double) * (size_t)n2 * n2)) return rc;
-    if (int rc = dev_alloc(ctx, dtheta, sizeof(double) * n2)) return rc;
-    if (int rc = dev_alloc(ctx, dsc, sizeof(double) * 4)) return rc;
+    std::vector<DevBuf> &sm = ctx->trl_small;   // projected-problem workspace, kept in the context
+    if (sm.size() < 12) sm.resize(12);
+    DevBuf &dHp = sm[0], &dh1 = sm[1], &dh2 = sm[2], &dpart = sm[3], &dnorm = sm[4], &dbeta = sm[5];
+    DevBuf &dA = sm[6], &dVj = sm[7], &devals = sm[8], &devecs = sm[9], &dtheta = sm[10], &dsc = sm[11];
+    if (int rc = ensure(ctx, dHp, sizeof(double) * (size_t)n2 * n2)) return rc;
+    if (int rc = ensure(ctx, dh1, sizeof(double) * n2)) return rc;
+    if (int rc = ensure(ctx, dh2, sizeof(double) * n2)) return rc;
+    if (int rc = ensure(ctx, dpart, sizeof(double) * (size_t)n2 * ctx->num_sms * 4)) return rc;
+    if (int rc = ensure(ctx, dnorm, sizeof(double) * G)) return rc;
+    if (int rc = ensure(ctx, dbeta, sizeof(double) * 2)) return rc;
+    if (int rc = ensure(ctx, dA, sizeof(double) * (size_t)n2 * n2)) return rc;
+    if (int rc = ensure(ctx, dVj, sizeof(double) * (size_t)n2 * n2)) return rc;
+    if (int rc = ensure(ctx, devals, sizeof(double) * n2)) return rc;
+    if (int rc = ensure(ctx, devecs, sizeof(double) * (size_t)n2 * n2)) return rc;
+    if (int rc = ensure(ctx, dtheta, sizeof(double) * n2)) return rc;
+    if (int rc = ensure(ctx, dsc, sizeof(double) * 4)) return rc;
     MOED_CUDA(ctx, cudaMemsetAsync(dHp.p, 0, dHp.bytes, ctx->stream));
     double *Hp = (double *)dHp.p;
     const int ldh = n2;

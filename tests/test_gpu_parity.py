@@ -120,7 +120,7 @@ def test_multiply_h_fp32(setup, oracle, name):
 @pytest.mark.parametrize("name", ["3x6_block", "4x4_mixed", "5x2_dense"])
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-13), ("fp32", 2e-6)])
 def test_multiply_h_every_variant(setup, oracle, pkg, name, precision, tol):
-    """Each tile-shape variant (k_hv and the bulk-copy staged k_hv_tma), pinned
+    """Each tile-shape variant (k_hv and the double-buffered staged k_hv_async), pinned
     in turn, against the oracle on several sectors."""
     s, m = setup(name, precision=precision)
     dt = pkg.FP32 if precision == "fp32" else pkg.FP64
@@ -133,12 +133,18 @@ def test_multiply_h_every_variant(setup, oracle, pkg, name, precision, tol):
             x = x.astype(np.float32)
         ref = oracle.multiply_H(m, b, x.astype(np.float64))
         variants, _ = s.hv_tuning(nu, nd, dt)
+        ran, staged = 0, 0
         for v, (shape, ms) in enumerate(variants):
-            if ms < 0:
-                continue      # does not fit this sector
-            s.hv_set_variant(nu, nd, v, dt)
-            y = s.multiply_H(nu, nd, x)
+            try:
+                s.hv_set_variant(nu, nd, v, dt)
+                y = s.multiply_H(nu, nd, x)
+            except pkg.EDError as e:
+                assert e.code == 1, e       # MO_ED_ERR_ARG: the shape does not fit this sector
+                continue
+            ran += 1
+            staged += shape[3]
             assert rel(y, ref) < tol, (name, nu, nd, v, shape)
+        assert ran >= 2 and staged >= 1
 
 
 def test_multiply_h_mixed(setup, oracle):
