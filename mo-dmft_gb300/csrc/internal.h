@@ -235,7 +235,7 @@ struct mo_ed_ctx {
     moed::DevBuf scratch_a, scratch_b, scratch_part;
     // eigensolver workspace reused across sectors (Krylov vectors of sectors
     // up to 64 MB per vector, and the projected-problem arrays)
-    std::vector<moed::DevBuf> trl_pool, trl_small;
+    std::vector<moed::DevBuf> trl_pool, trl_small, rr_pool;
     // autotuned H*v tile shape per (kind, Nup, Ndn), and the timings (ms) of
     // every shape measured when it was chosen (negative: did not fit)
     std::map<long long, int> hv_choice;

@@ -567,6 +567,7 @@ int lanczos_reference_in(mo_ed_ctx *ctx, const Sector &s, const double *h_vec, i
 // thick-restart Lanczos with full reorthogonalisation (diag replacement)
 // ---------------------------------------------------------------------------
 constexpr int kMaxNcv = 200;
+constexpr int kJacobiSmem = 80;   // k_jacobi keeps A and V in shared memory up to this order
 constexpr size_t kTrlPoolBytes = (size_t)64 << 20;   // largest pooled Krylov vector
 
 template <typename T>
@@ -646,6 +647,43 @@ __global__ void k_reduce_cols(const double *part, int G, int nv, double *out)
         double s = 0.0;
         for (int b = 0; b < G; ++b) s += part[(size_t)b * nv + l];
         out[l] = s;
+    }
+}
+
+// part[b][l] = block b's share of V_l . w with FP64 products and sums (an
+// FP32 x FP32 product is exact in FP64): the Gram and projected matrices of
+// the final Rayleigh-Ritz step.
+template <typename TV, typename TW>
+__global__ void __launch_bounds__(kVecThreads)
+k_multidot_exact(const __grid_constant__ VPtrs<TV> V, int nv, const TW *__restrict__ w, long long D,
+                 double *part)
+{
+    __shared__ double sred[kVecThreads / 32][kDotPass];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int l0 = 0; l0 < nv; l0 += kDotPass) {
+        const int np = min(kDotPass, nv - l0);
+        double acc[kDotPass];
+#pragma unroll
+        for (int l = 0; l < kDotPass; ++l) acc[l] = 0.0;
+        for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < D;
+             i += (long long)gridDim.x * blockDim.x) {
+            const double x = (double)w[i];
+#pragma unroll
+            for (int l = 0; l < kDotPass; ++l)
+                if (l < np) acc[l] += (double)V.p[l0 + l][i] * x;
+        }
+#pragma unroll
+        for (int l = 0; l < kDotPass; ++l) {
+            const double v = warp_sum(acc[l]);
+            if (lane == 0) sred[wid][l] = v;
+        }
+        __syncthreads();
+        for (int l = threadIdx.x; l < np; l += blockDim.x) {
+            double t = 0.0;
+            for (int q = 0; q < kVecThreads / 32; ++q) t += sred[q][l];
+            part[(size_t)blockIdx.x * nv + l0 + l] = t;
+        }
+        __syncthreads();
     }
 }
 
@@ -792,13 +830,17 @@ k_rotate(const __grid_constant__ VPtrs<T> V, int nv, const double *__restrict__ 
 // computed column j (Hp[j*ldh + i]).  One CTA.  Outputs ascending eigenvalues
 // and the matching eigenvectors (column-major m x m).
 __global__ void k_jacobi(const double *__restrict__ Hp, int ldh, int m, int kk,
-                         const double *__restrict__ theta, double *A, double *V, double *evals,
+                         const double *__restrict__ theta, double *Ag, double *Vg, double *evals,
                          double *evecs, int max_sweeps)
 {
     __shared__ double s_c[kMaxNcv / 2 + 1], s_s[kMaxNcv / 2 + 1];
     __shared__ int s_p[kMaxNcv / 2 + 1], s_q[kMaxNcv / 2 + 1];
+    extern __shared__ double s_work[];
     const int n = m + (m & 1);
     const int half = n / 2;
+    // working matrices in shared memory when the launch provides room (n <= kJacobiSmem)
+    double *A = n <= kJacobiSmem ? s_work : Ag;
+    double *V = n <= kJacobiSmem ? s_work + (size_t)n * n : Vg;
     for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
         const int i = idx % n, j = idx / n;
         double v;
@@ -895,6 +937,13 @@ __global__ void k_jacobi(const double *__restrict__ Hp, int ldh, int m, int kk,
         const int r = idx % m, c = idx / m;
         evecs[idx] = V[(size_t)order[c] * n + r];
     }
+}
+
+// dynamic shared memory of a k_jacobi launch of order m
+static size_t jacobi_smem(int m)
+{
+    const int n = m + (m & 1);
+    return n <= kJacobiSmem ? 2 * sizeof(double) * (size_t)n * n : 0;
 }
 
 // Generalized symmetric problem P c = lambda S c (k x k, column-major, upper
@@ -1078,8 +1127,13 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
     double anorm = 0.0;
     for (; cycle < ctx->opt.gs_maxcycles && !done; ++cycle) {
         m = ncv;
+        // The steps of a cycle run without a host round trip; the diagonal and
+        // the betas are read once at the end of the cycle.  A step whose beta
+        // falls below the breakdown threshold ends the cycle there (its Krylov
+        // space is invariant; later steps of the cycle are discarded).
         for (int j = k; j < ncv; ++j) {
             if (int rc = hv(V[j]->p, W->p)) return rc;
+            const bool last = j + 1 >= D;   // Krylov space is the whole sector
             if (int rc = orthogonalize<T>(ctx, V, j + 1, (T *)W->p, Dp, (double *)dh1.p, (double *)dh2.p,
                                           (double *)dpart.p, (double *)dnorm.p, G))
                 return rc;
@@ -1087,38 +1141,40 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
                                                      (const double *)dnorm.p, G, Hp + (size_t)j * ldh,
                                                      (double *)dbeta.p);
             MOED_CHECK_LAUNCH(ctx);
-            double beta[2], diag;
-            MOED_CUDA(ctx, cudaMemcpyAsync(beta, dbeta.p, sizeof(beta), cudaMemcpyDeviceToHost, ctx->stream));
-            MOED_CUDA(ctx, cudaMemcpyAsync(&diag, Hp + (size_t)j * ldh + j, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-            MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-            anorm = std::max(anorm, std::fabs(diag) + beta[0]);
-            if (j + 1 >= D) {             // Krylov space is the whole sector
-                m = j + 1;
-                break;
-            }
-            const double bd = (prec == MO_ED_FP32 ? 1e-5 : 1e-12) * std::max(anorm, 1.0);
-            if (beta[0] <= bd) {
-                // invariant subspace: continue from a fresh random direction
-                double zero = 0.0;
-                MOED_CUDA(ctx, cudaMemcpyAsync(Hp + (size_t)j * ldh + j + 1, &zero, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-                k_random<T><<<G, kVecThreads, 0, ctx->stream>>>((T *)W->p, Dp, s.ld(), s.up->n,
-                                                                seed + 7919ULL * (cycle * kMaxNcv + j + 1));
-                MOED_CHECK_LAUNCH(ctx);
-                if (int rc = orthogonalize<T>(ctx, V, j + 1, (T *)W->p, Dp, (double *)dh1.p, (double *)dh2.p,
-                                              (double *)dpart.p, (double *)dnorm.p, G))
-                    return rc;
-                if (int rc = normalize_into((T *)W->p, V[j + 1])) return rc;
-            } else {
+            if (!last) {
                 k_scale_copy<T><<<G, kVecThreads, 0, ctx->stream>>>((const T *)W->p, (T *)V[j + 1]->p, Dp,
                                                                     (double *)dbeta.p + 1);
                 MOED_CHECK_LAUNCH(ctx);
+            }
+            if (last) {
+                m = j + 1;
+                break;
+            }
+        }
+        bool broke = false;
+        {
+            std::vector<double> hc((size_t)ldh * m);
+            MOED_CUDA(ctx, cudaMemcpyAsync(hc.data(), Hp, sizeof(double) * hc.size(), cudaMemcpyDeviceToHost, ctx->stream));
+            MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            for (int j = k; j < m; ++j) {
+                const double diag = hc[(size_t)j * ldh + j], beta = hc[(size_t)j * ldh + j + 1];
+                anorm = std::max(anorm, std::fabs(diag) + beta);
+                if (j + 1 >= D) break;
+                const double bd = (prec == MO_ED_FP32 ? 1e-5 : 1e-12) * std::max(anorm, 1.0);
+                if (beta <= bd) {
+                    m = j + 1;
+                    broke = true;
+                    break;
+                }
             }
         }
         // Rayleigh-Ritz on span V[0..m-1]
         MOED_CUDA(ctx, cudaMemcpyAsync(dtheta.p, theta.data(), sizeof(double) * std::max(k, 1),
                                        cudaMemcpyHostToDevice, ctx->stream));
-        k_jacobi<<<1, 256, 0, ctx->stream>>>(Hp, ldh, m, k, (const double *)dtheta.p, (double *)dA.p,
-                                             (double *)dVj.p, (double *)devals.p, (double *)devecs.p, 60);
+        MOED_CUDA(ctx, cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)jacobi_smem(kJacobiSmem)));
+        k_jacobi<<<1, 256, jacobi_smem(m), ctx->stream>>>(Hp, ldh, m, k, (const double *)dtheta.p, (double *)dA.p,
+                                                           (double *)dVj.p, (double *)devals.p, (double *)devecs.p, 60);
         MOED_CHECK_LAUNCH(ctx);
         evecs_h.resize((size_t)m * m);
         double beta_m = 0.0;
@@ -1129,7 +1185,7 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
         MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         int nconv = 0;
         double maxres = 0.0;
-        for (int i = 0; i < nwant; ++i) {
+        for (int i = 0; i < std::min(nwant, m); ++i) {
             double res = std::fabs(beta_m * evecs_h[(size_t)i * m + (m - 1)]);
             maxres = std::max(maxres, res);
             if (res <= tol * std::max(anorm, 1.0) && nconv == i) ++nconv;
@@ -1144,7 +1200,8 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
             break;
         }
         // thick restart: keep kkeep lowest Ritz vectors, then the residual vector
-        const int kk = std::min(kkeep, m - 1);
+        // after a breakdown every Ritz vector of the invariant subspace is kept
+        const int kk = broke ? std::min(kkeep, m) : std::min(kkeep, m - 1);
         VPtrs<T> P = make_ptrs<T>(V, m);
         for (int c0 = 0; c0 < kk; c0 += 8) {
             const int nc = std::min(8, kk - c0);
@@ -1154,7 +1211,18 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
             MOED_CHECK_LAUNCH(ctx);
         }
         for (int i = 0; i < kk; ++i) std::swap(V[i], spare[i]);
-        std::swap(V[kk], V[m]);
+        if (broke) {
+            // invariant subspace: continue from a fresh random direction
+            k_random<T><<<G, kVecThreads, 0, ctx->stream>>>((T *)W->p, Dp, s.ld(), s.up->n,
+                                                            seed + 7919ULL * (cycle + 1) * kMaxNcv);
+            MOED_CHECK_LAUNCH(ctx);
+            if (int rc = orthogonalize<T>(ctx, V, kk, (T *)W->p, Dp, (double *)dh1.p, (double *)dh2.p,
+                                          (double *)dpart.p, (double *)dnorm.p, G))
+                return rc;
+            if (int rc = normalize_into((T *)W->p, V[kk])) return rc;
+        } else {
+            std::swap(V[kk], V[m]);
+        }
         k = kk;
         MOED_CUDA(ctx, cudaMemsetAsync(dHp.p, 0, dHp.bytes, ctx->stream));
     }
@@ -1167,11 +1235,18 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
     // of the spectrum), whatever the mixing inside the cluster.
     vals.assign(nev, DBL_MAX);
     const int nout = nwant;
-    std::vector<DevBuf> X(nout), HX(nout);
-    for (auto &b : X)
-        if (int rc = dev_alloc(ctx, b, vb)) return rc;
-    for (auto &b : HX)
-        if (int rc = dev_alloc(ctx, b, sizeof(double) * (size_t)Dp)) return rc;
+    // X, HX, HX2 and the small arrays come from the context's pool for sectors
+    // up to kTrlPoolBytes per FP64 vector; the refined vectors X2 are returned
+    const size_t vb64 = sizeof(double) * (size_t)Dp;
+    std::vector<DevBuf> rr_local;
+    std::vector<DevBuf> &rp = vb64 <= kTrlPoolBytes ? ctx->rr_pool : rr_local;
+    if (rp.size() < (size_t)(3 * nout + 2)) rp.resize(3 * nout + 2);
+    DevBuf *X = &rp[0], *HX = &rp[nout], *HX2 = &rp[2 * nout];
+    for (int i = 0; i < nout; ++i) {
+        if (int rc = ensure(ctx, X[i], vb)) return rc;
+        if (int rc = ensure(ctx, HX[i], vb64)) return rc;
+        if (int rc = ensure(ctx, HX2[i], vb64)) return rc;
+    }
     {
         VPtrs<T> P = make_ptrs<T>(V, m);
         for (int c0 = 0; c0 < nout; c0 += 8) {
@@ -1188,24 +1263,38 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
         if (int rc = hv_single(ctx, s, hk, X[i].p, HX[i].p)) return rc;
         ++matvecs;
     }
-    DevBuf dPS, dRR;
-    if (int rc = dev_alloc(ctx, dPS, sizeof(double) * 2 * (size_t)nout * nout)) return rc;
+    DevBuf &dPS = rp[3 * nout], &dRR = rp[3 * nout + 1];
+    if (int rc = ensure(ctx, dPS, sizeof(double) * 2 * (size_t)nout * nout)) return rc;
     const size_t k2 = (size_t)nout * nout, kp2 = (size_t)(nout + 1) * (nout + 1);
-    if (int rc = dev_alloc(ctx, dRR, sizeof(double) * (4 * k2 + 2 * kp2 + nout + 4))) return rc;
+    if (int rc = ensure(ctx, dRR, sizeof(double) * (4 * k2 + 2 * kp2 + nout + 4))) return rc;
     double *dP = (double *)dPS.p, *dS = dP + (size_t)nout * nout;
-    for (int i = 0; i < nout; ++i)
+    {   // P[i][j] = X_i . H X_j, S[i][j] = X_i . X_j: one exact multi-dot per column
+        std::vector<DevBuf *> xin(nout);
+        for (int i = 0; i < nout; ++i) xin[i] = &X[i];
+        VPtrs<T> Px = make_ptrs<T>(xin, nout);
+        const int Gd = (int)std::max(1LL, std::min((Dp + kVecThreads - 1) / kVecThreads, (long long)ctx->num_sms * 4));
         for (int j = 0; j < nout; ++j) {
-            if (int rc = dot_dev(ctx, prec, X[i].p, MO_ED_FP64, HX[j].p, Dp, dP + (size_t)j * nout + i)) return rc;
-            if (j >= i)
-                if (int rc = dot_dev(ctx, prec, X[i].p, prec, X[j].p, Dp, dS + (size_t)j * nout + i)) return rc;
+            k_multidot_exact<T, double><<<Gd, kVecThreads, 0, ctx->stream>>>(Px, nout, (const double *)HX[j].p, Dp,
+                                                                              (double *)dpart.p);
+            MOED_CHECK_LAUNCH(ctx);
+            k_reduce_cols<<<1, 256, 0, ctx->stream>>>((const double *)dpart.p, Gd, nout, dP + (size_t)j * nout);
+            MOED_CHECK_LAUNCH(ctx);
+            k_multidot_exact<T, T><<<Gd, kVecThreads, 0, ctx->stream>>>(Px, nout, (const T *)X[j].p, Dp,
+                                                                         (double *)dpart.p);
+            MOED_CHECK_LAUNCH(ctx);
+            k_reduce_cols<<<1, 256, 0, ctx->stream>>>((const double *)dpart.p, Gd, nout, dS + (size_t)j * nout);
+            MOED_CHECK_LAUNCH(ctx);
         }
+    }
     double *rr = (double *)dRR.p;
     double *dGA = rr, *dL = dGA + k2, *dW = dL + k2, *dC = dW + k2;
     double *dJa = dC + k2, *dJv = dJa + kp2;          // Jacobi work (n x n, n = k rounded up to even)
     double *dEv = dJv + kp2, *dFlag = dEv + nout;
     k_gen_eig_prep<<<1, 1, 0, ctx->stream>>>(dP, dS, nout, dGA, dL, dFlag);
     MOED_CHECK_LAUNCH(ctx);
-    k_jacobi<<<1, 256, 0, ctx->stream>>>(dGA, nout, nout, 0, dEv, dJa, dJv, dEv, dW, 60);
+    MOED_CUDA(ctx, cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)jacobi_smem(kJacobiSmem)));
+    k_jacobi<<<1, 256, jacobi_smem(nout), ctx->stream>>>(dGA, nout, nout, 0, dEv, dJa, dJv, dEv, dW, 60);
     MOED_CHECK_LAUNCH(ctx);
     k_gen_eig_post<<<1, 1, 0, ctx->stream>>>(dL, dW, nout, dC);
     MOED_CHECK_LAUNCH(ctx);
@@ -1216,11 +1305,9 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
     MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (flag != 0.0) return fail(ctx, MO_ED_ERR_NOCONV, "Ritz vectors numerically dependent");
     // refined vectors X C and their images (H X) C
-    std::vector<DevBuf> X2(nout), HX2(nout);
+    std::vector<DevBuf> X2(nout);
     for (auto &b : X2)
         if (int rc = dev_alloc(ctx, b, vb)) return rc;
-    for (auto &b : HX2)
-        if (int rc = dev_alloc(ctx, b, sizeof(double) * (size_t)Dp)) return rc;
     {
         std::vector<DevBuf *> xin, hin;
         for (int i = 0; i < nout; ++i) {
