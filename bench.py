@@ -177,6 +177,35 @@ def lanczos_g(pkg, name, nev):
     return out
 
 
+def fit_bench(pkg, cpu_fits=2):
+    """C5: 256 random starts of the chi^2 bath fit in one lockstep batch (FP64
+    adjoint gradient on the device), next to the oracle's frprmn on one host
+    core for a bounded number of the same starts."""
+    P = pkg.configs.fit_config(seed=4, nbatch=256)
+    norb, nbath = P["norb"], P["nbath"]
+    ns = norb + nbath
+    s = pkg.EDSolver(0)
+    s.set_options(precision="fp64")
+    t0 = time.perf_counter()
+    X, fret, it, st = s.fit_batch(P["X0"], P["omega"], P["dev"], nbath, norb)
+    t_gpu = time.perf_counter() - t0
+    s.close()
+    out = {"config": "C5", "nbatch": int(P["X0"].shape[0]), "nw": int(P["nw"]), "nxsize": int(P["X0"].shape[1]),
+           "gpu_s": round(t_gpu, 4), "fits_per_s": round(P["X0"].shape[0] / t_gpu, 2),
+           "cg_iterations_median": int(np.median(it)), "chi2_min": float(fret.min()),
+           "chi2_median": float(np.median(fret)), "failed": int((st != 0).sum())}
+    if cpu_fits > 0:
+        import __graft_entry__ as g
+        O = g.load_oracle()
+        t0 = time.perf_counter()
+        for b in range(cpu_fits):
+            O.frprmn(P["X0"][b], ns, P["omega"], P["dev"], nbath, norb)
+        t_cpu = (time.perf_counter() - t0) / cpu_fits
+        out["cpu_s_per_fit"] = round(t_cpu, 4)
+        out["cpu_sample"] = f"oracle frprmn (C port, 1 core) on the first {cpu_fits} starts"
+    return out
+
+
 def run_ours(args):
     import torch
     dist, rank, ws = dist_init()
@@ -260,8 +289,11 @@ def run_ours(args):
 
     tuning, chosen = s.hv_tuning(nup, ndn, pkg.FP32)
     lg = None
+    fit = None
     if rank == 0 and not args.no_lanczos_g:
-        lg = lanczos_g(pkg, args.lg_config, args.lg_nev)
+        lg = {c: lanczos_g(pkg, c, args.lg_nev) for c in args.lg_config.split(",") if c}
+    if rank == 0 and not args.no_fit:
+        fit = fit_bench(pkg, 0 if args.no_cpu else 2)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         cpu = cpu_baseline_sample(cfg, nup, ndn)
@@ -286,6 +318,7 @@ def run_ours(args):
                                           "ms": round(v[1], 4)} for v in tuning], "chosen": chosen},
             "clocks": clocks,
             "lanczos_g": lg,
+            "fit": fit,
         }
         print(json.dumps(line), flush=True)
     s.close()
@@ -342,7 +375,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-lanczos-g", action="store_true")
-    ap.add_argument("--lg-config", default="C3")
+    ap.add_argument("--lg-config", default="C2,C3,C4", help="comma-separated configurations for Lanczos+G")
+    ap.add_argument("--no-fit", action="store_true")
     ap.add_argument("--lg-nev", type=int, default=6)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

@@ -15,17 +15,13 @@
 // formed by CMPLX(0, w_n) -- a single-precision w_n -- when fortran_cmplx is
 // set, while the 1/w_n weights use the double w_n.
 //
-// frprmn / linmin / mnbrak / brent (frprmn.f90) run on the host exactly as
-// the reference (its default-REAL constants included); every FUNC / dfunc
-// they call is a device launch.  mo_ed_fit_batch runs nbatch fits in
-// lockstep: each fit is a host thread, and the FUNC / dfunc requests of all
-// waiting fits are evaluated by one batched launch.
+// frprmn / linmin / mnbrak / brent (frprmn.f90) are restated once, with the
+// reference's default-REAL constants, as host/device code.  mo_ed_minimization
+// and mo_ed_fit_batch run them on the device, one CTA per fit (k_fit), each
+// FUNC / dfunc evaluated by that CTA: nbatch fits in one launch.
 #include <algorithm>
 #include <cmath>
-#include <condition_variable>
 #include <cstring>
-#include <mutex>
-#include <thread>
 
 #include "internal.h"
 
@@ -44,6 +40,88 @@ __device__ __forceinline__ double2 zdiv(double2 a, double2 b)   // Smith (1962)
     return make_double2((a.x * r + a.y) / den, (a.y * r - a.x) / den);
 }
 
+// chi^2 of one parameter set xb by the whole CTA (blockDim.x threads, one
+// thread per frequency stripe): per-parameter partials in sm [nrow][blockDim.x]
+// summed in a fixed order; thread i < nrow writes row i (f, then g) to out[i].
+__device__ void chi2_block(const double *__restrict__ xb, int nx, bool grad, int nw, int norb, int nbath,
+                           const double *__restrict__ omega, const double *__restrict__ dev, int fcmplx,
+                           double *sm, double *out_f, double *out_g)
+{
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int nrow = grad ? nx + 1 : 1;
+    for (int i = 0; i < nrow; ++i) sm[i * nt + tid] = 0.0;
+    // parameters (x_to_ev)
+    const double *eps = xb;                       // eps_k
+    const double *V = xb + nbath;                 // V[a*nbath + k]
+    const double *ef = xb + nx - norb;            // ef_a
+    for (int n = tid; n < nw; n += nt) {
+        const double w = omega[n];
+        const double wz = fcmplx ? (double)(float)w : w;
+        const double inv_w = 1.0 / w;
+        // 1 / z_k with z_k = i wz - eps_k: one real reciprocal per bath level,
+        // shared by every orbital of this frequency; the orbitals' sums stay
+        // in registers (norb <= kMaxOrb)
+        double dre[kMaxOrb], dim[kMaxOrb];
+#pragma unroll
+        for (int a = 0; a < kMaxOrb; ++a) dre[a] = dim[a] = 0.0;
+        for (int k = 0; k < nbath; ++k) {
+            const double inv = 1.0 / (eps[k] * eps[k] + wz * wz);
+            const double izr = -eps[k] * inv, izi = -wz * inv;
+#pragma unroll
+            for (int a = 0; a < kMaxOrb; ++a) {
+                if (a < norb) {
+                    const double v = V[a * nbath + k];
+                    dre[a] += v * v * izr;
+                    dim[a] += v * v * izi;
+                }
+            }
+        }
+        double rr[kMaxOrb], ri[kMaxOrb];
+#pragma unroll
+        for (int a = 0; a < kMaxOrb; ++a) {
+            rr[a] = ri[a] = 0.0;
+            if (a < norb) {
+                const size_t di = 2 * ((size_t)n * norb + a);
+                rr[a] = (dre[a] + ef[a]) - dev[di];
+                ri[a] = dim[a] - dev[di + 1];
+                const double ar = hypot(rr[a], ri[a]);
+                sm[0 * nt + tid] += ar * ar / w;
+            }
+        }
+        if (grad) {
+            for (int k = 0; k < nbath; ++k) {
+                const double inv = 1.0 / (eps[k] * eps[k] + wz * wz);
+                const double izr = -eps[k] * inv, izi = -wz * inv;
+                const double sr = izr * izr - izi * izi, si = 2.0 * izr * izi;   // 1 / z^2
+#pragma unroll
+                for (int a = 0; a < kMaxOrb; ++a) {
+                    if (a < norb) {
+                        const double v = V[a * nbath + k];
+                        // conjg(r) v v / z / z, with conjg(r) = (rr, -ri)
+                        const double cr = rr[a] * v * v, ci = -ri[a] * v * v;
+                        sm[(1 + k) * nt + tid] += 2.0 * (cr * sr - ci * si) * inv_w;
+                        // conjg(r) v / z + conjg(r) v / z
+                        const double t2 = rr[a] * v * izr + ri[a] * v * izi;
+                        sm[(1 + nbath + a * nbath + k) * nt + tid] += 2.0 * (t2 + t2) * inv_w;
+                    }
+                }
+            }
+#pragma unroll
+            for (int a = 0; a < kMaxOrb; ++a)
+                if (a < norb) sm[(1 + nx - norb + a) * nt + tid] += 2.0 * rr[a] * inv_w;
+        }
+    }
+    __syncthreads();
+    const double fn = (double)(float)(norb * norb * nw);
+    const double gn1 = (double)(float)(norb * norb), gn2 = (double)(float)nw;
+    for (int i = tid; i < nrow; i += nt) {
+        double s = 0.0;
+        for (int t = 0; t < nt; ++t) s += sm[i * nt + t];
+        if (i == 0) *out_f = s / fn;
+        else out_g[i - 1] = s / gn1 / gn2;
+    }
+}
+
 // x: [nreq][nx]; dev: Fortran (norb, nw) interleaved complex; f: [nreq];
 // g: [nreq][nx] (written only where want_grad[b] != 0, or all if want_grad null)
 __global__ void __launch_bounds__(kFitThreads)
@@ -52,58 +130,10 @@ k_chi2(const double *__restrict__ x, int nx, const int *__restrict__ want_grad, 
        double *__restrict__ f, double *__restrict__ g)
 {
     extern __shared__ double sm[];          // [nx + 1][kFitThreads]
-    const int b = blockIdx.x, tid = threadIdx.x;
-    const double *xb = x + (size_t)b * nx;
+    const int b = blockIdx.x;
     const bool grad = g != nullptr && (want_grad ? want_grad[b] != 0 : true);
-    const int nrow = grad ? nx + 1 : 1;
-    for (int i = 0; i < nrow; ++i) sm[i * kFitThreads + tid] = 0.0;
-    // parameters (x_to_ev)
-    const double *eps = xb;                       // eps_k
-    const double *V = xb + nbath;                 // V[a*nbath + k]
-    const double *ef = xb + nx - norb;            // ef_a
-    for (int n = tid; n < nw; n += kFitThreads) {
-        const double w = omega[n];
-        const double wz = fcmplx ? (double)(float)w : w;
-        const double inv_w = 1.0 / w;
-        for (int a = 0; a < norb; ++a) {
-            double2 d = make_double2(0.0, 0.0);
-            for (int k = 0; k < nbath; ++k) {
-                const double v = V[a * nbath + k];
-                const double2 z = make_double2(0.0 - eps[k], wz);
-                const double2 t = zdiv(make_double2(v * v, 0.0), z);
-                d.x += t.x;
-                d.y += t.y;
-            }
-            d.x += ef[a];
-            const size_t di = 2 * ((size_t)n * norb + a);
-            const double2 r = make_double2(d.x - dev[di], d.y - dev[di + 1]);
-            const double ar = hypot(r.x, r.y);
-            sm[0 * kFitThreads + tid] += ar * ar / w;
-            if (grad) {
-                const double2 rc = make_double2(r.x, -r.y);
-                for (int k = 0; k < nbath; ++k) {
-                    const double v = V[a * nbath + k];
-                    const double2 z = make_double2(0.0 - eps[k], wz);
-                    // conjg(r)*vk*vk/(z)/(z)
-                    const double2 t1 = zdiv(zdiv(make_double2(rc.x * v * v, rc.y * v * v), z), z);
-                    sm[(1 + k) * kFitThreads + tid] += 2.0 * t1.x * inv_w;
-                    // conjg(r)*vk/(z) + conjg(r)*vk/(z)
-                    const double2 t2 = zdiv(make_double2(rc.x * v, rc.y * v), z);
-                    sm[(1 + nbath + a * nbath + k) * kFitThreads + tid] += 2.0 * (t2.x + t2.x) * inv_w;
-                }
-                sm[(1 + nx - norb + a) * kFitThreads + tid] += 2.0 * r.x * inv_w;
-            }
-        }
-    }
-    __syncthreads();
-    const double fn = (double)(float)(norb * norb * nw);
-    const double gn1 = (double)(float)(norb * norb), gn2 = (double)(float)nw;
-    for (int i = tid; i < nrow; i += kFitThreads) {
-        double s = 0.0;
-        for (int t = 0; t < kFitThreads; ++t) s += sm[i * kFitThreads + t];
-        if (i == 0) f[b] = s / fn;
-        else g[(size_t)b * nx + (i - 1)] = s / gn1 / gn2;
-    }
+    chi2_block(x + (size_t)b * nx, nx, grad, nw, norb, nbath, omega, dev, fcmplx, sm, f + b,
+               grad ? g + (size_t)b * nx : nullptr);
 }
 
 // calc_dev (ed_green.F90:260-273)
@@ -216,15 +246,15 @@ struct Frprmn {
     const double *pcom = nullptr, *xicom = nullptr;
     double xt[kMaxX];
 
-    static double fsign(double a, double b) { return b >= 0.0 ? std::fabs(a) : -std::fabs(a); }
+    __host__ __device__ static double fsign(double a, double b) { return b >= 0.0 ? fabs(a) : -fabs(a); }
 
-    double f1dim(double x)   // frprmn.f90:212-234
+    __host__ __device__ double f1dim(double x)   // frprmn.f90:212-234
     {
         for (int j = 0; j < n; ++j) xt[j] = pcom[j] + x * xicom[j];
         return func(xt);
     }
 
-    void mnbrak(double &ax, double &bx, double &cx, double &fa, double &fb, double &fc)
+    __host__ __device__ void mnbrak(double &ax, double &bx, double &cx, double &fa, double &fb, double &fc)
     {
         const double GOLD = (double)1.618034f, GLIMIT = (double)100.f, TINY = (double)1.e-20f;
         double dum, fu, q, r, u, ulim;
@@ -239,7 +269,7 @@ struct Frprmn {
         while (fb >= fc) {
             r = (bx - ax) * (fb - fc);
             q = (bx - cx) * (fb - fa);
-            u = bx - ((bx - cx) * q - (bx - ax) * r) / (2. * fsign(std::fmax(std::fabs(q - r), TINY), q - r));
+            u = bx - ((bx - cx) * q - (bx - ax) * r) / (2. * fsign(fmax(fabs(q - r), TINY), q - r));
             ulim = bx + GLIMIT * (cx - bx);
             if ((bx - u) * (u - cx) > 0.) {
                 fu = f1dim(u);
@@ -271,37 +301,37 @@ struct Frprmn {
         }
     }
 
-    int brent(double ax, double bx, double cx, double tol, double &xmin, double &fret)
+    __host__ __device__ int brent(double ax, double bx, double cx, double tol, double &xmin, double &fret)
     {
         const int ITMAX = 100;
         const double CGOLD = (double).3819660f, ZEPS = (double)1.0e-10f;
         double a, b, d = 0.0, e, etemp, fu, fv, fw, fx, p, q, r, tol1, tol2, u, v, w, x, xm;
-        a = std::fmin(ax, cx);
-        b = std::fmax(ax, cx);
+        a = fmin(ax, cx);
+        b = fmax(ax, cx);
         v = bx; w = v; x = v;
         e = 0.;
         fx = f1dim(x);
         fv = fx; fw = fx;
         for (int iter = 1; iter <= ITMAX; ++iter) {
             xm = 0.5 * (a + b);
-            tol1 = tol * std::fabs(x) + ZEPS;
+            tol1 = tol * fabs(x) + ZEPS;
             tol2 = 2. * tol1;
-            if (std::fabs(x - xm) <= (tol2 - .5 * (b - a))) {
+            if (fabs(x - xm) <= (tol2 - .5 * (b - a))) {
                 xmin = x;
                 fret = fx;
                 return 0;
             }
             bool golden = true;
-            if (std::fabs(e) > tol1) {
+            if (fabs(e) > tol1) {
                 r = (x - w) * (fx - fv);
                 q = (x - v) * (fx - fw);
                 p = (x - v) * q - (x - w) * r;
                 q = 2. * (q - r);
                 if (q > 0.) p = -p;
-                q = std::fabs(q);
+                q = fabs(q);
                 etemp = e;
                 e = d;
-                if (!(std::fabs(p) >= std::fabs(.5 * q * etemp) || p <= q * (a - x) || p >= q * (b - x))) {
+                if (!(fabs(p) >= fabs(.5 * q * etemp) || p <= q * (a - x) || p >= q * (b - x))) {
                     d = p / q;
                     u = x + d;
                     if (u - a < tol2 || b - u < tol2) d = fsign(tol1, xm - x);
@@ -312,7 +342,7 @@ struct Frprmn {
                 e = (x >= xm) ? a - x : b - x;
                 d = CGOLD * e;
             }
-            u = (std::fabs(d) >= tol1) ? x + d : x + fsign(tol1, d);
+            u = (fabs(d) >= tol1) ? x + d : x + fsign(tol1, d);
             fu = f1dim(u);
             if (fu <= fx) {
                 if (u >= x) a = x; else b = x;
@@ -331,7 +361,7 @@ struct Frprmn {
         return MO_ED_ERR_FIT;
     }
 
-    int linmin(double *p, double *xi, double &fret)
+    __host__ __device__ int linmin(double *p, double *xi, double &fret)
     {
         const double TOL = (double)1.e-8f;
         double pc[kMaxX], xc[kMaxX], ax, xx, bx, fa, fx, fb, xmin = 0.0;
@@ -352,7 +382,7 @@ struct Frprmn {
         return rc;
     }
 
-    int run(double *p, double ftol, int &iter, double &fret)
+    __host__ __device__ int run(double *p, double ftol, int &iter, double &fret)
     {
         const int itmax = 20000;
         const double eps = 1.e-10;
@@ -367,7 +397,7 @@ struct Frprmn {
         for (int its = 1; its <= itmax; ++its) {
             iter = its;
             if (int rc = linmin(p, xi, fret)) return rc;
-            if (2. * std::fabs(fret - fp) <= ftol * (std::fabs(fret) + std::fabs(fp) + eps)) return 0;
+            if (2. * fabs(fret - fp) <= ftol * (fabs(fret) + fabs(fp) + eps)) return 0;
             fp = fret;
             dfunc(p, xi);
             gg = 0.;
@@ -389,60 +419,88 @@ struct Frprmn {
 };
 
 // ---------------------------------------------------------------------------
-// lockstep batching of many fits: each fit is a host thread; evaluations of
-// all waiting fits go to the device together
+// fits on the device: one CTA of kFitCta threads per fit runs frprmn to the
+// end.  Every thread executes the same frprmn steps on its own copy of the
+// scalars and vectors; each FUNC / dfunc is evaluated by the whole CTA
+// (chi2_block) and broadcast through shared memory, so all threads follow the
+// same path.  No host round trip per evaluation.
 // ---------------------------------------------------------------------------
-struct Batcher {
-    Evaluator *ev;
-    int nx;
-    std::mutex mu;
-    std::condition_variable cv_done;
-    int live = 0, waiting = 0;
-    long long generation = 0;
-    int err = 0;
-    std::vector<double> xs, fs, gs;   // requests of the open batch / results of the last one
-    std::vector<int> want;
+constexpr int kFitCta = 128;   // threads per fit: all four SM sub-partitions' FP64 units
 
-    void init(int nfit) { live = nfit; }
-
-    // Called by one fit; blocks until the batch holding its request has been
-    // evaluated.  A new batch can only close after every reader of the last
-    // one has submitted again or finished, so fs / gs stay valid for them.
-    double request(const double *x, double *g)
+struct DevChi2 {
+    int nx, nw, norb, nbath, fcmplx;
+    const double *omega, *dev;
+    double *sm, *sx, *sres;
+    __device__ double eval(const double *x, double *g)
     {
-        std::unique_lock<std::mutex> lk(mu);
-        const int slot = (int)want.size();
-        xs.insert(xs.end(), x, x + nx);
-        want.push_back(g != nullptr);
-        ++waiting;
-        const long long gen = generation;
-        if (waiting == live) flush();
-        else cv_done.wait(lk, [&] { return generation != gen; });
+        for (int j = threadIdx.x; j < nx; j += blockDim.x) sx[j] = x[j];
+        __syncthreads();
+        chi2_block(sx, nx, g != nullptr, nw, norb, nbath, omega, dev, fcmplx, sm, sres, sres + 1);
+        __syncthreads();
         if (g)
-            for (int j = 0; j < nx; ++j) g[j] = gs[(size_t)slot * nx + j];
-        return fs[slot];
-    }
-    void finish()
-    {
-        std::unique_lock<std::mutex> lk(mu);
-        --live;
-        if (live > 0 && waiting == live) flush();
-    }
-
-  private:
-    void flush()
-    {
-        const int nreq = (int)want.size();
-        fs.assign(nreq, 0.0);
-        gs.assign((size_t)nreq * nx, 0.0);
-        if (int rc = ev->eval(nreq, xs.data(), want.data(), fs.data(), gs.data())) err = rc;
-        xs.clear();
-        want.clear();
-        waiting = 0;
-        ++generation;
-        cv_done.notify_all();
+            for (int j = 0; j < nx; ++j) g[j] = sres[1 + j];
+        const double f = sres[0];
+        __syncthreads();   // sx / sres are reused by the next evaluation
+        return f;
     }
 };
+struct DevFunc {
+    DevChi2 *c;
+    __device__ double operator()(const double *x) const { return c->eval(x, nullptr); }
+};
+struct DevDFunc {
+    DevChi2 *c;
+    __device__ void operator()(const double *x, double *g) const { c->eval(x, g); }
+};
+
+__global__ void __launch_bounds__(kFitCta)
+k_fit(double *__restrict__ X, int nx, int nw, int norb, int nbath, const double *__restrict__ omega,
+      const double *__restrict__ dev, int fcmplx, double ftol, double *fret, int *iter, int *status)
+{
+    extern __shared__ double sm[];   // [nx + 1][kFitCta] partial sums
+    __shared__ double sx[kMaxX], sres[kMaxX + 1];
+    const int b = blockIdx.x;
+    DevChi2 c{nx, nw, norb, nbath, fcmplx, omega, dev, sm, sx, sres};
+    Frprmn<DevFunc, DevDFunc> fr{DevFunc{&c}, DevDFunc{&c}, nx};
+    double p[kMaxX];
+    for (int j = 0; j < nx; ++j) p[j] = X[(size_t)b * nx + j];
+    int it = 0;
+    double f = 0.0;
+    const int rc = fr.run(p, ftol, it, f);
+    if (threadIdx.x == 0) {
+        for (int j = 0; j < nx; ++j) X[(size_t)b * nx + j] = p[j];
+        fret[b] = f;
+        iter[b] = it;
+        status[b] = rc;
+    }
+}
+
+// nbatch fits of host parameter sets x[nbatch][nxsize], in place
+static int fit_on_device(mo_ed_ctx *ctx, FitProblem &P, int nbatch, double *x, double ftol, double *fret, int *iter,
+                         int *status)
+{
+    const int nx = P.nxsize;
+    DevBuf dx, df, di, ds;
+    if (int rc = dev_alloc(ctx, dx, sizeof(double) * (size_t)nbatch * nx)) return rc;
+    if (int rc = dev_alloc(ctx, df, sizeof(double) * nbatch)) return rc;
+    if (int rc = dev_alloc(ctx, di, sizeof(int) * nbatch)) return rc;
+    if (int rc = dev_alloc(ctx, ds, sizeof(int) * nbatch)) return rc;
+    MOED_CUDA(ctx, cudaMemcpyAsync(dx.p, x, sizeof(double) * (size_t)nbatch * nx, cudaMemcpyHostToDevice, ctx->stream));
+    const size_t smem = sizeof(double) * (size_t)(nx + 1) * kFitCta;
+    MOED_CUDA(ctx, cudaFuncSetAttribute(k_fit, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)(sizeof(double) * (kMaxX + 1) * kFitCta)));
+    k_fit<<<nbatch, kFitCta, smem, ctx->stream>>>((double *)dx.p, nx, P.nwloc, P.norb, P.nbath,
+                                                (const double *)P.omega.p, (const double *)P.dev.p,
+                                                ctx->opt.fortran_cmplx, ftol, (double *)df.p, (int *)di.p,
+                                                (int *)ds.p);
+    MOED_CHECK_LAUNCH(ctx);
+    MOED_CUDA(ctx, cudaMemcpyAsync(x, dx.p, sizeof(double) * (size_t)nbatch * nx, cudaMemcpyDeviceToHost, ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpyAsync(fret, df.p, sizeof(double) * nbatch, cudaMemcpyDeviceToHost, ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpyAsync(iter, di.p, sizeof(int) * nbatch, cudaMemcpyDeviceToHost, ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpyAsync(status, ds.p, sizeof(int) * nbatch, cudaMemcpyDeviceToHost, ctx->stream));
+    MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return MO_ED_OK;
+}
 
 }  // namespace moed
 
@@ -497,23 +555,9 @@ int mo_ed_minimization(mo_ed_ctx *ctx, double *x, int nwloc, int ns, int nxsize,
     if (!x || !fret || !iter) return fail(ctx, MO_ED_ERR_ARG, "null argument");
     FitProblem P;
     if (int rc = fit_problem(ctx, P, omega, D_ev, nwloc, ns, nxsize, nbath, norb)) return rc;
-    Evaluator ev{ctx, &P};
-    int err = 0;
-    auto func = [&](const double *xx) {
-        double f = 0;
-        int w = 0;
-        if (int rc = ev.eval(1, xx, &w, &f, nullptr)) err = rc;
-        return f;
-    };
-    auto dfunc = [&](const double *xx, double *g) {
-        double f = 0;
-        int w = 1;
-        if (int rc = ev.eval(1, xx, &w, &f, g)) err = rc;
-    };
-    Frprmn<decltype(func), decltype(dfunc)> fr{func, dfunc, nxsize};
-    int rc = fr.run(x, 1.0e-7, *iter, *fret);   // FTOL (func.f90:155)
-    if (err) return err;
-    if (rc) return fail(ctx, rc, "frprmn: iteration limit exceeded");
+    int status = 0;
+    if (int rc = fit_on_device(ctx, P, 1, x, 1.0e-7, fret, iter, &status)) return rc;   // FTOL (func.f90:155)
+    if (status) return fail(ctx, status, "frprmn: iteration limit exceeded");
     return MO_ED_OK;
 }
 
@@ -527,30 +571,7 @@ int mo_ed_fit_batch(mo_ed_ctx *ctx, int nbatch, double *x, int nwloc, int ns, in
         return fail(ctx, MO_ED_ERR_ARG, "bad arguments");
     FitProblem P;
     if (int rc = fit_problem(ctx, P, omega, D_ev, nwloc, ns, nxsize, nbath, norb)) return rc;
-    Evaluator ev{ctx, &P};
-    Batcher B;
-    B.ev = &ev;
-    B.nx = nxsize;
-    B.init(nbatch);
-    std::vector<std::thread> th;
-    th.reserve(nbatch);
-    for (int b = 0; b < nbatch; ++b) {
-        th.emplace_back([&, b] {
-            auto func = [&](const double *xx) { return B.request(xx, nullptr); };
-            auto dfunc = [&](const double *xx, double *g) { B.request(xx, g); };
-            Frprmn<decltype(func), decltype(dfunc)> fr{func, dfunc, nxsize};
-            int it = 0;
-            double fr_ = 0.0;
-            int rc = fr.run(x + (size_t)b * nxsize, ftol, it, fr_);
-            fret[b] = fr_;
-            iter[b] = it;
-            status[b] = rc;
-            B.finish();
-        });
-    }
-    for (auto &t : th) t.join();
-    if (B.err) return fail(ctx, B.err, "batched chi^2 evaluation failed");
-    return MO_ED_OK;
+    return fit_on_device(ctx, P, nbatch, x, ftol, fret, iter, status);
 }
 
 int mo_ed_calc_dev(mo_ed_ctx *ctx, int norb, int nsite, int nwloc, const double *omega, const double *ek,
