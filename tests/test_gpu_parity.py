@@ -184,6 +184,36 @@ def test_multiply_h_symmetric_c3(setup, oracle):
     assert rel(s.multiply_H(6, 6, 2.0 * x - y), 2.0 * hx - hy) < 1e-13
 
 
+def test_multiply_h_c4_full_size(solver, pkg):
+    """C4 ground sector at full size (D = 41,409,225): FP64 symmetry <x|Hy> =
+    <y|Hx>, linearity, and every FP32 tile-shape variant (staged and previous
+    kernel) against the FP64 product of the same FP32 input."""
+    cfg = pkg.configs.config("C4")
+    ek, vk = cfg.model()
+    solver.set_options(precision="fp64")
+    solver.set_model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
+    nu, nd = 7, 8
+    D = solver.sector_dims(nu, nd)[2]
+    assert D == 41409225
+    rng = np.random.default_rng(14)
+    x, y = rng.standard_normal(D), rng.standard_normal(D)
+    hx, hy = solver.multiply_H(nu, nd, x), solver.multiply_H(nu, nd, y)
+    assert abs(x @ hy - y @ hx) < 1e-11 * abs(x @ hy)
+    assert rel(solver.multiply_H(nu, nd, 2.0 * x - y), 2.0 * hx - hy) < 1e-13
+    del y, hy
+    x32 = x.astype(np.float32)
+    h64 = solver.multiply_H(nu, nd, x32.astype(np.float64))
+    variants, chosen = solver.hv_tuning(nu, nd, pkg.FP32)
+    staged = 0
+    for v, (shape, ms) in enumerate(variants):
+        if ms < 0:
+            continue
+        solver.hv_set_variant(nu, nd, v, pkg.FP32)
+        assert rel(solver.multiply_H(nu, nd, x32), h64) < 2e-6, (v, shape)
+        staged += shape[3]
+    assert staged >= 1
+
+
 # ---------------------------------------------------------------- apply_c
 @pytest.mark.parametrize("name", ["1x4", "3x3_dense", "4x4_mixed"])
 def test_apply_c_bitexact(setup, oracle, name):
@@ -287,6 +317,31 @@ def test_ed_solve_green_c1(solver, oracle, pkg, precision, etol, gtol):
         out.append(sorted((x["sector"], x["level"]) for x in cur))
         return out
     assert groups(st) == groups(st_o)
+    G = solver.ed_calc_green_ftn()
+    Go = oracle.ed_calc_green_ftn(m, cfg.sectors, st_o, vecs, cfg.nstep, om)
+    assert rel(G, Go) < gtol
+
+
+@pytest.mark.parametrize("precision,etol,gtol", [("fp64", 1e-9, 1e-8), ("fp32", 1e-8, 2e-5)])
+def test_ed_solve_green_c2(solver, oracle, pkg, precision, etol, gtol):
+    """Config 2 (2-orbital Kanamori, 3 bath levels per orbital, all 81 sectors,
+    largest 4,900; beta = 100, 2048 w): kept states, probabilities and G(i w_n)
+    vs the oracle (dense / Lanczos eigensolves on the host)."""
+    cfg = pkg.configs.config("C2")
+    ek, vk = cfg.model()
+    nev = 6
+    solver.set_options(precision=precision, nstep=cfg.nstep, nev=nev, beta=cfg.beta)
+    solver.set_model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
+    solver.set_sectors([n for n, _ in cfg.sectors], [u for _, u in cfg.sectors])
+    om = cfg.omega()
+    solver.set_omega(om)
+    st = solver.ed_solve()
+    m = oracle.Model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
+    st_o, vecs = oracle.ed_solve(m, cfg.sectors, nev, cfg.beta)
+    assert len(st) == len(st_o) >= 1
+    for a, c in zip(st, st_o):
+        assert abs(a["val"] - c["val"]) < etol
+        assert abs(a["prob"] - c["prob"]) < 1e3 * etol
     G = solver.ed_calc_green_ftn()
     Go = oracle.ed_calc_green_ftn(m, cfg.sectors, st_o, vecs, cfg.nstep, om)
     assert rel(G, Go) < gtol
