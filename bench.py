@@ -8,7 +8,8 @@ algorithmic bytes (2*D*4: read x once, write y once) per second, aggregated
 over ranks; `e2e` is the same metric through the C-ABI entry point with host
 buffers (pinned H2D of x and D2H of y inside the timed region).  The
 `lanczos_g` object times the full eigensolve + Green's function pipeline on
-one configuration in both precisions and states the E0 / G differences.
+C2, C3 and C4 in both precisions and states the E0 / G differences; `fit`
+times the C5 batched bath fit (256 starts).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -115,7 +116,7 @@ def max_over_ranks(dist, v):
     if dist is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
