@@ -146,14 +146,14 @@ def cpu_baseline_sample(cfg, nup, ndn, seconds=3.0):
                 sample=f"{done} of {b.ntot} rows of one FP64 H*v (oracle C port, OpenMP over rows), {dt:.2f} s")
 
 
-def lanczos_g(pkg, name, nev):
+def lanczos_g(pkg, name, nev, precisions=("fp32", "fp64")):
     """Eigensolve + Green's function in FP32-mixed and FP64; times and errors."""
     import torch
     cfg = pkg.configs.config(name)
     ek, vk = cfg.model()
     out = {"config": name}
     res = {}
-    for prec in ("fp32", "fp64"):
+    for prec in precisions:
         s = pkg.EDSolver(torch.cuda.current_device(), torch.cuda.current_stream().cuda_stream)
         s.set_options(precision=prec, nstep=cfg.nstep, nev=nev, beta=cfg.beta)
         s.set_model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
@@ -170,6 +170,8 @@ def lanczos_g(pkg, name, nev):
                      "E0": float(st[0]["val"]), "nev_calc": len(st), "launches": s.kernel_launches,
                      "eigensolver": s.diag_stats()}
         s.close()
+    if len(res) < 2:
+        return out
     (s32, g32), (s64, g64) = res["fp32"], res["fp64"]
     out["dE0"] = abs(s32[0]["val"] - s64[0]["val"])
     out["dE_kept_max"] = max(abs(a["val"] - b["val"]) for a, b in zip(s32, s64)) if len(s32) == len(s64) else None
@@ -380,9 +382,20 @@ def main():
     ap.add_argument("--no-fit", action="store_true")
     ap.add_argument("--lg-nev", type=int, default=6)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--lg-only", action="store_true",
+                    help="only the Lanczos+G pipeline (one JSON object per configuration; for profiling)")
+    ap.add_argument("--lg-precisions", default="fp32,fp64")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.lg_only:
+        import torch
+        import __graft_entry__ as g
+        torch.cuda.set_stream(torch.cuda.Stream())
+        pkg = g.load_package()
+        for c in args.lg_config.split(","):
+            print(json.dumps(lanczos_g(pkg, c, args.lg_nev, tuple(args.lg_precisions.split(",")))), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
