@@ -17,19 +17,24 @@
 //     the -J.  Both transfers stay inside a bath group (rank offsets that
 //     depend only on the impurity bits).
 //
-// Work decomposition.  An item is up to R rows made of whole down-spin bath
-// groups, so the partner rows of spin-flip / pair hopping are in the item.
-// Items are ordered by the bath occupations of the conserved subsystems, so
-// the down-spin neighbours of the rows in flight stay L2-resident.  A CTA
-// stages its rows in shared memory transposed, S[u][r]: one shared load of
-// S[u'] serves the up-spin move u -> u' for all rows of the item, and the
-// partner rows are shared-memory reads too.  Each thread owns 4 consecutive
-// columns: 16-byte aligned global loads for the down-spin row AXPYs and
-// 16-byte stores of y (rows are padded to a 128-byte stride); its column
-// moves come from a chunk-major table, one contiguous block per slot.  The
-// kernel walks a batch of jobs (vectors of possibly different sectors) so that
-// all excitation vectors of a Lanczos step share one launch; optionally each
-// item writes the FP64 partial of x*y for the Lanczos alpha.
+// Work decomposition (both kernels).  An item is up to R rows made of whole
+// down-spin bath groups, so the partner rows of spin-flip / pair hopping are
+// in the item.  Items are ordered by the bath occupations of the conserved
+// subsystems, so the down-spin neighbours of the rows in flight stay
+// L2-resident.  A kernel walks a batch of jobs (vectors of possibly different
+// sectors) so that all excitation vectors of a Lanczos step share one launch;
+// optionally each item writes the FP64 partial of x*y for the Lanczos alpha.
+//
+// k_hv (first design): a CTA stages its rows in shared memory transposed,
+// S[u][r], by blocking loads; one shared load of S[u'] serves the up-spin move
+// u -> u' for all rows of the item.  Each thread owns 4 consecutive columns:
+// 16-byte global loads for the down-spin row AXPYs and 16-byte stores of y
+// (rows are padded to a 128-byte stride); its column moves come from a
+// chunk-major table, one contiguous block per slot.
+//
+// k_hv_async (below): double-buffered asynchronous stage, conflict-free
+// scheduled up-spin gathers, precomputed item descriptors.  The autotuner
+// picks between the two per (precision, sector).
 #include <algorithm>
 
 #include "internal.h"
