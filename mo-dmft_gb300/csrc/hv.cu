@@ -482,7 +482,7 @@ static size_t dyn_smem_bytes(int ld, const ModelDev &m)
 //     entries hold the stage offset of the target, one bank-conflict-free
 //     shared load per staged row and slot, no predication;
 //   * down-spin row AXPYs: one row offset per move serves the kHvCh chunks.
-constexpr int kHvCh = 2;
+constexpr int kHvCh = 4;
 
 __device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -767,7 +767,7 @@ k_hv_async(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict
         const bool want_dot = jb.dot_partial != nullptr;
         double dacc = 0.0;
         constexpr int SB = 4;
-        constexpr int DB = 4;
+        constexpr int DB = 2;
         for (int cb = warp; cb < nch; cb += NW * kHvCh) {
             // chunks cb + NW*q, q < kHvCh; column of this lane in chunk q: ub + 32*NW*q
             const int ub = 32 * cb + lane;
