@@ -146,8 +146,10 @@ def cpu_baseline_sample(cfg, nup, ndn, seconds=3.0):
                 sample=f"{done} of {b.ntot} rows of one FP64 H*v (oracle C port, OpenMP over rows), {dt:.2f} s")
 
 
-def lanczos_g(pkg, name, nev, precisions=("fp32", "fp64")):
-    """Eigensolve + Green's function in FP32-mixed and FP64; times and errors."""
+def lanczos_g(pkg, name, nev, precisions=("fp32", "fp32+g64", "fp64")):
+    """Eigensolve + Green's function in FP32-mixed, FP32-mixed with an FP64
+    Green's-function recurrence ("fp32+g64") and FP64; times and errors
+    against the FP64 run."""
     import torch
     cfg = pkg.configs.config(name)
     ek, vk = cfg.model()
@@ -155,7 +157,8 @@ def lanczos_g(pkg, name, nev, precisions=("fp32", "fp64")):
     res = {}
     for prec in precisions:
         s = pkg.EDSolver(torch.cuda.current_device(), torch.cuda.current_stream().cuda_stream)
-        s.set_options(precision=prec, nstep=cfg.nstep, nev=nev, beta=cfg.beta)
+        s.set_options(precision=prec.split("+")[0], green_fp64=prec.endswith("+g64"), nstep=cfg.nstep, nev=nev,
+                      beta=cfg.beta)
         s.set_model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
         s.set_sectors([n for n, _ in cfg.sectors], [u for _, u in cfg.sectors])
         s.set_omega(cfg.omega())
@@ -169,14 +172,20 @@ def lanczos_g(pkg, name, nev, precisions=("fp32", "fp64")):
         out[prec] = {"solve_s": round(t1 - t0, 4), "green_s": round(t2 - t1, 4), "total_s": round(t2 - t0, 4),
                      "E0": float(st[0]["val"]), "nev_calc": len(st), "launches": s.kernel_launches,
                      "eigensolver": s.diag_stats()}
+        if prec.endswith("+g64"):
+            out[prec]["refine_res"] = s.green_stats()
         s.close()
-    if len(res) < 2:
+    if "fp64" not in res:
         return out
-    (s32, g32), (s64, g64) = res["fp32"], res["fp64"]
-    out["dE0"] = abs(s32[0]["val"] - s64[0]["val"])
-    out["dE_kept_max"] = max(abs(a["val"] - b["val"]) for a, b in zip(s32, s64)) if len(s32) == len(s64) else None
-    out["dG_rel"] = float(np.abs(g32 - g64).max() / np.abs(g64).max())
-    out["speedup_fp32_vs_fp64"] = round(out["fp64"]["total_s"] / out["fp32"]["total_s"], 3)
+    s64, g64 = res["fp64"]
+    for prec, (s32, g32) in res.items():
+        if prec == "fp64":
+            continue
+        o = out[prec]
+        o["dE0"] = abs(s32[0]["val"] - s64[0]["val"])
+        o["dE_kept_max"] = max(abs(a["val"] - b["val"]) for a, b in zip(s32, s64)) if len(s32) == len(s64) else None
+        o["dG_rel"] = float(np.abs(g32 - g64).max() / np.abs(g64).max())
+        o["speedup_vs_fp64"] = round(out["fp64"]["total_s"] / o["total_s"], 3)
     return out
 
 
@@ -294,7 +303,7 @@ def run_ours(args):
     lg = None
     fit = None
     if rank == 0 and not args.no_lanczos_g:
-        lg = {c: lanczos_g(pkg, c, args.lg_nev) for c in args.lg_config.split(",") if c}
+        lg = {c: lanczos_g(pkg, c, args.lg_nev, tuple(args.lg_precisions.split(","))) for c in args.lg_config.split(",") if c}
     if rank == 0 and not args.no_fit:
         fit = fit_bench(pkg, 0 if args.no_cpu else 2)
     cpu = None
@@ -384,7 +393,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--lg-only", action="store_true",
                     help="only the Lanczos+G pipeline (one JSON object per configuration; for profiling)")
-    ap.add_argument("--lg-precisions", default="fp32,fp64")
+    ap.add_argument("--lg-precisions", default="fp32,fp32+g64,fp64",
+                    help="modes of Lanczos+G: fp32, fp32+g64 (FP64 Green's-function recurrence), fp64")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -69,7 +69,10 @@ typedef struct {
     int green_reorth;   /* must be 0: the Green's-function Lanczos is the reference
                            recurrence without reorthogonalisation (ed_lanczos.F90:53-68);
                            other values are rejected with MO_ED_ERR_ARG */
-    int reserved[8];
+    int green_fp64;     /* 0 (default): the Green's-function Lanczos runs in `precision`;
+                           1: it runs in FP64 whatever `precision` is (FP32 eigenvectors
+                           of ed_solve are widened to FP64 before c / c^dagger) */
+    int reserved[7];
 } mo_ed_options;
 
 /* ---- context ----------------------------------------------------------- */
@@ -196,6 +199,11 @@ int mo_ed_diag(mo_ed_ctx *ctx, int ne_up, int ne_down, int nev, double *eigval, 
  * the largest FP64 residual ||H x - E x|| / ||x|| of the returned vectors. */
 int mo_ed_diag_stats(mo_ed_ctx *ctx, int *cycles, long long *matvecs, double *res_est,
                      double *res_true);
+
+/* Statistics of the last mo_ed_calc_green_ftn (no counterpart in the
+ * reference): with green_fp64 over FP32 eigenvectors, the largest Ritz
+ * residual ||H x - E x|| of their FP64 refinement; 0 when none ran. */
+int mo_ed_green_stats(mo_ed_ctx *ctx, double *refine_res);
 
 /* ---- a14: ed_solve (ed_solver.F90:28-105) ------------------------------- */
 /* All sectors of mo_ed_set_sectors: eigenpairs, heapsort, Boltzmann weights,

@@ -226,10 +226,12 @@ int calc_green(mo_ed_ctx *ctx, double *Gr)
 {
     if (ctx->states.empty()) return fail(ctx, MO_ED_ERR_STATE, "mo_ed_solve has not been run");
     if (ctx->omega.empty()) return fail(ctx, MO_ED_ERR_STATE, "omega grid not set");
-    const int prec = ctx->opt.precision;
+    // The recurrence runs in the eigenvectors' precision, or in FP64 with
+    // green_fp64 (FP32 eigenvectors are widened before c / c^dagger).
+    const int sprec = ctx->states[0].prec;
+    const int prec = ctx->opt.green_fp64 ? MO_ED_FP64 : sprec;
     const int nstep = ctx->opt.nstep;
     const int norb = ctx->norb;
-    const size_t es = prec == MO_ED_FP32 ? sizeof(float) : sizeof(double);
 
     // excitation list in the reference's record order
     struct Exc {
@@ -278,6 +280,21 @@ int calc_green(mo_ed_ctx *ctx, double *Gr)
     std::vector<int> valid;
     for (size_t i = 0; i < exc.size(); ++i)
         if (exc[i].ok) valid.push_back((int)i);
+    // green_fp64 over FP32 states: each kept eigenvector refined in FP64 once
+    std::vector<DevBuf> wide(ctx->states.size());
+    ctx->refine_res = 0.0;
+    if (sprec != prec) {
+        if (prec != MO_ED_FP64) return fail(ctx, MO_ED_ERR_STATE, "eigenvector precision mismatch");
+        for (size_t iev = 0; iev < ctx->states.size(); ++iev) {
+            const StateVec &st = ctx->states[iev];
+            const int nu = ctx->nup[st.sector], nd = ctx->nelec[st.sector] - nu;
+            Sector in;
+            if (int rc = get_sector(ctx, nu, nd, &in)) return rc;
+            double res = 0.0;
+            if (int rc = refine_fp64(ctx, in, (const float *)st.vec.p, wide[iev], &res)) return rc;
+            ctx->refine_res = std::max(ctx->refine_res, res);
+        }
+    }
     for (size_t b0 = 0; b0 < valid.size(); b0 += kLzMaxRuns) {
         const size_t b1 = std::min(valid.size(), b0 + kLzMaxRuns);
         std::vector<Sector> secs;
@@ -287,7 +304,8 @@ int calc_green(mo_ed_ctx *ctx, double *Gr)
         for (size_t k = b0; k < b1; ++k) {
             const Exc &e = exc[valid[k]];
             const StateVec &st = ctx->states[e.iev];
-            if (int rc = apply_c_dev(ctx, e.in, e.out, prec, st.vec.p, lz_start_vector(lb, (int)(k - b0)),
+            const void *x = st.prec == prec ? st.vec.p : wide[e.iev].p;
+            if (int rc = apply_c_dev(ctx, e.in, e.out, prec, x, lz_start_vector(lb, (int)(k - b0)),
                                      e.pm, e.iorb, e.ispin))
                 return rc;
         }
@@ -305,7 +323,6 @@ int calc_green(mo_ed_ctx *ctx, double *Gr)
             A[i] = a[r];
             B[i] = bb[r];
         }
-        (void)es;
     }
     // records: ap, bp(0) = normsq, an, bn(0) = 1 - normsq (ed_green.F90:158,174)
     const int ld = nstep + 1;
@@ -403,6 +420,13 @@ int mo_ed_diag(mo_ed_ctx *ctx, int ne_up, int ne_down, int nev, double *eigval, 
     return MO_ED_OK;
 }
 
+int mo_ed_green_stats(mo_ed_ctx *ctx, double *refine_res)
+{
+    if (!ctx) return MO_ED_ERR_ARG;
+    if (refine_res) *refine_res = ctx->refine_res;
+    return MO_ED_OK;
+}
+
 int mo_ed_diag_stats(mo_ed_ctx *ctx, int *cycles, long long *matvecs, double *res_est, double *res_true)
 {
     if (!ctx) return MO_ED_ERR_ARG;
@@ -449,6 +473,7 @@ int mo_ed_solve(mo_ed_ctx *ctx, int *nev_calc, double *val, double *prob, int *s
         st.level = k % nev;
         st.val = eig_all[k];
         st.prob = pev[k] / Z;
+        st.prec = ctx->opt.precision;
         if (st.level < (int)vecs[st.sector].size()) std::swap(st.vec, vecs[st.sector][st.level]);
         ctx->states.push_back(std::move(st));
         // std::move of DevBuf: ensure ownership transferred

@@ -185,7 +185,8 @@ struct StateVec {             // an eigenpair kept on the device after ed_solve
     int sector;               // 0-based index into the sector list
     int level;                // 0-based level within the sector
     double val, prob;
-    DevBuf vec;               // FP32 or FP64 per precision
+    int prec;                 // MO_ED_FP32 / MO_ED_FP64: the precision of vec
+    DevBuf vec;               // Dpad elements in the layout of its sector
 };
 
 struct GreenRecord {          // one apbpanbn.dat record (ed_green.F90:112-115)
@@ -222,6 +223,7 @@ struct mo_ed_ctx {
     int diag_cycles = 0;
     long long diag_matvecs = 0;
     double diag_res_est = 0.0, diag_res_true = 0.0;
+    double refine_res = 0.0;   // largest Ritz residual of the last FP64 refinement (green_fp64)
 
     // sectors / omega
     std::vector<int> nelec, nup;
@@ -321,6 +323,9 @@ int lanczos_reference_in(mo_ed_ctx *ctx, const Sector &s, const double *h_vec, i
                          int *nstep_calc, double *a, double *b, void *scratch, size_t cap);
 int diag_sector(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<double> &vals,
                 std::vector<DevBuf> *vecs);
+// FP64 refinement of an FP32 eigenvector (short FP64 Lanczos + Rayleigh-Ritz
+// from it); out gets Dpad doubles, res the final Ritz residual.
+int refine_fp64(mo_ed_ctx *ctx, const Sector &s, const float *x, DevBuf &out, double *res);
 
 // ---- Green's function (green.cu) ---------------------------------------------
 int apply_c_dev(mo_ed_ctx *ctx, const Sector &in, const Sector &out, int prec, const void *x,

@@ -1359,6 +1359,112 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
     return MO_ED_OK;
 }
 
+// FP64 refinement of an FP32 eigenvector x (Dpad elements of sector s).
+// The FP32 eigensolve leaves a residual near eps_32 * ||H|| in x, spread over
+// the whole spectrum.  A Lanczos run of kRefineSteps FP64 steps from x (full
+// CGS2 reorthogonalisation) and a Rayleigh-Ritz on its Krylov space damp every
+// component away from the eigenvalue; the Ritz vector with the largest weight
+// on x is the refined vector.  Rounds repeat from it until the Ritz residual
+// is below 1e-9 * ||H|| or kRefineRounds have run: G(i w_n) inherits the
+// vector's error to first order, and a residual 1e-9 * ||H|| leaves it near
+// 1e-8 relative.  out receives the FP64 vector; res the last Ritz residual.
+int refine_fp64(mo_ed_ctx *ctx, const Sector &s, const float *x, DevBuf &out, double *res)
+{
+    constexpr int kRefineSteps = 16, kRefineRounds = 3;
+    const long long D = s.D(), Dp = s.Dpad();
+    const int m0 = (int)std::min<long long>(kRefineSteps, D);
+    const size_t vb = sizeof(double) * (size_t)Dp;
+    std::vector<DevBuf> buf(m0 + 1);
+    for (auto &b : buf)
+        if (int rc = dev_alloc(ctx, b, vb)) return rc;
+    std::vector<DevBuf *> V(m0);
+    for (int i = 0; i < m0; ++i) V[i] = &buf[i];
+    DevBuf *W = &buf[m0];
+    const int G = (int)std::max(1LL, std::min((Dp + kVecThreads - 1) / kVecThreads, (long long)ctx->num_sms * 4));
+    const int n2 = m0 + 2, ldh = n2;
+    DevBuf dHp, dh1, dh2, dpart, dnorm, dbeta, dA, dVj, devals, devecs, dsc;
+    if (int rc = dev_alloc(ctx, dHp, sizeof(double) * (size_t)n2 * n2)) return rc;
+    if (int rc = dev_alloc(ctx, dh1, sizeof(double) * n2)) return rc;
+    if (int rc = dev_alloc(ctx, dh2, sizeof(double) * n2)) return rc;
+    if (int rc = dev_alloc(ctx, dpart, sizeof(double) * (size_t)n2 * ctx->num_sms * 4)) return rc;
+    if (int rc = dev_alloc(ctx, dnorm, sizeof(double) * G)) return rc;
+    if (int rc = dev_alloc(ctx, dbeta, sizeof(double) * 2)) return rc;
+    if (int rc = dev_alloc(ctx, dA, sizeof(double) * (size_t)n2 * n2)) return rc;
+    if (int rc = dev_alloc(ctx, dVj, sizeof(double) * (size_t)n2 * n2)) return rc;
+    if (int rc = dev_alloc(ctx, devals, sizeof(double) * n2)) return rc;
+    if (int rc = dev_alloc(ctx, devecs, sizeof(double) * (size_t)n2 * n2)) return rc;
+    if (int rc = dev_alloc(ctx, dsc, sizeof(double) * 2)) return rc;
+    if (int rc = dev_alloc(ctx, out, vb)) return rc;
+    if (int rc = convert_f32_to_f64(ctx, x, (double *)out.p, Dp)) return rc;
+    double *Hp = (double *)dHp.p;
+    *res = -1.0;
+    for (int round = 0; round < kRefineRounds; ++round) {
+        // V[0] = out / ||out||
+        if (int rc = dot_dev(ctx, MO_ED_FP64, out.p, MO_ED_FP64, out.p, Dp, (double *)dsc.p)) return rc;
+        double nrm2 = 0.0;
+        MOED_CUDA(ctx, cudaMemcpyAsync(&nrm2, dsc.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (!(nrm2 > 0)) return fail(ctx, MO_ED_ERR_NOCONV, "zero eigenvector in FP64 refinement");
+        const double inv = 1.0 / std::sqrt(nrm2);
+        MOED_CUDA(ctx, cudaMemcpyAsync((double *)dsc.p + 1, &inv, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        k_scale_copy<double><<<G, kVecThreads, 0, ctx->stream>>>((const double *)out.p, (double *)V[0]->p, Dp,
+                                                                 (double *)dsc.p + 1);
+        MOED_CHECK_LAUNCH(ctx);
+        MOED_CUDA(ctx, cudaMemsetAsync(dHp.p, 0, dHp.bytes, ctx->stream));
+        // the steps run without a host round trip; a breakdown is found
+        // afterwards and ends the Krylov space there (later steps are discarded)
+        for (int j = 0; j < m0; ++j) {
+            if (int rc = hv_single(ctx, s, HV_F64, V[j]->p, W->p)) return rc;
+            if (int rc = orthogonalize<double>(ctx, V, j + 1, (double *)W->p, Dp, (double *)dh1.p, (double *)dh2.p,
+                                               (double *)dpart.p, (double *)dnorm.p, G))
+                return rc;
+            k_cgs_finish<<<1, 256, 0, ctx->stream>>>((const double *)dh1.p, (const double *)dh2.p, j + 1,
+                                                     (const double *)dnorm.p, G, Hp + (size_t)j * ldh,
+                                                     (double *)dbeta.p);
+            MOED_CHECK_LAUNCH(ctx);
+            if (j + 1 < m0) {
+                k_scale_copy<double><<<G, kVecThreads, 0, ctx->stream>>>((const double *)W->p, (double *)V[j + 1]->p,
+                                                                         Dp, (double *)dbeta.p + 1);
+                MOED_CHECK_LAUNCH(ctx);
+            }
+        }
+        std::vector<double> hc((size_t)ldh * m0);
+        MOED_CUDA(ctx, cudaMemcpyAsync(hc.data(), Hp, sizeof(double) * hc.size(), cudaMemcpyDeviceToHost, ctx->stream));
+        MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        int m = m0;
+        double anorm = 0.0, beta_m = 0.0;
+        for (int j = 0; j < m0; ++j) {
+            const double diag = hc[(size_t)j * ldh + j], beta = hc[(size_t)j * ldh + j + 1];
+            anorm = std::max(anorm, std::fabs(diag) + beta);
+            beta_m = beta;
+            if (j + 1 >= D || beta <= 1e-12 * std::max(anorm, 1.0)) {
+                m = j + 1;
+                beta_m = 0.0;   // invariant subspace: its Ritz pairs are exact
+                break;
+            }
+        }
+        MOED_CUDA(ctx, cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)jacobi_smem(kJacobiSmem)));
+        k_jacobi<<<1, 256, jacobi_smem(m), ctx->stream>>>(Hp, ldh, m, 0, (const double *)dh1.p, (double *)dA.p,
+                                                           (double *)dVj.p, (double *)devals.p, (double *)devecs.p, 60);
+        MOED_CHECK_LAUNCH(ctx);
+        std::vector<double> ev((size_t)m * m);
+        MOED_CUDA(ctx, cudaMemcpyAsync(ev.data(), devecs.p, sizeof(double) * ev.size(), cudaMemcpyDeviceToHost, ctx->stream));
+        MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        int best = 0;
+        for (int i = 1; i < m; ++i)
+            if (std::fabs(ev[(size_t)i * m]) > std::fabs(ev[(size_t)best * m])) best = i;
+        *res = std::fabs(beta_m * ev[(size_t)best * m + (m - 1)]);
+        VPtrs<double> P = make_ptrs<double>(V, m);
+        std::vector<DevBuf *> o(1, &out);
+        VPtrs<double> X = make_ptrs<double>(o, 1);
+        k_rotate<double, 8><<<G, kVecThreads, 0, ctx->stream>>>(P, m, (const double *)devecs.p, m, best, 1, X, Dp);
+        MOED_CHECK_LAUNCH(ctx);
+        if (*res <= 1e-9 * std::max(anorm, 1.0)) break;
+    }
+    return MO_ED_OK;
+}
+
 int diag_sector(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<double> &vals,
                 std::vector<DevBuf> *vecs)
 {

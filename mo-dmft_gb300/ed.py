@@ -49,7 +49,8 @@ class Options(C.Structure):
     """mo_ed_options (include/mo_ed.h)."""
     _fields_ = [("nstep", C.c_int), ("nev", C.c_int), ("beta", C.c_double), ("precision", C.c_int),
                 ("fortran_cmplx", C.c_int), ("gs_ncv", C.c_int), ("gs_maxcycles", C.c_int),
-                ("gs_tol", C.c_double), ("green_reorth", C.c_int), ("reserved", C.c_int * 8)]
+                ("gs_tol", C.c_double), ("green_reorth", C.c_int),
+                ("green_fp64", C.c_int), ("reserved", C.c_int * 7)]
 
 
 class EDError(RuntimeError):
@@ -90,6 +91,7 @@ SIGNATURES = [
     ("mo_ed_lanczos_iteration_noalloc", C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _ip, _dp, _dp]),
     ("mo_ed_diag", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _dp]),
     ("mo_ed_diag_stats", C.c_int, [C.c_void_p, _ip, _llp, _dp, _dp]),
+    ("mo_ed_green_stats", C.c_int, [C.c_void_p, _dp]),
     ("mo_ed_solve", C.c_int, [C.c_void_p, _ip, _dp, _dp, _ip, _ip, C.c_int]),
     ("mo_ed_calc_green_ftn", C.c_int, [C.c_void_p, _dp]),
     ("mo_ed_green_coeffs", C.c_int, [C.c_void_p, _ip, _ip, _dp, C.c_int]),
@@ -209,7 +211,7 @@ class EDSolver:
         for k, v in kw.items():
             if k == "precision" and isinstance(v, str):
                 v = {"fp32": FP32, "fp64": FP64}[v.lower()]
-            if k in ("fortran_cmplx", "green_reorth"):
+            if k in ("fortran_cmplx", "green_reorth", "green_fp64"):
                 v = int(bool(v))
             setattr(self.opt, k, v)
         self._chk(lib().mo_ed_set_options(self._ctx, C.byref(self.opt)))
@@ -350,6 +352,13 @@ class EDSolver:
         c, m, a, b = C.c_int(), C.c_longlong(), C.c_double(), C.c_double()
         self._chk(lib().mo_ed_diag_stats(self._ctx, C.byref(c), C.byref(m), C.byref(a), C.byref(b)))
         return dict(cycles=c.value, matvecs=m.value, res_est=a.value, res_true=b.value)
+
+    def green_stats(self):
+        """Largest Ritz residual of the FP64 eigenvector refinement of the last
+        ed_calc_green_ftn (green_fp64 over FP32 eigenvectors; 0 if none ran)."""
+        r = C.c_double()
+        self._chk(lib().mo_ed_green_stats(self._ctx, C.byref(r)))
+        return r.value
 
     def ed_solve(self):
         """ed_solver.F90:28 -> list of eigval_t dicts (val, prob, sector, level; 1-based)."""

@@ -34,7 +34,8 @@ module mo_ed_bind
         integer(c_int) :: gs_maxcycles
         real(c_double) :: gs_tol
         integer(c_int) :: green_reorth
-        integer(c_int) :: reserved(8)
+        integer(c_int) :: green_fp64
+        integer(c_int) :: reserved(7)
     end type mo_ed_options
 
     interface

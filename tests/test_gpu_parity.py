@@ -8,7 +8,9 @@ Tolerances (stated per test):
   * FP64 Lanczos coefficients: 1e-9 relative over the first 12 steps (later
     steps amplify rounding after loss of orthogonality in both codes);
   * FP64 eigenvalues: 1e-9 absolute; FP32-mixed eigenvalues: 1e-8 absolute;
-  * G(i w_n): FP64 1e-8, FP32-mixed 1e-5, relative to max |G|;
+  * G(i w_n): FP64 1e-8, FP32-mixed 1e-5 (2e-5 on config 2), FP32-mixed
+    eigensolve with green_fp64 (FP64 refinement of the kept eigenvectors and
+    an FP64 Green's-function recurrence) 1e-7, relative to max |G|;
   * chi^2 / gradient: 1e-12 relative.
 """
 import numpy as np
@@ -286,14 +288,16 @@ def test_diag_vs_dense(setup, oracle, precision, tol):
 
 
 # ---------------------------------------------------------------- ed_solve + G
-@pytest.mark.parametrize("precision,etol,gtol", [("fp64", 1e-9, 1e-8), ("fp32", 1e-8, 1e-5)])
+@pytest.mark.parametrize("precision,etol,gtol", [("fp64", 1e-9, 1e-8), ("fp32", 1e-8, 1e-5),
+                                                  ("fp32+g64", 1e-8, 1e-7)])
 def test_ed_solve_green_c1(solver, oracle, pkg, precision, etol, gtol):
     """Config 1 (single band, 4 bath levels, all 36 sectors, beta = 50, 1024 w,
     100 steps): states, probabilities and G(i w_n) vs the oracle."""
     cfg = pkg.configs.config("C1")
     ek, vk = cfg.model()
     nev = 8
-    solver.set_options(precision=precision, nstep=cfg.nstep, nev=nev, beta=cfg.beta)
+    solver.set_options(precision=precision.split("+")[0], green_fp64=precision.endswith("+g64"),
+                       nstep=cfg.nstep, nev=nev, beta=cfg.beta)
     solver.set_model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
     solver.set_sectors([n for n, _ in cfg.sectors], [u for _, u in cfg.sectors])
     om = cfg.omega()
@@ -322,7 +326,8 @@ def test_ed_solve_green_c1(solver, oracle, pkg, precision, etol, gtol):
     assert rel(G, Go) < gtol
 
 
-@pytest.mark.parametrize("precision,etol,gtol", [("fp64", 1e-9, 1e-8), ("fp32", 1e-8, 2e-5)])
+@pytest.mark.parametrize("precision,etol,gtol", [("fp64", 1e-9, 1e-8), ("fp32", 1e-8, 2e-5),
+                                                  ("fp32+g64", 1e-8, 1e-7)])
 def test_ed_solve_green_c2(solver, oracle, pkg, precision, etol, gtol):
     """Config 2 (2-orbital Kanamori, 3 bath levels per orbital, all 81 sectors,
     largest 4,900; beta = 100, 2048 w): kept states, probabilities and G(i w_n)
@@ -330,7 +335,8 @@ def test_ed_solve_green_c2(solver, oracle, pkg, precision, etol, gtol):
     cfg = pkg.configs.config("C2")
     ek, vk = cfg.model()
     nev = 6
-    solver.set_options(precision=precision, nstep=cfg.nstep, nev=nev, beta=cfg.beta)
+    solver.set_options(precision=precision.split("+")[0], green_fp64=precision.endswith("+g64"),
+                       nstep=cfg.nstep, nev=nev, beta=cfg.beta)
     solver.set_model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
     solver.set_sectors([n for n, _ in cfg.sectors], [u for _, u in cfg.sectors])
     om = cfg.omega()
@@ -344,7 +350,12 @@ def test_ed_solve_green_c2(solver, oracle, pkg, precision, etol, gtol):
         assert abs(a["prob"] - c["prob"]) < 1e3 * etol
     G = solver.ed_calc_green_ftn()
     Go = oracle.ed_calc_green_ftn(m, cfg.sectors, st_o, vecs, cfg.nstep, om)
+    print(precision, rel(G, Go), solver.green_stats())
     assert rel(G, Go) < gtol
+    if precision == "fp32+g64":
+        assert 0 < solver.green_stats() < 1e-7   # Ritz residual of the FP64 refinement
+    else:
+        assert solver.green_stats() == 0
 
 
 # ---------------------------------------------------------------- bath fit
