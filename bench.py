@@ -146,6 +146,11 @@ def cpu_baseline_sample(cfg, nup, ndn, seconds=3.0):
                 sample=f"{done} of {b.ntot} rows of one FP64 H*v (oracle C port, OpenMP over rows), {dt:.2f} s")
 
 
+# H*v kernel of each tile-shape variant kind (hv_tuning's fourth field)
+KERNEL_NAMES = {0: "k_hv", 1: "k_hv_async", 2: "k_hv_down (128-byte slices) + k_hv_async<split>",
+                3: "k_hv_down (64-byte slices) + k_hv_async<split>"}
+
+
 def lanczos_g(pkg, name, nev, precisions=("fp32", "fp32+g64", "fp64")):
     """Eigensolve + Green's function in FP32-mixed, FP32-mixed with an FP64
     Green's-function recurrence ("fp32+g64") and FP64; times and errors
@@ -326,7 +331,7 @@ def run_ours(args):
                     "ms_per_step": round(t_e2e * 1e3, 4)},
             "gpu_launches": launches,
             "hv_autotune": {"variants": [{"rows_per_item": v[0][0], "threads": v[0][1], "ctas_per_sm": v[0][2],
-                                          "kernel": "k_hv_async" if v[0][3] else "k_hv",
+                                          "kernel": KERNEL_NAMES[v[0][3]],
                                           "ms": round(v[1], 4)} for v in tuning], "chosen": chosen},
             "clocks": clocks,
             "lanczos_g": lg,

@@ -143,8 +143,11 @@ int mo_ed_multiply_h_mixed_dev(mo_ed_ctx *ctx, int ne_up, int ne_down, const flo
  * times every variant on that sector and keeps the fastest; this call runs
  * the tuning if needed and reports *nvariant variants: shape[4*i..4*i+3] =
  * (rows per item, threads per CTA, CTAs per SM, kernel: 0 k_hv, 1 the
- * double-buffered staged k_hv_async), ms[i] (negative: does not
- * fit), and the *chosen index.  Arrays hold capacity variants. */
+ * double-buffered staged k_hv_async, 2 / 3 split: k_hv_down over down-spin
+ * blocks on 128- / 64-byte row slices, then k_hv_async for the other terms),
+ * ms[i] (negative: does not fit this sector or model), and the *chosen
+ * index.  Arrays hold capacity variants.  Pinning a split variant on a model
+ * whose down-spin blocks do not fit one CTA fails with MO_ED_ERR_ARG. */
 int mo_ed_hv_tuning(mo_ed_ctx *ctx, int ne_up, int ne_down, int dtype, int capacity, int *nvariant,
                     int *shape, float *ms, int *chosen);
 /* Pin the H*v variant (index into the list mo_ed_hv_tuning reports) of a

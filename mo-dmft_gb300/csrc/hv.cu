@@ -33,8 +33,12 @@
 // chunk-major table, one contiguous block per slot.
 //
 // k_hv_async (below): double-buffered asynchronous stage, conflict-free
-// scheduled up-spin gathers, precomputed item descriptors.  The autotuner
-// picks between the two per (precision, sector).
+// scheduled up-spin gathers, precomputed item descriptors.
+//
+// Split (below): k_hv_down computes the down-spin hybridisation over
+// down-spin blocks x column slices from shared memory, then k_hv_async<SPLIT>
+// adds the other terms.  The autotuner picks among all of them per
+// (precision, sector).
 #include <algorithm>
 
 #include "internal.h"
@@ -699,7 +703,9 @@ __device__ __forceinline__ void hv_stage_item(const HvBatch<TA> &b, int item, TX
     cp_async_commit();
 }
 
-template <typename TX, typename TA, typename TY, int R, int NT, int MINB>
+// SPLIT: k_hv_down has already written the down-spin hybridisation into y;
+// this kernel adds the other terms to it instead of computing the row AXPYs.
+template <typename TX, typename TA, typename TY, int R, int NT, int MINB, bool SPLIT>
 __global__ void __launch_bounds__(NT, MINB)
 k_hv_async(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict__ mdl, const DescGeom g)
 {
@@ -780,17 +786,29 @@ k_hv_async(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict
                 has[q] = cb + NW * q < nch;
                 h[q] = has[q] ? __ldg(jb.up_sched_hdr + cb + NW * q) : make_int2(0, 0);
             }
-            // the first DB down-spin moves of every row: loads in flight early
+            // the first DB down-spin moves of every row (SPLIT: the down-spin
+            // part already in y): loads in flight early
             TX gd[R][DB][kHvCh];
+            TY yp[R][kHvCh];
+            if constexpr (SPLIT) {
 #pragma unroll
-            for (int r = 0; r < R; ++r)
+                for (int r = 0; r < R; ++r) {
+                    const TY *yr = y + (size_t)(live[r] ? s_d[r] : 0) * ld + ub;
 #pragma unroll
-                for (int t = 0; t < DB; ++t) {
-                    const bool mv = t < dcnt[r];
-                    const TX *xr = x + (size_t)s_dtgt[r * dm + (mv ? t : 0)] * ld + ub;
-#pragma unroll
-                    for (int q = 0; q < kHvCh; ++q) gd[r][t][q] = (mv && has[q]) ? __ldg(xr + 32 * NW * q) : TX(0);
+                    for (int q = 0; q < kHvCh; ++q) yp[r][q] = (live[r] && has[q]) ? yr[32 * NW * q] : TY(0);
                 }
+            } else {
+#pragma unroll
+                for (int r = 0; r < R; ++r)
+#pragma unroll
+                    for (int t = 0; t < DB; ++t) {
+                        const bool mv = t < dcnt[r];
+                        const TX *xr = x + (size_t)s_dtgt[r * dm + (mv ? t : 0)] * ld + ub;
+#pragma unroll
+                        for (int q = 0; q < kHvCh; ++q)
+                            gd[r][t][q] = (mv && has[q]) ? __ldg(xr + 32 * NW * q) : TX(0);
+                    }
+            }
             // first SB schedule entries of every chunk
             HopEnt<TA> e0[kHvCh][SB];
 #pragma unroll
@@ -891,6 +909,12 @@ k_hv_async(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict
                 }
             }
             // down-spin hybridisation: the early loads, then the remaining moves
+            if constexpr (SPLIT) {
+#pragma unroll
+                for (int r = 0; r < R; ++r)
+#pragma unroll
+                    for (int q = 0; q < kHvCh; ++q) acc[q][r] += (TA)yp[r][q];
+            } else {
 #pragma unroll
             for (int r = 0; r < R; ++r) {
 #pragma unroll
@@ -919,6 +943,7 @@ k_hv_async(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict
                         }
                     }
                 }
+            }
             }
 #pragma unroll
             for (int r = 0; r < R; ++r) {
@@ -958,6 +983,173 @@ k_hv_async(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict
     asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
+// ---------------------------------------------------------------------------
+// k_hv_down: the down-spin hybridisation of the split H*v,
+//   y[d][u] = sum over moves (d -> d', t) of t * x[d'][u],
+// for every row d, written (not accumulated) into y; k_hv_async<SPLIT> then
+// adds the other terms.  The rows of a down-spin block (equal electron counts
+// in every conserved subsystem) are closed under the moves, so a chunk = one
+// block x a range of columns is independent of all others.  A CTA stages the
+// block's move list once ({target index within the block, signed coupling})
+// and then walks the chunk's column slices, staged by cp.async and double-
+// buffered when two slices fit.  A slice is kb groups of WB bytes (one 64- or
+// 128-byte line segment) of every row of the block, kb as large as the buffer
+// allows, so small blocks take wide slices.  Every element of x is read from
+// memory once per H*v and the moves read shared memory only.  CTAs take
+// contiguous chunk ranges, so consecutive chunks usually share the block and
+// its move list.
+// ---------------------------------------------------------------------------
+template <typename TA>
+__device__ __forceinline__ int hv_tile_job(const HvBatch<TA> &b, int tile)
+{
+    int j = 0;
+    while (j + 1 < b.njobs && tile >= b.job[j + 1].tile0) ++j;
+    return j;
+}
+
+struct DownLayout {        // shared-memory layout of k_hv_down, in bytes
+    int ptr, rows, mv, x0, x1;
+};
+
+// stage columns [col, col + kw * W) of the block's rows: row i at buf + i * kw * W
+template <typename TX, int NT, int WB>
+__device__ __forceinline__ void hv_down_slice(const TX *__restrict__ x, const int *s_rows, int nr, int ld,
+                                              int col, int kw, TX *buf)
+{
+    constexpr int CPG = WB / 16;                // 16-byte copies per group of a row
+    constexpr int EPV = 16 / (int)sizeof(TX);
+    const int cpr = kw * CPG;
+    for (int q = threadIdx.x; q < nr * cpr; q += NT) {
+        const int i = q / cpr, c = q - i * cpr;
+        cp_async16(buf + (size_t)i * cpr * EPV + c * EPV, x + (size_t)s_rows[i] * ld + col + c * EPV);
+    }
+}
+
+template <typename TX, typename TA, typename TY, int NT, int WB>
+__global__ void __launch_bounds__(NT, 1)
+k_hv_down(const __grid_constant__ HvBatch<TA> batch, int total, const DownLayout L, int cap_rows, int dbuf)
+{
+    extern __shared__ __align__(16) unsigned char smem_down[];
+    constexpr int W = WB / (int)sizeof(TX);   // columns per group (one WB-byte segment of a row)
+    constexpr int RPW = 32 / W;               // groups per warp pass
+    constexpr int NW = NT / 32;
+    int *s_ptr = reinterpret_cast<int *>(smem_down + L.ptr);
+    int *s_rows = reinterpret_cast<int *>(smem_down + L.rows);
+    HopEnt<TA> *s_mv = reinterpret_cast<HopEnt<TA> *>(smem_down + L.mv);
+    TX *const xb0 = reinterpret_cast<TX *>(smem_down + L.x0);
+    TX *const xb1 = reinterpret_cast<TX *>(smem_down + L.x1);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int sub = lane / W, c = lane - sub * W;
+    const int c_begin = (int)((long long)total * blockIdx.x / gridDim.x);
+    const int c_end = (int)((long long)total * (blockIdx.x + 1) / gridDim.x);
+    int have_job = -1, have_blk = -1;
+    for (int ch = c_begin; ch < c_end; ++ch) {
+        const int jid = hv_tile_job(batch, ch);
+        const HvJobT<TA> &jb = batch.job[jid];
+        if (jb.active && *jb.active == 0) continue;
+        const int lc = ch - jb.tile0;
+        // block of this chunk: last b with chunks[b].x <= lc
+        int lo = 0, hi = jb.dblk_n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(&jb.dblk_chunks[mid].x) <= lc) lo = mid;
+            else hi = mid - 1;
+        }
+        const int blk = lo;
+        const int2 cinfo = jb.dblk_chunks[blk];
+        const int ld = jb.ld;
+        const int col0 = (lc - cinfo.x) * cinfo.y * 32;
+        const int col1 = min(ld, col0 + cinfo.y * 32);
+        const int p0 = __ldg(jb.dblk_off + blk), nr = __ldg(jb.dblk_off + blk + 1) - p0;
+        const TX *x = (const TX *)jb.x;
+        TY *y = (TY *)jb.y;
+        __syncthreads();   // the previous chunk is done with shared memory
+        if (jid != have_job || blk != have_blk) {
+            const int m0 = __ldg(jb.dblk_ptr + p0), nm = __ldg(jb.dblk_ptr + p0 + nr) - m0;
+            for (int i = tid; i <= nr; i += NT) s_ptr[i] = __ldg(jb.dblk_ptr + p0 + i) - m0;
+            for (int i = tid; i < nr; i += NT) s_rows[i] = __ldg(jb.dblk_rows + p0 + i);
+            for (int i = tid; i < nm; i += NT) s_mv[i] = jb.dblk_mv[m0 + i];
+            have_job = jid;
+            have_blk = blk;
+            __syncthreads();
+        }
+        // a slice = kb groups of W columns of every row (small blocks: wide slices)
+        const int ngr = (col1 - col0) / W;
+        const int kb = max(1, min(cap_rows / nr, ngr));
+        const int ns = (ngr + kb - 1) / kb;
+        hv_down_slice<TX, NT, WB>(x, s_rows, nr, ld, col0, min(kb, ngr), xb0);
+        cp_async_commit();
+        for (int sl = 0; sl < ns; ++sl) {
+            const TX *S = (dbuf && (sl & 1)) ? xb1 : xb0;
+            const int kw = min(kb, ngr - sl * kb);   // groups in this slice
+            if (dbuf && sl + 1 < ns) {
+                hv_down_slice<TX, NT, WB>(x, s_rows, nr, ld, col0 + (sl + 1) * kb * W, min(kb, ngr - (sl + 1) * kb),
+                                          (sl & 1) ? xb0 : xb1);
+                cp_async_commit();
+                cp_async_wait_all_but_newest();
+            } else {
+                asm volatile("cp.async.wait_all;" ::: "memory");
+            }
+            __syncthreads();
+            const int ws = kw * W;               // row stride of the staged slice
+            TY *ys = y + col0 + sl * kb * W + c;
+            if (kw == 1) {
+                // one group per row (large blocks): 4 moves in flight
+                for (int i = warp * RPW + sub; i < nr; i += NW * RPW) {
+                    const int b1 = s_ptr[i], e1 = s_ptr[i + 1];
+                    const TX *Sc = S + c;
+                    TA a = TA(0);
+                    int e = b1;
+                    for (; e + 4 <= e1; e += 4) {
+                        const HopEnt<TA> m0 = s_mv[e], m1 = s_mv[e + 1], m2 = s_mv[e + 2], m3 = s_mv[e + 3];
+                        const TX x0 = Sc[m0.t * W], x1 = Sc[m1.t * W], x2 = Sc[m2.t * W], x3 = Sc[m3.t * W];
+                        a += m0.v * (TA)x0;
+                        a += m1.v * (TA)x1;
+                        a += m2.v * (TA)x2;
+                        a += m3.v * (TA)x3;
+                    }
+                    for (; e < e1; ++e) {
+                        const HopEnt<TA> m = s_mv[e];
+                        a += m.v * (TA)Sc[m.t * W];
+                    }
+                    ys[(size_t)s_rows[i] * ld] = (TY)a;
+                }
+            } else {
+                // several groups per row (small blocks, wide slices): each move
+                // serves up to KQ groups
+                constexpr int KQ = 4;
+                const int npass = (kw + KQ - 1) / KQ;
+                for (int it = warp * RPW + sub; it < nr * npass; it += NW * RPW) {
+                    const int i = it / npass, g0 = (it - i * npass) * KQ;
+                    const int b1 = s_ptr[i], e1 = s_ptr[i + 1];
+                    const TX *Sc = S + g0 * W + c;
+                    TA a[KQ];
+#pragma unroll
+                    for (int q = 0; q < KQ; ++q) a[q] = TA(0);
+                    for (int e = b1; e < e1; ++e) {
+                        const HopEnt<TA> m = s_mv[e];
+                        const TX *Sm = Sc + m.t * ws;
+#pragma unroll
+                        for (int q = 0; q < KQ; ++q)
+                            if (g0 + q < kw) a[q] += m.v * (TA)Sm[q * W];
+                    }
+                    TY *yr = ys + (size_t)s_rows[i] * ld + g0 * W;
+#pragma unroll
+                    for (int q = 0; q < KQ; ++q)
+                        if (g0 + q < kw) yr[q * W] = (TY)a[q];
+                }
+            }
+            __syncthreads();   // slice done: its buffer is free
+            if (!dbuf && sl + 1 < ns) {
+                hv_down_slice<TX, NT, WB>(x, s_rows, nr, ld, col0 + (sl + 1) * kb * W, min(kb, ngr - (sl + 1) * kb),
+                                          xb0);
+                cp_async_commit();
+            }
+        }
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
 template <typename TX, typename TA, int R>
 static size_t dyn_smem_bytes_async(int ld, const ModelDev &m, const DescGeom &g)
 {
@@ -977,11 +1169,15 @@ static size_t dyn_smem_bytes_async(int ld, const ModelDev &m, const DescGeom &g)
 // (scratch vectors, CUDA events on the context stream) and keeps the fastest.
 struct HvVariant {
     int R, NT, MINB;
-    int staged; // 1: k_hv_async (double-buffered asynchronous stage), 0: k_hv
+    // 0: k_hv; 1: k_hv_async (double-buffered asynchronous stage);
+    // 2 / 3: split, k_hv_down on 128- / 64-byte row slices + k_hv_async<SPLIT>
+    int staged;
 };
-static const HvVariant kVarF32[] = {{3, 512, 2, 0}, {4, 256, 2, 0}, {6, 512, 1, 0}, {3, 256, 3, 0}, {8, 512, 1, 0},
-                                    {4, 512, 1, 1}, {3, 512, 1, 1}, {2, 512, 2, 1}, {2, 256, 2, 1}};
-static const HvVariant kVarF64[] = {{2, 256, 2, 0}, {3, 256, 1, 0}, {2, 512, 1, 0}, {2, 512, 1, 1}, {4, 512, 1, 1}};
+static const HvVariant kVarF32[] = {{3, 512, 2, 0}, {4, 256, 2, 0}, {6, 512, 1, 0}, {3, 256, 3, 0},
+                                    {8, 512, 1, 0}, {4, 512, 1, 1}, {3, 512, 1, 1}, {2, 512, 2, 1},
+                                    {2, 256, 2, 1}, {3, 512, 1, 2}, {4, 512, 1, 2}, {3, 512, 1, 3}};
+static const HvVariant kVarF64[] = {{2, 256, 2, 0}, {3, 256, 1, 0}, {2, 512, 1, 0}, {2, 512, 1, 1},
+                                    {4, 512, 1, 1}, {2, 512, 1, 2}, {2, 512, 1, 3}};
 static const int kNVarF32 = sizeof(kVarF32) / sizeof(kVarF32[0]);
 static const int kNVarF64 = sizeof(kVarF64) / sizeof(kVarF64[0]);
 
@@ -1025,6 +1221,19 @@ void hv_fill_job(const mo_ed_ctx *ctx, const Sector &s, int R, const void *x, vo
         auto dsc = s.dn->desc.find(R * 2 + (f32 ? 0 : 1));
         j.desc = dsc != s.dn->desc.end() ? dsc->second : nullptr;
     }
+    j.dblk_off = s.dn->dblk_off;
+    j.dblk_rows = s.dn->dblk_rows;
+    j.dblk_ptr = s.dn->dblk_ptr;
+    j.dblk_mv = f32 ? (const HopEnt<TA> *)s.dn->dblk_mv_f : (const HopEnt<TA> *)s.dn->dblk_mv_d;
+    {
+        auto ch = s.dn->dblk_chunks.find(s.ld());
+        j.dblk_chunks = ch != s.dn->dblk_chunks.end() ? ch->second : nullptr;
+        j.ntiles = ch != s.dn->dblk_chunks.end() ? s.dn->dblk_nchunks.at(s.ld()) : 0;
+    }
+    j.dblk_n = s.dn->dblk_n;
+    j.dblk_max = s.dn->dblk_max;
+    j.dblk_mvmax = s.dn->dblk_mvmax;
+    j.tile0 = 0;
     if (f32) {
         auto sf = s.up->sched_rf.find(R);
         j.up_sched = sf != s.up->sched_rf.end() ? (const HopEnt<TA> *)sf->second : nullptr;
@@ -1058,7 +1267,7 @@ static int launch_batch(mo_ed_ctx *ctx, const HvBatch<TA> &b)
     return MO_ED_OK;
 }
 
-template <typename TX, typename TA, typename TY, int R, int NT, int MINB = 1>
+template <typename TX, typename TA, typename TY, int R, int NT, int MINB = 1, bool SPLIT = false>
 static int launch_batch_async(mo_ed_ctx *ctx, const HvBatch<TA> &b)
 {
     if (b.total_items <= 0) return MO_ED_OK;
@@ -1070,7 +1279,7 @@ static int launch_batch_async(mo_ed_ctx *ctx, const HvBatch<TA> &b)
     }
     const DescGeom g = desc_geom<TA, R>(ctx->mdl.ncpl, ctx->mdl);
     const size_t smem = dyn_smem_bytes_async<TX, TA, R>(ldmax, ctx->mdl, g);
-    auto kern = k_hv_async<TX, TA, TY, R, NT, MINB>;
+    auto kern = k_hv_async<TX, TA, TY, R, NT, MINB, SPLIT>;
     MOED_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     MOED_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     int per_sm = 0;
@@ -1080,6 +1289,77 @@ static int launch_batch_async(mo_ed_ctx *ctx, const HvBatch<TA> &b)
     kern<<<grid, NT, smem, ctx->stream>>>(b, ctx->d_mdl, g);
     MOED_CHECK_LAUNCH(ctx);
     return MO_ED_OK;
+}
+
+constexpr int kDownNT = 1024;
+constexpr size_t kDownSmemMax = 220 * 1024;   // dynamic shared memory of one k_hv_down CTA
+
+static size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
+
+// shared-memory layout of k_hv_down for blocks of up to `rows` rows and `mv`
+// moves and slices of wb bytes per row; nbuf = 1 or 2 slice buffers
+static DownLayout down_layout(int rows, int mv, size_t wb, int nbuf, size_t ent_bytes, size_t *total)
+{
+    DownLayout L;
+    size_t o = 0;
+    L.ptr = (int)o;
+    o = align16(o + sizeof(int) * ((size_t)rows + 1));
+    L.rows = (int)o;
+    o = align16(o + sizeof(int) * (size_t)rows);
+    L.mv = (int)o;
+    o = align16(o + ent_bytes * (size_t)std::max(mv, 1));
+    L.x0 = (int)o;
+    o += (size_t)rows * wb;
+    L.x1 = (int)o;
+    if (nbuf == 2) o += (size_t)rows * wb;
+    *total = o;
+    return L;
+}
+
+// Split H*v: k_hv_down writes the down-spin hybridisation into y, then
+// k_hv_async<SPLIT> adds the other terms (both on the context stream).
+template <typename TX, typename TA, typename TY, int R, int NT, int MINB, int WB>
+static int launch_batch_split(mo_ed_ctx *ctx, const HvBatch<TA> &b0)
+{
+    if (b0.total_items <= 0) return MO_ED_OK;
+    HvBatch<TA> b = b0;
+    int tiles = 0, maxrows = 0, maxmv = 0;
+    for (int i = 0; i < b.njobs; ++i) {
+        HvJobT<TA> &j = b.job[i];
+        if (!j.dblk_ptr || !j.dblk_chunks || j.dblk_n < 1 || j.ld % 32 != 0)
+            return fail(ctx, MO_ED_ERR_STATE, "H*v down-spin block tables missing");
+        j.tile0 = tiles;
+        tiles += j.ntiles;
+        maxrows = std::max(maxrows, j.dblk_max);
+        maxmv = std::max(maxmv, j.dblk_mvmax);
+    }
+    size_t smem = 0;
+    int dbuf = 1;
+    DownLayout L = down_layout(maxrows, maxmv, WB, 2, sizeof(HopEnt<TA>), &smem);
+    if (smem > kDownSmemMax) {
+        dbuf = 0;
+        L = down_layout(maxrows, maxmv, WB, 1, sizeof(HopEnt<TA>), &smem);
+    }
+    if (smem > kDownSmemMax) return fail(ctx, MO_ED_ERR_ARG, "down-spin blocks too large for the split H*v");
+    auto kd = k_hv_down<TX, TA, TY, kDownNT, WB>;
+    MOED_CUDA(ctx, cudaFuncSetAttribute(kd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MOED_CUDA(ctx, cudaFuncSetAttribute(kd, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    int per_sm = 0;
+    MOED_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kd, kDownNT, smem));
+    if (per_sm < 1) return fail(ctx, MO_ED_ERR_ARG, "down-spin blocks too large for the split H*v");
+    const int grid = std::min(tiles, ctx->num_sms * per_sm);
+    kd<<<grid, kDownNT, smem, ctx->stream>>>(b, tiles, L, maxrows, dbuf);
+    MOED_CHECK_LAUNCH(ctx);
+    return launch_batch_async<TX, TA, TY, R, NT, MINB, true>(ctx, b);
+}
+
+// Whether the split kernel fits every down-spin block of the model (any
+// electron count: at most dblk_bound rows and dblk_mv_bound moves).
+static bool split_fits(const mo_ed_ctx *ctx, size_t wb, size_t ent_bytes)
+{
+    size_t smem = 0;
+    down_layout(ctx->dblk_bound, ctx->dblk_mv_bound, wb, 1, ent_bytes, &smem);
+    return smem <= kDownSmemMax;
 }
 
 template <typename TA, int R>
@@ -1129,7 +1409,10 @@ static int launch_variant(mo_ed_ctx *ctx, int kind, int v, const HvBatch<TA> &b)
         case 5: return launch_batch_async<float, float, float, 4, 512>(ctx, b);
         case 6: return launch_batch_async<float, float, float, 3, 512>(ctx, b);
         case 7: return launch_batch_async<float, float, float, 2, 512, 2>(ctx, b);
-        default: return launch_batch_async<float, float, float, 2, 256, 2>(ctx, b);
+        case 8: return launch_batch_async<float, float, float, 2, 256, 2>(ctx, b);
+        case 9: return launch_batch_split<float, float, float, 3, 512, 1, 128>(ctx, b);
+        case 10: return launch_batch_split<float, float, float, 4, 512, 1, 128>(ctx, b);
+        default: return launch_batch_split<float, float, float, 3, 512, 1, 64>(ctx, b);
         }
     } else if (kind == HV_F64) {
         switch (v) {
@@ -1137,7 +1420,9 @@ static int launch_variant(mo_ed_ctx *ctx, int kind, int v, const HvBatch<TA> &b)
         case 1: return launch_batch<double, double, double, 3, 256, 1>(ctx, b);
         case 2: return launch_batch<double, double, double, 2, 512, 1>(ctx, b);
         case 3: return launch_batch_async<double, double, double, 2, 512>(ctx, b);
-        default: return launch_batch_async<double, double, double, 4, 512>(ctx, b);
+        case 4: return launch_batch_async<double, double, double, 4, 512>(ctx, b);
+        case 5: return launch_batch_split<double, double, double, 2, 512, 1, 128>(ctx, b);
+        default: return launch_batch_split<double, double, double, 2, 512, 1, 64>(ctx, b);
         }
     } else {
         switch (v) {
@@ -1145,7 +1430,9 @@ static int launch_variant(mo_ed_ctx *ctx, int kind, int v, const HvBatch<TA> &b)
         case 1: return launch_batch<float, double, double, 3, 256, 1>(ctx, b);
         case 2: return launch_batch<float, double, double, 2, 512, 1>(ctx, b);
         case 3: return launch_batch_async<float, double, double, 2, 512>(ctx, b);
-        default: return launch_batch_async<float, double, double, 4, 512>(ctx, b);
+        case 4: return launch_batch_async<float, double, double, 4, 512>(ctx, b);
+        case 5: return launch_batch_split<float, double, double, 2, 512, 1, 128>(ctx, b);
+        default: return launch_batch_split<float, double, double, 2, 512, 1, 64>(ctx, b);
         }
     }
 }
@@ -1202,6 +1489,14 @@ static int prepare_variant(mo_ed_ctx *ctx, const Sector &s, int kind, int v)
     int n;
     if (int rc = species_items(ctx, s.dn, h.R, &items, &n)) return rc;
     if (!h.staged) return MO_ED_OK;
+    if (h.staged >= 2) {
+        // the split kernel stages whole down-spin blocks: the largest block of
+        // the model (any electron count) must fit one CTA's shared memory
+        const size_t wb = h.staged == 2 ? 128 : 64;
+        if (!split_fits(ctx, wb, kind == HV_F32 ? sizeof(HopEnt<float>) : sizeof(HopEnt<double>)))
+            return fail(ctx, MO_ED_ERR_ARG, "down-spin blocks too large for the split H*v");
+        if (int rc = species_dblocks(ctx, s.dn, s.ld())) return rc;
+    }
     if (int rc = species_sched(ctx, s.up, h.R)) return rc;
     return species_desc(ctx, s.dn, h.R, kind == HV_F32);
 }
@@ -1223,7 +1518,10 @@ static int tune(mo_ed_ctx *ctx, const Sector &s, int kind, int *best)
     std::vector<float> &times = ctx->hv_times[shape_key(kind, s)];
     times.assign(nvariants(kind), -1.0f);
     for (int v = 0; v < nvariants(kind); ++v) {
-        if (int rc = prepare_variant(ctx, s, kind, v)) return rc;
+        if (int rc = prepare_variant(ctx, s, kind, v)) {
+            if (rc == MO_ED_ERR_ARG) continue;   // variant not applicable to this model
+            return rc;
+        }
         if (launch_one(ctx, s, kind, v, dx.p, dy.p) != MO_ED_OK) {   // variant does not fit this sector
             cudaGetLastError();
             continue;
@@ -1307,6 +1605,7 @@ int hv_lookup(mo_ed_ctx *ctx, const Sector &s, int kind, int *v_out, int *R_out)
     bool ready = s.dn->items.count(R) != 0;
     if (h.staged)
         ready = ready && s.up->sched_rf.count(R) && s.dn->desc.count(R * 2 + (kind == HV_F32 ? 0 : 1));
+    if (h.staged >= 2) ready = ready && s.dn->dblk_ptr != nullptr && s.dn->dblk_chunks.count(s.ld());
     if (!ready) return fail(ctx, MO_ED_ERR_STATE, "H*v item table of this sector not built yet");
     if (v_out) *v_out = it->second;
     if (R_out) *R_out = R;

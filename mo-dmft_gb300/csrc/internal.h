@@ -114,6 +114,20 @@ struct Species {
     // per-item descriptors of the staged H*v kernel, key R*2 + (FP64 ? 1 : 0)
     std::map<int, unsigned *> desc;
     std::map<int, int> nitems;
+    // down-spin blocks of the split H*v: rows with equal electron counts in
+    // every conserved subsystem, closed under hybridisation moves.  Positions
+    // p run over the rows block by block (largest block first).
+    int dblk_n = 0, dblk_max = 0, dblk_mvmax = 0;  // blocks, largest block, most moves in a block
+    int *dblk_off = nullptr;      // [dblk_n + 1] first position of each block
+    int *dblk_rows = nullptr;     // [n] row (rank) at position p
+    int *dblk_ptr = nullptr;      // [n + 1] first move of position p
+    // moves of each position: {target index within the block, signed coupling}
+    HopEnt<float> *dblk_mv_f = nullptr;
+    HopEnt<double> *dblk_mv_d = nullptr;
+    // per row stride ld: {first chunk, 32-column units per chunk} of each block
+    std::map<int, int2 *> dblk_chunks;
+    std::map<int, int> dblk_nchunks;
+    std::vector<int> dblk_h_off;  // host copy of dblk_off
     ~Species();
 };
 
@@ -150,6 +164,12 @@ struct HvJobT {
     const unsigned *up_sched_ent;
     const HopEnt<TA> *up_sched;
     const unsigned *desc;          // per-item descriptors (staged kernel)
+    // down-spin blocks of the split kernel (Species::dblk_*)
+    const int *dblk_off, *dblk_rows, *dblk_ptr;
+    const HopEnt<TA> *dblk_mv;
+    const int2 *dblk_chunks;
+    int dblk_n, dblk_max, dblk_mvmax;
+    int tile0, ntiles;             // this job's chunks in the batch (split kernel)
 };
 
 // ---------------------------------------------------------------------------
@@ -217,6 +237,8 @@ struct mo_ed_ctx {
     std::vector<int> cpl_orb, cpl_bath;  // nonzero couplings in reference loop order
     std::vector<double> cpl_val;
     std::vector<int> site_subsys;  // conserved subsystem (orbital + coupled bath levels) of each site
+    int dblk_bound = 0;            // largest down-spin block over every electron count
+    int dblk_mv_bound = 0;         // most hybridisation moves in one such block
     std::map<int, std::unique_ptr<moed::Species>> species;  // by N
 
     // statistics of the last eigensolve (mo_ed_diag_stats)
@@ -304,6 +326,9 @@ int hv_tuning(mo_ed_ctx *ctx, const Sector &s, int kind, int cap, int *nvar, int
 int hv_prepare_rows(mo_ed_ctx *ctx, const Sector &s, int kind, int v);
 // Per-R stage offsets of the up-spin gather schedule (built once per R).
 int species_sched(mo_ed_ctx *ctx, Species *sp, int R);
+// Down-spin block tables of a species (split H*v), built once; chunk table
+// for row stride ld.
+int species_dblocks(mo_ed_ctx *ctx, Species *sp, int ld);
 // Lookup only: the tile shape and item table that hv_prepare left for this
 // sector and kind, or MO_ED_ERR_STATE if it never ran (never tunes or allocates).
 int hv_lookup(mo_ed_ctx *ctx, const Sector &s, int kind, int *v, int *R);

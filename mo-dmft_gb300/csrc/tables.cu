@@ -56,6 +56,12 @@ Species::~Species()
     for (auto &kv : sched_rd) cudaFree(kv.second);
     for (auto &kv : items) cudaFree(kv.second);
     for (auto &kv : desc) cudaFree(kv.second);
+    cudaFree(dblk_off);
+    cudaFree(dblk_rows);
+    cudaFree(dblk_ptr);
+    cudaFree(dblk_mv_f);
+    cudaFree(dblk_mv_d);
+    for (auto &kv : dblk_chunks) cudaFree(kv.second);
 }
 
 // ---------------------------------------------------------------------------
@@ -331,6 +337,30 @@ int build_model(mo_ed_ctx *ctx)
             if (id[r] < 0) id[r] = nsub++;
             ctx->site_subsys[i] = id[r];
         }
+        // largest down-spin block and most hybridisation moves in one block,
+        // over every electron count (all 2^nsite words, nsite <= 15)
+        std::map<unsigned long long, std::pair<long long, long long>> blk;
+        for (unsigned w = 0; w < (1u << m.nsite); ++w) {
+            unsigned long long key = (unsigned long long)__builtin_popcount(w);
+            for (int sub = 0; sub < nsub; ++sub) {
+                int c = 0;
+                for (int i = 0; i < m.nsite; ++i)
+                    if (((w >> i) & 1) && ctx->site_subsys[i] == sub) ++c;
+                key = key * 32 + (unsigned)c;
+            }
+            int mv = 0;
+            for (int i = 0; i < m.ncpl; ++i)
+                mv += (int)(((w >> ctx->cpl_orb[i]) & 1) != ((w >> ctx->cpl_bath[i]) & 1));
+            auto &e = blk[key];
+            e.first += 1;
+            e.second += mv;
+        }
+        ctx->dblk_bound = 0;
+        ctx->dblk_mv_bound = 0;
+        for (const auto &kv : blk) {
+            ctx->dblk_bound = (int)std::max<long long>(ctx->dblk_bound, kv.second.first);
+            ctx->dblk_mv_bound = (int)std::max<long long>(ctx->dblk_mv_bound, kv.second.second);
+        }
     }
     if (!ctx->d_mdl) MOED_CUDA(ctx, cudaMalloc(&ctx->d_mdl, sizeof(ModelDev)));
     MOED_CUDA(ctx, cudaMemcpyAsync(ctx->d_mdl, &m, sizeof(m), cudaMemcpyHostToDevice, ctx->stream));
@@ -403,6 +433,119 @@ int species_items(mo_ed_ctx *ctx, Species *sp, int R, const int **items, int *ni
     sp->nitems[R] = n_items;
     *items = d;
     *nitems = n_items;
+    return MO_ED_OK;
+}
+
+// Down-spin blocks of a species for the split H*v.  Rows (words, rank order)
+// are keyed by their electron count in every conserved subsystem; a
+// hybridisation move stays inside its subsystem, so every block is closed
+// under the moves and a block times a column range is an independent chunk.
+// Moves are copied from the species' move tables with their targets rewritten
+// as indices within the block.  Chunks: a block's columns are cut into ranges of about
+// kChunkElems elements (whole 32-column units), so the chunks of a sector do
+// similar work whatever the block sizes.
+int species_dblocks(mo_ed_ctx *ctx, Species *sp, int ld)
+{
+    constexpr long long kChunkElems = 1 << 16;
+    if (!sp->dblk_ptr) {
+        const int n = sp->n, hw = sp->hw, nsite = sp->nsite, N = sp->N;
+        int nsub = 0;
+        for (int v : ctx->site_subsys) nsub = std::max(nsub, v + 1);
+        std::vector<int> cnt(n), tgt((size_t)hw * n);
+        std::vector<double> val((size_t)hw * n);
+        MOED_CUDA(ctx, cudaMemcpyAsync(cnt.data(), sp->hop_cnt, sizeof(int) * n, cudaMemcpyDeviceToHost, ctx->stream));
+        MOED_CUDA(ctx, cudaMemcpyAsync(tgt.data(), sp->hop_tgt, sizeof(int) * tgt.size(), cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+        MOED_CUDA(ctx, cudaMemcpyAsync(val.data(), sp->hop_val_d, sizeof(double) * val.size(),
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+        MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        // block key of every rank (words in increasing numeric order = rank order)
+        std::map<unsigned long long, std::vector<int>> blocks;
+        int r = 0;
+        for (unsigned w = 0; w < (1u << nsite); ++w) {
+            if (__builtin_popcount(w) != N) continue;
+            unsigned long long k = 0;
+            for (int sub = 0; sub < nsub; ++sub) {
+                int c = 0;
+                for (int i = 0; i < nsite; ++i)
+                    if (((w >> i) & 1) && ctx->site_subsys[i] == sub) ++c;
+                k = k * 32 + (unsigned)c;
+            }
+            blocks[k].push_back(r++);
+        }
+        std::vector<const std::vector<int> *> order;
+        for (auto &kv : blocks) order.push_back(&kv.second);
+        std::stable_sort(order.begin(), order.end(),
+                         [](const std::vector<int> *a, const std::vector<int> *b) { return a->size() > b->size(); });
+        std::vector<int> local(n, -1), blk(n, -1);
+        for (size_t b = 0; b < order.size(); ++b)
+            for (size_t i = 0; i < order[b]->size(); ++i) {
+                local[(*order[b])[i]] = (int)i;
+                blk[(*order[b])[i]] = (int)b;
+            }
+        std::vector<int> off(1, 0), rows, ptr(1, 0);
+        std::vector<HopEnt<float>> mvf;
+        std::vector<HopEnt<double>> mvd;
+        int maxrows = 0, mvmax = 0;
+        for (size_t b = 0; b < order.size(); ++b) {
+            const size_t m0 = mvf.size();
+            for (int row : *order[b]) {
+                rows.push_back(row);
+                for (int s = 0; s < cnt[row]; ++s) {
+                    const int tr = tgt[(size_t)s * n + row];
+                    if (tr < 0 || tr >= n || blk[tr] != (int)b)
+                        return fail(ctx, MO_ED_ERR_STATE, "down-spin move leaves its conserved block");
+                    const double v = val[(size_t)s * n + row];
+                    HopEnt<float> ef;
+                    ef.t = local[tr];
+                    ef.v = (float)v;
+                    HopEnt<double> ed;
+                    ed.t = local[tr];
+                    ed.pad = 0;
+                    ed.v = v;
+                    mvf.push_back(ef);
+                    mvd.push_back(ed);
+                }
+                ptr.push_back((int)mvf.size());
+            }
+            off.push_back((int)rows.size());
+            maxrows = std::max(maxrows, (int)order[b]->size());
+            mvmax = std::max(mvmax, (int)(mvf.size() - m0));
+        }
+        auto up = [&](auto **dst, const auto &v) -> int {
+            using E = std::remove_const_t<std::remove_reference_t<decltype(v[0])>>;
+            MOED_CUDA(ctx, cudaMalloc((void **)dst, sizeof(E) * std::max<size_t>(1, v.size())));
+            MOED_CUDA(ctx, cudaMemcpyAsync((void *)*dst, v.data(), sizeof(E) * v.size(), cudaMemcpyHostToDevice,
+                                           ctx->stream));
+            return MO_ED_OK;
+        };
+        if (int rc = up(&sp->dblk_off, off)) return rc;
+        if (int rc = up(&sp->dblk_rows, rows)) return rc;
+        if (int rc = up(&sp->dblk_mv_f, mvf)) return rc;
+        if (int rc = up(&sp->dblk_mv_d, mvd)) return rc;
+        if (int rc = up(&sp->dblk_ptr, ptr)) return rc;   // last: marks the tables complete
+        MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        sp->dblk_n = (int)order.size();
+        sp->dblk_max = maxrows;
+        sp->dblk_mvmax = mvmax;
+        sp->dblk_h_off = off;
+    }
+    if (sp->dblk_chunks.count(ld)) return MO_ED_OK;
+    const int units = ld / 32;
+    std::vector<int2> ch(sp->dblk_n);
+    int total = 0;
+    for (int b = 0; b < sp->dblk_n; ++b) {
+        const long long nr = sp->dblk_h_off[b + 1] - sp->dblk_h_off[b];
+        const int per = (int)std::max(1LL, std::min<long long>(units, kChunkElems / (32 * nr)));
+        ch[b] = make_int2(total, per);
+        total += (units + per - 1) / per;
+    }
+    int2 *d = nullptr;
+    MOED_CUDA(ctx, cudaMalloc(&d, sizeof(int2) * std::max<size_t>(1, ch.size())));
+    MOED_CUDA(ctx, cudaMemcpyAsync(d, ch.data(), sizeof(int2) * ch.size(), cudaMemcpyHostToDevice, ctx->stream));
+    MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    sp->dblk_chunks[ld] = d;
+    sp->dblk_nchunks[ld] = total;
     return MO_ED_OK;
 }
 

@@ -297,7 +297,8 @@ class EDSolver:
         self._chk(lib().mo_ed_hv_set_variant(self._ctx, ne_up, ne_down, dtype, variant))
 
     def hv_tuning(self, ne_up, ne_down, dtype=FP32):
-        """Autotuner record: list of ((R, threads, CTAs/SM, staged), ms) and the chosen index."""
+        """Autotuner record: list of ((R, threads, CTAs/SM, kernel), ms) and the chosen index;
+        kernel 0 k_hv, 1 k_hv_async, 2 / 3 split (k_hv_down on 128- / 64-byte slices + k_hv_async)."""
         cap = 16
         nv, ch = C.c_int(), C.c_int()
         shape = np.zeros(4 * cap, np.int32)

@@ -122,8 +122,11 @@ def test_multiply_h_fp32(setup, oracle, name):
 @pytest.mark.parametrize("name", ["3x6_block", "4x4_mixed", "5x2_dense"])
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-13), ("fp32", 2e-6)])
 def test_multiply_h_every_variant(setup, oracle, pkg, name, precision, tol):
-    """Each tile-shape variant (k_hv and the double-buffered staged k_hv_async), pinned
-    in turn, against the oracle on several sectors."""
+    """Each tile-shape variant (k_hv, the double-buffered staged k_hv_async and the
+    split k_hv_down + k_hv_async), pinned in turn, against the oracle on several
+    sectors.  The split variants need every down-spin block of the model in one
+    CTA's shared memory: the dense-V model has one block per sector and rejects
+    them with MO_ED_ERR_ARG."""
     s, m = setup(name, precision=precision)
     dt = pkg.FP32 if precision == "fp32" else pkg.FP64
     ns = m.nsite
@@ -135,7 +138,7 @@ def test_multiply_h_every_variant(setup, oracle, pkg, name, precision, tol):
             x = x.astype(np.float32)
         ref = oracle.multiply_H(m, b, x.astype(np.float64))
         variants, _ = s.hv_tuning(nu, nd, dt)
-        ran, staged = 0, 0
+        ran, staged, split = 0, 0, 0
         for v, (shape, ms) in enumerate(variants):
             try:
                 s.hv_set_variant(nu, nd, v, dt)
@@ -144,9 +147,12 @@ def test_multiply_h_every_variant(setup, oracle, pkg, name, precision, tol):
                 assert e.code == 1, e       # MO_ED_ERR_ARG: the shape does not fit this sector
                 continue
             ran += 1
-            staged += shape[3]
+            staged += shape[3] == 1
+            split += shape[3] >= 2
             assert rel(y, ref) < tol, (name, nu, nd, v, shape)
         assert ran >= 2 and staged >= 1
+        if name == "3x6_block":
+            assert split >= 2
 
 
 def test_multiply_h_mixed(setup, oracle):
@@ -188,8 +194,9 @@ def test_multiply_h_symmetric_c3(setup, oracle):
 
 def test_multiply_h_c4_full_size(solver, pkg):
     """C4 ground sector at full size (D = 41,409,225): FP64 symmetry <x|Hy> =
-    <y|Hx>, linearity, and every FP32 tile-shape variant (staged and previous
-    kernel) against the FP64 product of the same FP32 input."""
+    <y|Hx>, linearity, and every FP32 tile-shape variant (previous, staged and
+    split kernels) against the FP64 product of the same FP32 input; the FP64
+    split variants against the FP64 product."""
     cfg = pkg.configs.config("C4")
     ek, vk = cfg.model()
     solver.set_options(precision="fp64")
@@ -206,14 +213,23 @@ def test_multiply_h_c4_full_size(solver, pkg):
     x32 = x.astype(np.float32)
     h64 = solver.multiply_H(nu, nd, x32.astype(np.float64))
     variants, chosen = solver.hv_tuning(nu, nd, pkg.FP32)
-    staged = 0
+    kinds = set()
     for v, (shape, ms) in enumerate(variants):
         if ms < 0:
             continue
         solver.hv_set_variant(nu, nd, v, pkg.FP32)
         assert rel(solver.multiply_H(nu, nd, x32), h64) < 2e-6, (v, shape)
-        staged += shape[3]
-    assert staged >= 1
+        kinds.add(shape[3])
+    assert kinds == {0, 1, 2, 3}
+    variants, chosen = solver.hv_tuning(nu, nd, pkg.FP64)
+    for v, (shape, ms) in enumerate(variants):
+        if shape[3] >= 2:
+            try:   # FP64 move lists and slices may not fit one CTA for C4's blocks
+                solver.hv_set_variant(nu, nd, v, pkg.FP64)
+            except pkg.EDError as e:
+                assert e.code == 1, e
+                continue
+            assert rel(solver.multiply_H(nu, nd, x), hx) < 1e-13, (v, shape)
 
 
 # ---------------------------------------------------------------- apply_c
