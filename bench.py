@@ -46,12 +46,13 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per launch of the H*v kernel from the committed ncu summary."""
+def profile_traffic(kind):
+    """DRAM bytes of one H*v with the given kernel kind (hv_tuning's fourth
+    field) from the committed ncu summary, or None."""
     p = os.path.join(ROOT, "profiles", "hv_c4_traffic.json")
     if os.path.exists(p):
         with open(p) as f:
-            return json.load(f)
+            return json.load(f).get("by_kind", {}).get(str(kind))
     return None
 
 
@@ -240,6 +241,8 @@ def run_ours(args):
     s = pkg.EDSolver(local, stream.cuda_stream)
     s.set_options(precision="fp32")
     s.set_model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
+    if args.hv_variant >= 0:
+        s.hv_set_variant(nup, ndn, args.hv_variant, pkg.FP32)
     nu_, nd_, D = s.sector_dims(nup, ndn)
     ld, nelem = s.vector_layout(nup, ndn)
     # device layout: nd rows of stride ld (128-byte aligned rows), zero pads
@@ -276,7 +279,6 @@ def run_ours(args):
     value = ws * bytes_step / (t_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
     achieved = bytes_step / (t_ms * 1e-3) / 1e9
-    traffic = profile_traffic()
 
     # end to end through the C-ABI with pinned host buffers
     xh = torch.empty(D, dtype=torch.float32, pin_memory=True)
@@ -305,6 +307,7 @@ def run_ours(args):
 
 
     tuning, chosen = s.hv_tuning(nup, ndn, pkg.FP32)
+    traffic = profile_traffic(tuning[chosen][0][3])
     lg = None
     fit = None
     if rank == 0 and not args.no_lanczos_g:
@@ -323,7 +326,7 @@ def run_ours(args):
                        "l2": "inputs larger than L2 (x and y 166 MB each)", "parallelism": f"replicas{ws}"},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                         "traffic": (traffic or {}).get("bytes_per_launch"),
+                         "traffic": (traffic or {}).get("bytes_per_hv"),
                          "traffic_note": (traffic or {}).get("note")},
             "cpu_baseline": cpu,
             "e2e": {"value": round(bytes_step / t_e2e / 1e9 * ws, 3), "unit": "GB/s",
@@ -396,6 +399,8 @@ def main():
     ap.add_argument("--no-fit", action="store_true")
     ap.add_argument("--lg-nev", type=int, default=6)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--hv-variant", type=int, default=-1,
+                    help="pin this H*v variant (index of the autotuner list) instead of tuning; for profiling")
     ap.add_argument("--lg-only", action="store_true",
                     help="only the Lanczos+G pipeline (one JSON object per configuration; for profiling)")
     ap.add_argument("--lg-precisions", default="fp32,fp32+g64,fp64",
