@@ -195,6 +195,44 @@ def lanczos_g(pkg, name, nev, precisions=("fp32", "fp32+g64", "fp64")):
     return out
 
 
+def dmft_bench(pkg, cpu=True):
+    """ed_delta_new at the reference's defaults (Nq = 10,000, 3 orbitals) on
+    C4's 4,096 w_n through the C-ABI (host arrays, copies included), next to
+    the oracle on one host core for a bounded w_n sample."""
+    cfg = pkg.configs.config("C4")
+    ek, vk = cfg.model()
+    s = pkg.EDSolver(0)
+    s.set_model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
+    nq, nw = 10000, cfg.nw
+    s.set_band_structure(nq)
+    rng = np.random.default_rng(9)
+    om = pkg.matsubara(nw, cfg.beta)
+    gr = 1.0 / (1j * om[None, :] + 0.3 * rng.standard_normal((cfg.norb, 1)))
+    dev = 0.2 * (rng.standard_normal((cfg.norb, nw)) + 1j * rng.standard_normal((cfg.norb, nw)))
+    s.delta_new(gr, dev, 1.0)
+    reps = 5
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        dn, gk = s.delta_new(gr, dev, 1.0)
+        s.n_from_gksum(gk, cfg.beta)
+    t_gpu = (time.perf_counter() - t0) / reps
+    s.close()
+    terms = cfg.norb * nw * nq
+    out = {"config": "C4 omega grid, Nq=10000", "norb": cfg.norb, "nw": nw, "nq": nq,
+           "gpu_ms": round(t_gpu * 1e3, 3), "gpu_terms_per_s": round(terms / t_gpu, 1)}
+    if cpu:
+        import __graft_entry__ as g
+        O = g.load_oracle()
+        hk, _ = O.set_band_structure(cfg.norb, nq)
+        ns = 64
+        t0 = time.perf_counter()
+        O.delta_new(hk, 1.0, gr[:, :ns], dev[:, :ns])
+        t_cpu = (time.perf_counter() - t0) * nw / ns
+        out["cpu_ms_full_estimate"] = round(t_cpu * 1e3, 1)
+        out["cpu_sample"] = f"oracle delta_new (C port, 1 core) on {ns} of {nw} w_n, scaled"
+    return out
+
+
 def fit_bench(pkg, cpu_fits=2):
     """C5: 256 random starts of the chi^2 bath fit in one lockstep batch (FP64
     adjoint gradient on the device), next to the oracle's frprmn on one host
@@ -314,6 +352,7 @@ def run_ours(args):
         lg = {c: lanczos_g(pkg, c, args.lg_nev, tuple(args.lg_precisions.split(","))) for c in args.lg_config.split(",") if c}
     if rank == 0 and not args.no_fit:
         fit = fit_bench(pkg, 0 if args.no_cpu else 2)
+    dmft = dmft_bench(pkg, not args.no_cpu) if rank == 0 and not args.no_fit else None
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         cpu = cpu_baseline_sample(cfg, nup, ndn)
@@ -339,6 +378,7 @@ def run_ours(args):
             "clocks": clocks,
             "lanczos_g": lg,
             "fit": fit,
+            "dmft_delta_new": dmft,
         }
         print(json.dumps(line), flush=True)
     s.close()

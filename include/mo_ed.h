@@ -225,9 +225,35 @@ int mo_ed_calc_green_ftn(mo_ed_ctx *ctx, double *Gr);
 /* The continued-fraction coefficients of the last mo_ed_calc_green_ftn, in
  * the order the reference writes apbpanbn.dat (ed_green.F90:112-115,
  * 125-128): for record r, nstep_calc[2r] (particle) and nstep_calc[2r+1]
- * (hole), coefficients ab[r][4][nstep+1] = ap, bp, an, bn.  *nrec receives
- * the record count; ab / nstep_calc may be NULL to query it. */
+ * (hole), coefficients ab[r][4][nstep+1] = ap, bp, an, bn.  nstep_calc = -1
+ * marks a run whose excitation leaves the Fock space (c+ on a full or c on an
+ * empty spin species): it adds nothing to G or A.  *nrec receives the record
+ * count; ab / nstep_calc may be NULL to query it. */
 int mo_ed_green_coeffs(mo_ed_ctx *ctx, int *nrec, int *nstep_calc, double *ab, int capacity);
+
+/* ---- DMFT self-consistency (ed_hamiltonian.F90:29-85, ed_green.F90:187-253) -- */
+/* ed_set_band_structure: the square-lattice band Hk(i,i,k) = -0.5 (cos kx +
+ * cos ky) on a sqrt(Nq) x sqrt(Nq) grid, kept on the device for
+ * mo_ed_delta_new; ef(norb) = its k-average (the reference also copies ef
+ * into ek(1:norb)).  Nq must be a perfect square (the reference stops). */
+int mo_ed_set_band_structure(mo_ed_ctx *ctx, int nq, double *ef);
+/* ed_delta_new: for every orbital and w_n, Gksum = (1/Nq) sum_k 1 / (1/Gr +
+ * D_ev + mu - Hk(k)) and D_ev <- 1/Gr - 1/Gksum + D_ev.  Gr, D_ev (in/out)
+ * and Gksum (out, may be NULL) are complex (norb, nwloc), interleaved re/im. */
+int mo_ed_delta_new(mo_ed_ctx *ctx, int nwloc, double rmu, const double *Gr, double *D_ev,
+                    double *Gksum);
+/* n_from_gksum: nocc(iorb) = 2 sum_w Re Gksum(iorb, w) / beta + 0.5. */
+int mo_ed_n_from_gksum(mo_ed_ctx *ctx, int nw, const double *Gksum, double beta, double *nocc);
+
+/* ---- real-frequency spectral function (dos.f90:1-106) ------------------------ */
+/* A(iorb, w) = -Im(G+ + G-) / pi from the records of the last
+ * mo_ed_calc_green_ftn (the apbpanbn.dat content), z+ = CMPLX(E + w, small),
+ * z- = CMPLX(w - E, small) (default-REAL rounding with fortran_cmplx).
+ * weighted = 0: as dos_diag, each record assigns A(iorb, :), so the last
+ * record of an orbital sets it; weighted = 1: sum of pev * factor * A over
+ * the records.  omega_real(nw); Aff real (norb, nw). */
+int mo_ed_dos(mo_ed_ctx *ctx, int nw, const double *omega_real, double small, int weighted,
+              double *Aff);
 
 /* ---- a18-a22: bath fit (func.f90, frprmn.f90, ed_green.F90:260-273) ------ */
 /* FUNC (func.f90:1-45): chi^2 at x(nxsize); D_ev (norb, nwloc) complex. */

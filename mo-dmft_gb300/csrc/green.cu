@@ -220,6 +220,125 @@ __global__ void k_green_cf(const CfRec *__restrict__ rec, int nrec, const double
 }
 
 // ---------------------------------------------------------------------------
+// real-frequency spectral function (dos.f90:1-106)
+// ---------------------------------------------------------------------------
+// One thread per (iorb, w).  z+ = CMPLX(E + w, small), z- = CMPLX(w - E,
+// small) (default-REAL rounding with fcmplx), A = -Im(G+ + G-) / pi.  As
+// dos_diag assigns A(iorb, :) for every record, the last record of each
+// orbital sets it (weighted = 0); weighted = 1 sums pev * factor * A over the
+// records instead.  Runs that leave the Fock space (np / nn < 0) add nothing.
+__global__ void k_dos(const CfRec *__restrict__ rec, int nrec, const double *__restrict__ ab, int ld,
+                      const double *__restrict__ omega, int nw, int norb, double small, int fcmplx, int weighted,
+                      double *__restrict__ aff)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nw * norb) return;
+    const int iw = t / norb, iorb = t - iw * norb;
+    const double pi = 3.14159265358979323846;
+    const double w = omega[iw];
+    const double sm = fcmplx ? (double)(float)small : small;
+    double out = 0.0;
+    for (int r = weighted ? 0 : nrec - 1; weighted ? r < nrec : r >= 0; r += weighted ? 1 : -1) {
+        const CfRec R = rec[r];
+        if (R.iorb != iorb) continue;
+        const double *ap = ab + (size_t)r * 4 * ld, *bp = ap + ld, *an = bp + ld, *bn = an + ld;
+        double gim = 0.0;
+        if (R.np >= 0) {
+            const double zr = fcmplx ? (double)(float)(R.E + w) : R.E + w;
+            double2 g = cdiv(make_double2(bp[R.np], 0.0), make_double2(zr - ap[R.np], sm));
+            for (int j = R.np - 1; j >= 0; --j)
+                g = cdiv(make_double2(bp[j], 0.0), make_double2(zr - ap[j] - g.x, sm - g.y));
+            gim += g.y;
+        }
+        if (R.nn >= 0) {
+            const double zr = fcmplx ? (double)(float)(w - R.E) : w - R.E;
+            double2 g = cdiv(make_double2(bn[R.nn], 0.0), make_double2(zr + an[R.nn], sm));
+            for (int j = R.nn - 1; j >= 0; --j)
+                g = cdiv(make_double2(bn[j], 0.0), make_double2(zr + an[j] - g.x, sm - g.y));
+            gim += g.y;
+        }
+        const double a = -gim / pi;
+        if (!weighted) {
+            out = a;
+            break;
+        }
+        out += R.weight * a;
+    }
+    aff[(size_t)iw * norb + iorb] = out;
+}
+
+// ---------------------------------------------------------------------------
+// DMFT self-consistency (ed_hamiltonian.F90:29-85, ed_green.F90:187-253)
+// ---------------------------------------------------------------------------
+// Square-lattice band: Hk(i,i,ik) = -0.5 (cos kx + cos ky), the same for every
+// orbital, kx = dq * (i-1) outer, ky = dq * (j-1) inner.
+__global__ void k_band(int nk, double dq, double *hk)
+{
+    const int ik = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ik >= nk * nk) return;
+    const int i = ik / nk, j = ik - i * nk;
+    hk[ik] = -0.5 * (cos(dq * (double)(float)i) + cos(dq * (double)(float)j));
+}
+
+// ef = sum_k Hk / float(Nq), summed in k order (one thread, Nq terms)
+__global__ void k_band_mean(const double *hk, int nq, double *ef)
+{
+    double s = 0.0;
+    for (int k = 0; k < nq; ++k) s += hk[k];
+    ef[0] = s / (double)(float)nq;
+}
+
+// ed_delta_new: one warp per (iorb, w_n).  Its lanes sum 1 / ((1/Gr + D_ev +
+// mu) - Hk(q)) over strided q, a xor butterfly adds the lanes (every lane
+// ends with the same sum, in a fixed order), then Gksum = sum / float(Nq) and
+// D_ev <- 1/Gr - 1/Gksum + D_ev.  Complex divisions by Smith's algorithm.
+__global__ void k_delta_new(const double *__restrict__ hk, int nq, double rmu, const double *__restrict__ gr,
+                            double *__restrict__ dev, double *__restrict__ gksum, int n)
+{
+    const int wid = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (wid >= n) return;
+    const double2 g = make_double2(gr[2 * wid], gr[2 * wid + 1]);
+    const double2 d = make_double2(dev[2 * wid], dev[2 * wid + 1]);
+    const double2 gi = cdiv(make_double2(1.0, 0.0), g);
+    const double br = gi.x + d.x + rmu, bi = gi.y + d.y;
+    double sre = 0.0, sim = 0.0;
+    for (int q = lane; q < nq; q += 32) {
+        const double2 r = cdiv(make_double2(1.0, 0.0), make_double2(br - __ldg(hk + q), bi));
+        sre += r.x;
+        sim += r.y;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        sre += __shfl_xor_sync(0xffffffffu, sre, off);
+        sim += __shfl_xor_sync(0xffffffffu, sim, off);
+    }
+    if (lane == 0) {
+        const double fq = (double)(float)nq;
+        const double2 gk = make_double2(sre / fq, sim / fq);
+        const double2 gki = cdiv(make_double2(1.0, 0.0), gk);
+        gksum[2 * wid] = gk.x;
+        gksum[2 * wid + 1] = gk.y;
+        dev[2 * wid] = gi.x - gki.x + d.x;
+        dev[2 * wid + 1] = gi.y - gki.y + d.y;
+    }
+}
+
+// n_from_gksum: one CTA per orbital, nocc = 2 sum_w Re Gksum / beta + 0.5
+__global__ void k_nocc(const double *__restrict__ gksum, int nw, int norb, double beta, double *__restrict__ nocc)
+{
+    __shared__ double red[256];
+    const int iorb = blockIdx.x;
+    double s = 0.0;
+    for (int iw = threadIdx.x; iw < nw; iw += blockDim.x) s += gksum[2 * ((size_t)iw * norb + iorb)];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) nocc[iorb] = 2.0 * red[0] / beta + 0.5;
+}
+
+// ---------------------------------------------------------------------------
 // ed_calc_green_ftn
 // ---------------------------------------------------------------------------
 int calc_green(mo_ed_ctx *ctx, double *Gr)
@@ -346,13 +465,13 @@ int calc_green(mo_ed_ctx *ctx, double *Gr)
         }
         g.bp[0] = nsq;
         g.bn[0] = 1.0 - nsq;
-        g.np = ep.ok ? nsc[2 * r] : 0;
-        g.nn = en.ok ? nsc[2 * r + 1] : 0;
+        g.np = ep.ok ? nsc[2 * r] : -1;
+        g.nn = en.ok ? nsc[2 * r + 1] : -1;
         const StateVec &st = ctx->states[ep.iev];
         const int nu = ctx->nup[st.sector], nd = ctx->nelec[st.sector] - nu;
         cf[r].iorb = g.iorb - 1;
-        cf[r].np = ep.ok ? g.np : -1;
-        cf[r].nn = en.ok ? g.nn : -1;
+        cf[r].np = g.np;
+        cf[r].nn = g.nn;
         cf[r].E = st.val;
         cf[r].weight = st.prob * (nd == nu ? 1.0 : 0.5);
         std::copy(g.ap.begin(), g.ap.end(), ab.begin() + (r * 4 + 0) * ld);
@@ -417,6 +536,113 @@ int mo_ed_diag(mo_ed_ctx *ctx, int ne_up, int ne_down, int nev, double *eigval, 
             MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         }
     }
+    return MO_ED_OK;
+}
+
+int mo_ed_set_band_structure(mo_ed_ctx *ctx, int nq, double *ef)
+{
+    if (!ctx) return MO_ED_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (!ctx->have_model) return fail(ctx, MO_ED_ERR_STATE, "model not set");
+    if (nq < 1 || !ef) return fail(ctx, MO_ED_ERR_ARG, "bad arguments");
+    const int nk = (int)std::sqrt((double)nq);
+    if (nk * nk != nq) return fail(ctx, MO_ED_ERR_ARG, "Nq is not a square (ed_hamiltonian.F90:50 stops)");
+    if (int rc = dev_alloc(ctx, ctx->d_hk, sizeof(double) * ((size_t)nq + 1))) return rc;
+    ctx->nq = nq;
+    const double pi = 4.0 * std::atan(1.0);
+    const double dq = 2.0 * pi / (double)(float)nk;
+    double *hk = (double *)ctx->d_hk.p;
+    k_band<<<(nq + 255) / 256, 256, 0, ctx->stream>>>(nk, dq, hk);
+    MOED_CHECK_LAUNCH(ctx);
+    k_band_mean<<<1, 1, 0, ctx->stream>>>(hk, nq, hk + nq);
+    MOED_CHECK_LAUNCH(ctx);
+    double m = 0.0;
+    MOED_CUDA(ctx, cudaMemcpyAsync(&m, hk + nq, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int i = 0; i < ctx->norb; ++i) ef[i] = m;
+    return MO_ED_OK;
+}
+
+int mo_ed_delta_new(mo_ed_ctx *ctx, int nwloc, double rmu, const double *Gr, double *D_ev, double *Gksum)
+{
+    if (!ctx) return MO_ED_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (!ctx->have_model || !ctx->d_hk.p) return fail(ctx, MO_ED_ERR_STATE, "model or band structure not set");
+    if (nwloc < 1 || !Gr || !D_ev) return fail(ctx, MO_ED_ERR_ARG, "bad arguments");
+    const int n = ctx->norb * nwloc;
+    const size_t b = sizeof(double) * 2 * (size_t)n;
+    DevBuf dg, dd, dk;
+    if (int rc = dev_alloc(ctx, dg, b)) return rc;
+    if (int rc = dev_alloc(ctx, dd, b)) return rc;
+    if (int rc = dev_alloc(ctx, dk, b)) return rc;
+    MOED_CUDA(ctx, cudaMemcpyAsync(dg.p, Gr, b, cudaMemcpyHostToDevice, ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpyAsync(dd.p, D_ev, b, cudaMemcpyHostToDevice, ctx->stream));
+    const int T = 256;
+    k_delta_new<<<(unsigned)(((long long)n * 32 + T - 1) / T), T, 0, ctx->stream>>>(
+        (const double *)ctx->d_hk.p, ctx->nq, rmu, (const double *)dg.p, (double *)dd.p, (double *)dk.p, n);
+    MOED_CHECK_LAUNCH(ctx);
+    MOED_CUDA(ctx, cudaMemcpyAsync(D_ev, dd.p, b, cudaMemcpyDeviceToHost, ctx->stream));
+    if (Gksum) MOED_CUDA(ctx, cudaMemcpyAsync(Gksum, dk.p, b, cudaMemcpyDeviceToHost, ctx->stream));
+    MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return MO_ED_OK;
+}
+
+int mo_ed_n_from_gksum(mo_ed_ctx *ctx, int nw, const double *Gksum, double beta, double *nocc)
+{
+    if (!ctx) return MO_ED_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (!ctx->have_model) return fail(ctx, MO_ED_ERR_STATE, "model not set");
+    if (nw < 1 || !Gksum || !nocc || !(beta > 0)) return fail(ctx, MO_ED_ERR_ARG, "bad arguments");
+    const size_t b = sizeof(double) * 2 * (size_t)nw * ctx->norb;
+    DevBuf dk, dn;
+    if (int rc = dev_alloc(ctx, dk, b)) return rc;
+    if (int rc = dev_alloc(ctx, dn, sizeof(double) * ctx->norb)) return rc;
+    MOED_CUDA(ctx, cudaMemcpyAsync(dk.p, Gksum, b, cudaMemcpyHostToDevice, ctx->stream));
+    k_nocc<<<ctx->norb, 256, 0, ctx->stream>>>((const double *)dk.p, nw, ctx->norb, beta, (double *)dn.p);
+    MOED_CHECK_LAUNCH(ctx);
+    MOED_CUDA(ctx, cudaMemcpyAsync(nocc, dn.p, sizeof(double) * ctx->norb, cudaMemcpyDeviceToHost, ctx->stream));
+    MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return MO_ED_OK;
+}
+
+int mo_ed_dos(mo_ed_ctx *ctx, int nw, const double *omega_real, double small, int weighted, double *Aff)
+{
+    if (!ctx) return MO_ED_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->green.empty()) return fail(ctx, MO_ED_ERR_STATE, "mo_ed_calc_green_ftn has not been run");
+    if (nw < 1 || !omega_real || !Aff || (weighted != 0 && weighted != 1))
+        return fail(ctx, MO_ED_ERR_ARG, "bad arguments");
+    const int norb = ctx->norb, ld = ctx->opt.nstep + 1;
+    const size_t nrec = ctx->green.size();
+    std::vector<CfRec> cf(nrec);
+    std::vector<double> ab(nrec * 4 * (size_t)ld, 0.0);
+    for (size_t r = 0; r < nrec; ++r) {
+        const GreenRecord &g = ctx->green[r];
+        cf[r].iorb = g.iorb - 1;
+        cf[r].np = g.np;
+        cf[r].nn = g.nn;
+        cf[r].E = g.val;
+        cf[r].weight = g.prob * (g.even ? 1.0 : 0.5);
+        const std::vector<double> *src[4] = {&g.ap, &g.bp, &g.an, &g.bn};
+        for (int k = 0; k < 4; ++k)
+            std::copy(src[k]->begin(), src[k]->begin() + std::min<size_t>(ld, src[k]->size()),
+                      ab.begin() + (r * 4 + k) * ld);
+    }
+    DevBuf drec, dab, dom, da;
+    if (int rc = dev_alloc(ctx, drec, sizeof(CfRec) * nrec)) return rc;
+    if (int rc = dev_alloc(ctx, dab, sizeof(double) * ab.size())) return rc;
+    if (int rc = dev_alloc(ctx, dom, sizeof(double) * nw)) return rc;
+    if (int rc = dev_alloc(ctx, da, sizeof(double) * (size_t)nw * norb)) return rc;
+    MOED_CUDA(ctx, cudaMemcpyAsync(drec.p, cf.data(), sizeof(CfRec) * nrec, cudaMemcpyHostToDevice, ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpyAsync(dab.p, ab.data(), sizeof(double) * ab.size(), cudaMemcpyHostToDevice, ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpyAsync(dom.p, omega_real, sizeof(double) * nw, cudaMemcpyHostToDevice, ctx->stream));
+    const int T = 128;
+    k_dos<<<(nw * norb + T - 1) / T, T, 0, ctx->stream>>>((const CfRec *)drec.p, (int)nrec, (const double *)dab.p,
+                                                          ld, (const double *)dom.p, nw, norb, small,
+                                                          ctx->opt.fortran_cmplx, weighted, (double *)da.p);
+    MOED_CHECK_LAUNCH(ctx);
+    MOED_CUDA(ctx, cudaMemcpyAsync(Aff, da.p, sizeof(double) * (size_t)nw * norb, cudaMemcpyDeviceToHost, ctx->stream));
+    MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return MO_ED_OK;
 }
 

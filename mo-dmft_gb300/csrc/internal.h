@@ -254,6 +254,9 @@ struct mo_ed_ctx {
     // results of ed_solve / green
     std::vector<moed::StateVec> states;
     std::vector<moed::GreenRecord> green;
+    // square-lattice band of the DMFT self-consistency (mo_ed_set_band_structure)
+    moed::DevBuf d_hk;
+    int nq = 0;
 
     // scratch
     moed::DevBuf scratch_a, scratch_b, scratch_part;

@@ -92,6 +92,10 @@ SIGNATURES = [
     ("mo_ed_diag", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _dp]),
     ("mo_ed_diag_stats", C.c_int, [C.c_void_p, _ip, _llp, _dp, _dp]),
     ("mo_ed_green_stats", C.c_int, [C.c_void_p, _dp]),
+    ("mo_ed_set_band_structure", C.c_int, [C.c_void_p, C.c_int, _dp]),
+    ("mo_ed_delta_new", C.c_int, [C.c_void_p, C.c_int, C.c_double, _dp, _dp, _dp]),
+    ("mo_ed_n_from_gksum", C.c_int, [C.c_void_p, C.c_int, _dp, C.c_double, _dp]),
+    ("mo_ed_dos", C.c_int, [C.c_void_p, C.c_int, _dp, C.c_double, C.c_int, _dp]),
     ("mo_ed_solve", C.c_int, [C.c_void_p, _ip, _dp, _dp, _ip, _ip, C.c_int]),
     ("mo_ed_calc_green_ftn", C.c_int, [C.c_void_p, _dp]),
     ("mo_ed_green_coeffs", C.c_int, [C.c_void_p, _ip, _ip, _dp, C.c_int]),
@@ -388,6 +392,38 @@ class EDSolver:
         ab = ab.reshape(-1, 4, ld)
         return [dict(np=int(nsc[2 * r]), nn=int(nsc[2 * r + 1]), ap=ab[r, 0], bp=ab[r, 1], an=ab[r, 2],
                      bn=ab[r, 3]) for r in range(n)]
+
+    # ---- DMFT self-consistency and spectra (ed_green.F90:187-253, dos.f90) --
+    def set_band_structure(self, nq):
+        """ed_hamiltonian.F90:29-85 -> ef (norb); the band stays on the device."""
+        ef = np.zeros(self.norb)
+        self._chk(lib().mo_ed_set_band_structure(self._ctx, nq, _d(ef)))
+        return ef
+
+    def delta_new(self, Gr, D_ev, rmu):
+        """ed_green.F90:187-214 -> (new D_ev, Gksum), complex (norb, nw)."""
+        norb, nw = Gr.shape
+        g = np.ascontiguousarray(np.asarray(Gr, np.complex128).T).view(np.float64).ravel()
+        d = np.ascontiguousarray(np.asarray(D_ev, np.complex128).T).view(np.float64).ravel().copy()
+        k = np.zeros_like(d)
+        self._chk(lib().mo_ed_delta_new(self._ctx, nw, float(rmu), _d(g), _d(d), _d(k)))
+        back = lambda a: a.view(np.complex128).reshape(nw, norb).T.copy()
+        return back(d), back(k)
+
+    def n_from_gksum(self, Gksum, beta):
+        """ed_green.F90:227-253 -> nocc (norb)."""
+        norb, nw = Gksum.shape
+        g = np.ascontiguousarray(np.asarray(Gksum, np.complex128).T).view(np.float64).ravel()
+        out = np.zeros(norb)
+        self._chk(lib().mo_ed_n_from_gksum(self._ctx, nw, _d(g), float(beta), _d(out)))
+        return out
+
+    def dos(self, omega_real, small, weighted=False):
+        """dos.f90:1-106 from the last Green's function's records -> A (norb, nw)."""
+        om = _f64(omega_real)
+        out = np.zeros(self.norb * len(om))
+        self._chk(lib().mo_ed_dos(self._ctx, len(om), _d(om), float(small), int(bool(weighted)), _d(out)))
+        return out.reshape(len(om), self.norb).T.copy()
 
     # ---- bath fit (func.f90, frprmn.f90) ---------------------------------
     def FUNC(self, x, Ns, nwloc, nxsize, omega, D_ev, Nbath, Norb):

@@ -205,6 +205,41 @@ module mo_ed_bind
             real(c_double), intent(in) :: omega(*), ek(*), vk(*), ef(*)
             complex(c_double_complex), intent(out) :: d_ev(*)
         end function
+        integer(c_int) function mo_ed_set_band_structure(ctx, nq, ef) &
+                bind(C, name="mo_ed_set_band_structure")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: nq
+            real(c_double), intent(out) :: ef(*)
+        end function
+        integer(c_int) function mo_ed_delta_new(ctx, nwloc, rmu, gr, d_ev, gksum) &
+                bind(C, name="mo_ed_delta_new")
+            import :: c_int, c_ptr, c_double, c_double_complex
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: nwloc
+            real(c_double), value :: rmu
+            complex(c_double_complex), intent(in) :: gr(*)
+            complex(c_double_complex), intent(inout) :: d_ev(*)
+            complex(c_double_complex), intent(out) :: gksum(*)
+        end function
+        integer(c_int) function mo_ed_n_from_gksum(ctx, nw, gksum, beta, nocc) &
+                bind(C, name="mo_ed_n_from_gksum")
+            import :: c_int, c_ptr, c_double, c_double_complex
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: nw
+            complex(c_double_complex), intent(in) :: gksum(*)
+            real(c_double), value :: beta
+            real(c_double), intent(out) :: nocc(*)
+        end function
+        integer(c_int) function mo_ed_dos(ctx, nw, omega_real, small, weighted, aff) &
+                bind(C, name="mo_ed_dos")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: nw, weighted
+            real(c_double), intent(in) :: omega_real(*)
+            real(c_double), value :: small
+            real(c_double), intent(out) :: aff(*)
+        end function
         integer(c_int) function mo_ed_ev_to_x(ek, vk, ef, ns, nbath, nxsize, x) &
                 bind(C, name="mo_ed_ev_to_x")
             import :: c_int, c_double
@@ -232,6 +267,7 @@ module mo_ed_gpu
     public :: mo_ed_gpu_init, mo_ed_gpu_finalize, mo_ed_gpu_context, mo_ed_gpu_check
     public :: mo_ed_gpu_set_problem, mo_ed_gpu_solve, mo_ed_gpu_green
     public :: mo_ed_gpu_multiply_h, mo_ed_gpu_lanczos, mo_ed_gpu_diag
+    public :: mo_ed_gpu_set_band_structure, mo_ed_gpu_delta_new, mo_ed_gpu_dos
 contains
 
     ! Stop with the library's message on a nonzero status (the reference's die).
@@ -314,6 +350,36 @@ contains
         integer, intent(in) :: Norb, nwloc
         double complex, intent(out) :: Gr(Norb, nwloc)
         call mo_ed_gpu_check(mo_ed_calc_green_ftn(ctx, Gr), 'ed_calc_green_ftn')
+    end subroutine
+
+    ! ed_set_band_structure (ed_hamiltonian.F90:29-85): ef(Norb); the caller
+    ! copies ef into ek(1:Norb) as the reference does.
+    subroutine mo_ed_gpu_set_band_structure(Nq, Norb, ef)
+        integer, intent(in) :: Nq, Norb
+        double precision, intent(out) :: ef(Norb)
+        call mo_ed_gpu_check(mo_ed_set_band_structure(ctx, int(Nq, c_int), ef), 'ed_set_band_structure')
+    end subroutine
+
+    ! ed_delta_new + n_from_gksum (ed_green.F90:187-253): D_ev updated in place,
+    ! Gksum and the occupations returned.
+    subroutine mo_ed_gpu_delta_new(Norb, nwloc, rMu, beta, Gr, D_ev, Gksum, nocc)
+        integer, intent(in) :: Norb, nwloc
+        double precision, intent(in) :: rMu, beta
+        double complex, intent(in) :: Gr(Norb, nwloc)
+        double complex, intent(inout) :: D_ev(Norb, nwloc)
+        double complex, intent(out) :: Gksum(Norb, nwloc)
+        double precision, intent(out) :: nocc(Norb)
+        call mo_ed_gpu_check(mo_ed_delta_new(ctx, int(nwloc, c_int), rMu, Gr, D_ev, Gksum), 'ed_delta_new')
+        call mo_ed_gpu_check(mo_ed_n_from_gksum(ctx, int(nwloc, c_int), Gksum, beta, nocc), 'n_from_gksum')
+    end subroutine
+
+    ! dos (dos.f90:1-106) from the last Green's function's records, without
+    ! re-reading apbpanbn.dat; weighted = 0 is the reference's assignment.
+    subroutine mo_ed_gpu_dos(Norb, Nw, omega_real, small, weighted, Aff)
+        integer, intent(in) :: Norb, Nw, weighted
+        double precision, intent(in) :: omega_real(Nw), small
+        double precision, intent(out) :: Aff(Norb, Nw)
+        call mo_ed_gpu_check(mo_ed_dos(ctx, int(Nw, c_int), omega_real, small, int(weighted, c_int), Aff), 'dos')
     end subroutine
 
     ! multiply_H (ed_hamiltonian.F90:88-191) on a whole sector vector.

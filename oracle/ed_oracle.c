@@ -865,3 +865,111 @@ void or_calc_dev(int norb, int nsite, int nwloc, const double *omega, const doub
             dev[2 * k + 1] = d.im;
         }
 }
+
+/* ------------------------------------------------------------------ */
+/* DMFT self-consistency and real-frequency spectra                    */
+/* ------------------------------------------------------------------ */
+/* ed_hamiltonian.F90:29-85: Hk(i,i,ik) = -0.5 (cos kx + cos ky) for every
+ * orbital on an nk x nk grid (nk = int(sqrt(Nq)), kx outer), dq = 2 pi /
+ * float(nk); ef(i) = sum_k Hk(i,i,k) / float(Nq).  hk[nq] is the diagonal
+ * (the same for every orbital).  Returns -1 if nk*nk != nq (the reference
+ * stops). */
+int or_set_band_structure(int norb, int nq, double *hk, double *ef)
+{
+    const double pi = 4.0 * atan(1.0);
+    const int nk = (int)sqrt((double)nq);
+    const double dq = 2.0 * pi / (double)(float)nk;
+    int ik = 0;
+    for (int i = 1; i <= nk; ++i)
+        for (int j = 1; j <= nk; ++j) {
+            const double kx = dq * (double)(float)(i - 1), ky = dq * (double)(float)(j - 1);
+            hk[ik++] = -0.5 * (cos(kx) + cos(ky));
+        }
+    if (ik != nq) return -1;
+    for (int i = 0; i < norb; ++i) {
+        double s = 0.0;
+        for (int k = 0; k < nq; ++k) s += hk[k];
+        ef[i] = s / (double)(float)nq;
+    }
+    return 0;
+}
+
+/* ed_green.F90:187-214 (H(k) diagonal): per w_n and orbital,
+ * Gksum = (1/Nq) sum_q 1 / (1/Gr + D_ev + mu - Hk(q)), then
+ * D_ev <- 1/Gr - 1/Gksum + D_ev.  Gr, D_ev, Gksum: complex (norb, nwloc). */
+void or_delta_new(int norb, int nwloc, int nq, const double *hk, double rmu, const double *gr, double *dev,
+                  double *gksum)
+{
+    for (int iw = 0; iw < nwloc; ++iw) {
+        for (int iorb = 0; iorb < norb; ++iorb) {
+            const size_t k = (size_t)iw * norb + iorb;
+            const cplx g = c_make(gr[2 * k], gr[2 * k + 1]), d = c_make(dev[2 * k], dev[2 * k + 1]);
+            const cplx ginv = c_div(c_make(1.0, 0.0), g);
+            cplx acc = c_make(0.0, 0.0);
+            for (int jq = 0; jq < nq; ++jq) {
+                const cplx tmp = c_sub(c_add(c_add(ginv, d), c_make(rmu, 0.0)), c_make(hk[jq], 0.0));
+                acc = c_add(acc, c_div(c_make(1.0, 0.0), tmp));
+            }
+            acc = c_make(acc.re / (double)(float)nq, acc.im / (double)(float)nq);
+            const cplx dn = c_add(c_sub(ginv, c_div(c_make(1.0, 0.0), acc)), d);
+            gksum[2 * k] = acc.re;
+            gksum[2 * k + 1] = acc.im;
+            dev[2 * k] = dn.re;
+            dev[2 * k + 1] = dn.im;
+        }
+    }
+}
+
+/* ed_green.F90:227-253: nocc(iorb) = 2 sum_w Re Gksum(iorb, w) / beta + 0.5 */
+void or_n_from_gksum(int norb, int nw, const double *gksum, double beta, double *nocc)
+{
+    for (int iorb = 0; iorb < norb; ++iorb) {
+        double s = 0.0;
+        for (int iw = 0; iw < nw; ++iw) s += gksum[2 * ((size_t)iw * norb + iorb)];
+        nocc[iorb] = 2.0 * s / beta + 0.5;
+    }
+}
+
+/* dos.f90:1-106 over the records of apbpanbn.dat in file order: record r has
+ * orbital iorb[r] (1-based), energy ev[r], nstep_calc np[r] / nn[r] and
+ * coefficients ab[r][4][ld] = ap, bp, an, bn.  For each w:
+ *   G+ = bp(0)/(z+ - ap(0) - bp(1)/(z+ - ap(1) - ...)), z+ = CMPLX(ev + w, small),
+ *   G- = bn(0)/(z- + an(0) - bn(1)/(z- + an(1) - ...)), z- = CMPLX(w - ev, small),
+ *   A(iorb, w) = -Im(G+ + G-) / pi.
+ * As in dos_diag, A(iorb, :) is assigned, not accumulated, so the last
+ * record of each orbital sets it (weighted = 0).  weighted = 1 instead sums
+ * prob[r] * factor (1 if even[r], else 0.5) * (-Im(G+ + G-) / pi) over the
+ * records.  A run with nstep_calc < 0 (its excitation leaves the Fock
+ * space) adds nothing.  aff: real (norb, nw). */
+void or_dos(int norb, int nrec, const int *iorb, const double *ev, const double *prob, const int *even,
+            const int *np, const int *nn, const double *ab, int ld, int nw, const double *omega_real,
+            double small, int weighted, double *aff)
+{
+    const double pi = 4.0 * atan(1.0);
+    for (size_t i = 0; i < (size_t)norb * nw; ++i) aff[i] = 0.0;
+    for (int r = 0; r < nrec; ++r) {
+        const double *ap = ab + (size_t)(4 * r + 0) * ld, *bp = ab + (size_t)(4 * r + 1) * ld;
+        const double *an = ab + (size_t)(4 * r + 2) * ld, *bn = ab + (size_t)(4 * r + 3) * ld;
+        for (int iw = 0; iw < nw; ++iw) {
+            cplx grx = c_make(0.0, 0.0);
+            if (np[r] >= 0) {
+                const cplx z = fcmplx(ev[r] + omega_real[iw], small);
+                cplx g = c_div(c_make(bp[np[r]], 0.0), c_sub(z, c_make(ap[np[r]], 0.0)));
+                for (int is = np[r] - 1; is >= 0; --is)
+                    g = c_div(c_make(bp[is], 0.0), c_sub(c_sub(z, c_make(ap[is], 0.0)), g));
+                grx = g;
+            }
+            if (nn[r] >= 0) {
+                const cplx z = fcmplx(omega_real[iw] - ev[r], small);
+                cplx g = c_div(c_make(bn[nn[r]], 0.0), c_add(z, c_make(an[nn[r]], 0.0)));
+                for (int is = nn[r] - 1; is >= 0; --is)
+                    g = c_div(c_make(bn[is], 0.0), c_sub(c_add(z, c_make(an[is], 0.0)), g));
+                grx = c_add(grx, g);
+            }
+            const double a = -grx.im / pi;
+            double *out = aff + (size_t)iw * norb + (iorb[r] - 1);
+            if (weighted) *out += prob[r] * (even[r] ? 1.0 : 0.5) * a;
+            else *out = a;
+        }
+    }
+}

@@ -122,6 +122,19 @@ int or_frprmn(double *p, int n, double ftol, int *iter, double *fret, int nxsize
 void or_calc_dev(int norb, int nsite, int nwloc, const double *omega,
                  const double *ek, const double *vk, const double *ef, double *dev);
 
+/* ed_hamiltonian.F90:29-85: square-lattice band hk[nq] and ef[norb]. */
+int or_set_band_structure(int norb, int nq, double *hk, double *ef);
+/* ed_green.F90:187-214: Gksum and the updated D_ev (complex (norb, nwloc)). */
+void or_delta_new(int norb, int nwloc, int nq, const double *hk, double rmu, const double *gr,
+                  double *dev, double *gksum);
+/* ed_green.F90:227-253 */
+void or_n_from_gksum(int norb, int nw, const double *gksum, double beta, double *nocc);
+/* dos.f90:1-106 over apbpanbn.dat records (weighted = 0: the reference's
+ * assignment; 1: probability-weighted sum). */
+void or_dos(int norb, int nrec, const int *iorb, const double *ev, const double *prob,
+            const int *even, const int *np, const int *nn, const double *ab, int ld, int nw,
+            const double *omega_real, double small, int weighted, double *aff);
+
 /* Number of FUNC evaluations performed by or_frprmn since the last reset. */
 int64_t or_func_calls(void);
 void or_reset_func_calls(void);

@@ -91,6 +91,12 @@ def lib():
         L.or_frprmn.argtypes = [_dp, C.c_int, C.c_double, _ip, _dp, C.c_int, C.c_int, C.c_int,
                                 _dp, _dp, C.c_int, C.c_int]
         L.or_calc_dev.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp]
+        L.or_set_band_structure.restype = C.c_int
+        L.or_set_band_structure.argtypes = [C.c_int, C.c_int, _dp, _dp]
+        L.or_delta_new.argtypes = [C.c_int, C.c_int, C.c_int, _dp, C.c_double, _dp, _dp, _dp]
+        L.or_n_from_gksum.argtypes = [C.c_int, C.c_int, _dp, C.c_double, _dp]
+        L.or_dos.argtypes = [C.c_int, C.c_int, _ip, _dp, _dp, _ip, _ip, _ip, _dp, C.c_int, C.c_int, _dp,
+                             C.c_double, C.c_int, _dp]
         L.or_func_calls.restype = C.c_int64
         _lib = L
     return _lib
@@ -304,6 +310,55 @@ def calc_dev(norb, nsite, omega, ek, vk, ef):
     lib().or_calc_dev(norb, nsite, len(om), _d(om), _d(np.ascontiguousarray(ek, dtype=np.float64)),
                       _d(vkf), _d(np.ascontiguousarray(ef, dtype=np.float64)), _d(out))
     return out.view(np.complex128).reshape(len(om), norb).T.copy()
+
+
+def set_band_structure(norb, nq):
+    """ed_hamiltonian.F90:29-85 -> (hk[nq], ef[norb])."""
+    hk, ef = np.zeros(nq), np.zeros(norb)
+    if lib().or_set_band_structure(norb, nq, _d(hk), _d(ef)) != 0:
+        raise ValueError("Nq is not a square")
+    return hk, ef
+
+
+def delta_new(hk, rmu, gr, dev):
+    """ed_green.F90:187-214: gr, dev complex (norb, nw) -> (new dev, gksum)."""
+    norb, nw = gr.shape
+    g = np.ascontiguousarray(np.asarray(gr, np.complex128).T).view(np.float64).ravel()
+    d = np.ascontiguousarray(np.asarray(dev, np.complex128).T).view(np.float64).ravel().copy()
+    gk = np.zeros_like(d)
+    lib().or_delta_new(norb, nw, len(hk), _d(np.ascontiguousarray(hk, np.float64)), rmu, _d(g), _d(d), _d(gk))
+    back = lambda a: a.view(np.complex128).reshape(nw, norb).T.copy()
+    return back(d), back(gk)
+
+
+def n_from_gksum(gksum, beta):
+    """ed_green.F90:227-253: occupations from Gksum (complex (norb, nw))."""
+    norb, nw = gksum.shape
+    g = np.ascontiguousarray(np.asarray(gksum, np.complex128).T).view(np.float64).ravel()
+    out = np.zeros(norb)
+    lib().or_n_from_gksum(norb, nw, _d(g), beta, _d(out))
+    return out
+
+
+def dos(norb, records, omega_real, small, weighted=False):
+    """dos.f90:1-106 over apbpanbn.dat records: list of dicts with iorb (1-based),
+    ev, prob, even, np, nn (-1: no run), ap, bp, an, bn -> A (norb, nw)."""
+    n = len(records)
+    ld = max(max(r["np"], r["nn"]) for r in records) + 1 if n else 1
+    ab = np.zeros((max(n, 1), 4, ld))
+    for i, r in enumerate(records):
+        ab[i, 0, :r["np"] + 1] = r["ap"][:r["np"] + 1]
+        ab[i, 1, :r["np"] + 1] = r["bp"][:r["np"] + 1]
+        ab[i, 2, :r["nn"] + 1] = r["an"][:r["nn"] + 1]
+        ab[i, 3, :r["nn"] + 1] = r["bn"][:r["nn"] + 1]   # nstep_calc -1: no run
+    ii = lambda k: np.ascontiguousarray([int(r[k]) for r in records] or [0], np.int32)
+    dd = lambda k: np.ascontiguousarray([float(r[k]) for r in records] or [0.0], np.float64)
+    om = np.ascontiguousarray(omega_real, np.float64)
+    out = np.zeros(norb * len(om))
+    lib().or_dos(norb, n, _i(ii("iorb")), _d(dd("ev")), _d(dd("prob")), _i(ii("even")), _i(ii("np")),
+                 _i(ii("nn")), _d(np.ascontiguousarray(ab.ravel())), ld, len(om), _d(om), small, int(weighted),
+                 _d(out))
+    return out.reshape(len(om), norb).T.copy()
 
 
 def matsubara(nw, beta):

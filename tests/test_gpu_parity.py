@@ -374,6 +374,62 @@ def test_ed_solve_green_c2(solver, oracle, pkg, precision, etol, gtol):
         assert solver.green_stats() == 0
 
 
+# ---------------------------------------------------------------- DMFT loop pieces, spectra
+def test_band_delta_new_occupation(solver, oracle, pkg):
+    """ed_hamiltonian.F90:29-85 and ed_green.F90:187-253 at the reference's
+    default Nq = 10,000 (100 x 100 grid), 3 orbitals, 512 w_n: band average,
+    Gksum and the new D_ev to 1e-12 relative (the device sums the k grid in
+    another order), occupations to 1e-12."""
+    cfg = pkg.configs.config("C4")
+    ek, vk = cfg.model()
+    solver.set_model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
+    nq, nw, beta = 10000, 512, cfg.beta
+    ef = solver.set_band_structure(nq)
+    hk, ef_o = oracle.set_band_structure(cfg.norb, nq)
+    assert np.abs(ef - ef_o).max() < 1e-15
+    rng = np.random.default_rng(8)
+    om = pkg.matsubara(nw, beta)
+    gr = 1.0 / (1j * om[None, :] + 0.3 * rng.standard_normal((cfg.norb, 1)))
+    dev = 0.2 * (rng.standard_normal((cfg.norb, nw)) + 1j * rng.standard_normal((cfg.norb, nw)))
+    dn, gk = solver.delta_new(gr, dev, 1.0)
+    dn_o, gk_o = oracle.delta_new(hk, 1.0, gr, dev)
+    assert rel(gk, gk_o) < 1e-12 and rel(dn, dn_o) < 1e-12
+    assert np.abs(solver.n_from_gksum(gk, beta) - oracle.n_from_gksum(gk_o, beta)).max() < 1e-12
+    with pytest.raises(pkg.EDError):
+        solver.set_band_structure(10001)   # not a square grid
+
+
+@pytest.mark.parametrize("weighted", [False, True])
+def test_dos_vs_oracle(solver, oracle, pkg, weighted):
+    """dos.f90:1-106 on the records of a C1 solve + Green's function: the
+    device spectral function against the oracle on the same records, 1e-12
+    relative (runs that leave the Fock space are covered on the CPU)."""
+    cfg = pkg.configs.config("C1")
+    ek, vk = cfg.model()
+    solver.set_options(precision="fp64", nstep=cfg.nstep, nev=8, beta=cfg.beta)
+    solver.set_model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
+    solver.set_sectors([n for n, _ in cfg.sectors], [u for _, u in cfg.sectors])
+    solver.set_omega(cfg.omega())
+    st = solver.ed_solve()
+    solver.ed_calc_green_ftn()
+    recs = solver.green_coeffs()
+    meta = []
+    for e in st:
+        nelec, nup = cfg.sectors[e["sector"] - 1]
+        even = nelec - nup == nup
+        for _ in range(1 if even else 2):
+            for iorb in range(1, cfg.norb + 1):
+                meta.append(dict(iorb=iorb, ev=e["val"], prob=e["prob"], even=int(even)))
+    assert len(meta) == len(recs)
+    for m, r in zip(meta, recs):
+        r.update(m)
+    w = np.linspace(-4.0, 4.0, 801)
+    A = solver.dos(w, 0.05, weighted=weighted)
+    A_o = oracle.dos(cfg.norb, recs, w, 0.05, weighted=weighted)
+    assert rel(A, A_o) < 1e-12
+    assert np.all(np.isfinite(A))
+
+
 # ---------------------------------------------------------------- bath fit
 def fit_problem(pkg, nbatch=8):
     return pkg.configs.fit_config(seed=4, nbatch=nbatch)

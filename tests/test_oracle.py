@@ -264,3 +264,72 @@ def test_lanczos_iteration_tridiagonal(oracle):
         Q.append(w / np.sqrt(be2[-1]))
     np.testing.assert_allclose(a[:6], al, rtol=1e-10, atol=1e-10)
     np.testing.assert_allclose(bb[1:6], be2[:5], rtol=1e-10)
+
+
+# ---------------------------------------------------------------- DMFT loop pieces
+def test_band_structure(oracle):
+    """ed_hamiltonian.F90:29-85: -0.5 (cos kx + cos ky) on the k grid, kx outer;
+    the k-average vanishes on a full even grid; a non-square Nq is refused."""
+    hk, ef = oracle.set_band_structure(3, 16)
+    k = 2 * np.pi / 4 * np.arange(4)
+    ref = (-0.5 * (np.cos(k)[:, None] + np.cos(k)[None, :])).ravel()
+    assert np.abs(hk - ref).max() < 1e-15
+    assert np.abs(ef).max() < 1e-15 and ef.shape == (3,)
+    with pytest.raises(ValueError):
+        oracle.set_band_structure(1, 10)
+
+
+def test_delta_new_and_occupation(oracle):
+    """ed_green.F90:187-253 against a vectorised restatement."""
+    rng = np.random.default_rng(21)
+    norb, nw = 3, 16
+    hk, _ = oracle.set_band_structure(norb, 64)
+    gr = rng.standard_normal((norb, nw)) + 1j * (rng.standard_normal((norb, nw)) - 3.0)
+    dev = 0.1 * (rng.standard_normal((norb, nw)) + 1j * rng.standard_normal((norb, nw)))
+    dn, gk = oracle.delta_new(hk, 0.7, gr, dev)
+    gi = 1.0 / gr
+    gk2 = np.mean(1.0 / ((gi + dev + 0.7)[:, :, None] - hk[None, None, :]), axis=2)
+    assert np.abs(gk - gk2).max() < 1e-14 * np.abs(gk2).max()
+    assert np.abs(dn - (gi - 1.0 / gk2 + dev)).max() < 1e-13 * np.abs(dn).max()
+    beta = 50.0
+    assert np.abs(oracle.n_from_gksum(gk, beta) - (2.0 * gk.real.sum(axis=1) / beta + 0.5)).max() < 1e-14
+
+
+def _cf(z, a, b, n, sgn):
+    g = b[n] / (z + sgn * a[n])
+    for j in range(n - 1, -1, -1):
+        g = b[j] / (z + sgn * a[j] - g)
+    return g
+
+
+def test_dos_records(oracle):
+    """dos.f90:1-106: last record of an orbital assigns A (the reference's
+    dos_diag), or the probability-weighted sum; runs with nstep_calc = -1 add
+    nothing; CMPLX rounds E + w and small to default REAL."""
+    rng = np.random.default_rng(5)
+    norb, ld = 2, 6
+    recs = []
+    for r in range(5):
+        recs.append(dict(iorb=r % norb + 1, ev=-1.3 + 0.1 * r, prob=0.2 + 0.1 * r, even=r % 2,
+                         np=int(rng.integers(0, ld)) if r != 2 else -1, nn=int(rng.integers(0, ld)),
+                         ap=rng.standard_normal(ld), bp=rng.uniform(0.1, 1, ld), an=rng.standard_normal(ld),
+                         bn=rng.uniform(0.1, 1, ld)))
+    w = np.linspace(-3, 3, 41)
+    small = 0.05
+    f32 = lambda v: np.float64(np.float32(v))
+    A0 = oracle.dos(norb, recs, w, small, weighted=False)
+    A1 = oracle.dos(norb, recs, w, small, weighted=True)
+    R0 = np.zeros((norb, len(w)))
+    R1 = np.zeros((norb, len(w)))
+    for r in recs:
+        for i, x in enumerate(w):
+            g = 0j
+            if r["np"] >= 0:
+                g += _cf(complex(f32(r["ev"] + x), f32(small)), r["ap"], r["bp"], r["np"], -1)
+            if r["nn"] >= 0:
+                g += _cf(complex(f32(x - r["ev"]), f32(small)), r["an"], r["bn"], r["nn"], +1)
+            a = -g.imag / np.pi
+            R0[r["iorb"] - 1, i] = a
+            R1[r["iorb"] - 1, i] += r["prob"] * (1.0 if r["even"] else 0.5) * a
+    assert np.abs(A0 - R0).max() < 1e-12 * np.abs(R0).max()
+    assert np.abs(A1 - R1).max() < 1e-12 * np.abs(R1).max()
