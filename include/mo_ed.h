@@ -255,6 +255,26 @@ int mo_ed_n_from_gksum(mo_ed_ctx *ctx, int nw, const double *Gksum, double beta,
 int mo_ed_dos(mo_ed_ctx *ctx, int nw, const double *omega_real, double small, int weighted,
               double *Aff);
 
+/* ---- eigenpair and coefficient files (ed_io.F90:13-147, ed_green.F90:112-115) -- */
+/* Fortran unformatted sequential files as gfortran writes them (4-byte record
+ * length markers before and after each record, LOGICAL as a 4-byte 1/0).
+ * export: eigenvalues.dat (export_eigval's layout: nev_calc, then
+ * {ind, eigenvalue, Boltzmann factor} per kept state) and eigvec-SS-LLL-0000
+ * (nloc, then the vector in the reference's row order) for every state kept
+ * by the last mo_ed_solve, into directory dir (NULL or "": the current one).
+ * import: reads them back as the kept states (same model, sectors and nev),
+ * so mo_ed_calc_green_ftn can run without mo_ed_solve; *nev_calc receives the
+ * state count. */
+int mo_ed_export_eigvec(mo_ed_ctx *ctx, const char *dir);
+int mo_ed_import_eigvec(mo_ed_ctx *ctx, const char *dir, int *nev_calc);
+/* apbpanbn.dat: the records of the last mo_ed_calc_green_ftn in the
+ * reference's layout ({nstep_calcp, nstep_calcn}, then {iev, iorb, E, prob,
+ * even, ap, bp, an, bn}; nstep_calc = -1: no run).  read replaces the
+ * context's records (for mo_ed_dos, as dos.f90 reads the file); *nrec
+ * receives the record count. */
+int mo_ed_write_apbpanbn(mo_ed_ctx *ctx, const char *path);
+int mo_ed_read_apbpanbn(mo_ed_ctx *ctx, const char *path, int *nrec);
+
 /* ---- a18-a22: bath fit (func.f90, frprmn.f90, ed_green.F90:260-273) ------ */
 /* FUNC (func.f90:1-45): chi^2 at x(nxsize); D_ev (norb, nwloc) complex. */
 int mo_ed_func(mo_ed_ctx *ctx, const double *x, int ns, int nwloc, int nxsize,

@@ -699,6 +699,7 @@ int mo_ed_solve(mo_ed_ctx *ctx, int *nev_calc, double *val, double *prob, int *s
         st.level = k % nev;
         st.val = eig_all[k];
         st.prob = pev[k] / Z;
+        st.pev = pev[k];
         st.prec = ctx->opt.precision;
         if (st.level < (int)vecs[st.sector].size()) std::swap(st.vec, vecs[st.sector][st.level]);
         ctx->states.push_back(std::move(st));

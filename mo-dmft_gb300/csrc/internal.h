@@ -205,6 +205,7 @@ struct StateVec {             // an eigenpair kept on the device after ed_solve
     int sector;               // 0-based index into the sector list
     int level;                // 0-based level within the sector
     double val, prob;
+    double pev = 0.0;         // Boltzmann factor before normalisation (eigenvalues.dat)
     int prec;                 // MO_ED_FP32 / MO_ED_FP64: the precision of vec
     DevBuf vec;               // Dpad elements in the layout of its sector
 };

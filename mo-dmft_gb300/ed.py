@@ -96,6 +96,10 @@ SIGNATURES = [
     ("mo_ed_delta_new", C.c_int, [C.c_void_p, C.c_int, C.c_double, _dp, _dp, _dp]),
     ("mo_ed_n_from_gksum", C.c_int, [C.c_void_p, C.c_int, _dp, C.c_double, _dp]),
     ("mo_ed_dos", C.c_int, [C.c_void_p, C.c_int, _dp, C.c_double, C.c_int, _dp]),
+    ("mo_ed_export_eigvec", C.c_int, [C.c_void_p, C.c_char_p]),
+    ("mo_ed_import_eigvec", C.c_int, [C.c_void_p, C.c_char_p, _ip]),
+    ("mo_ed_write_apbpanbn", C.c_int, [C.c_void_p, C.c_char_p]),
+    ("mo_ed_read_apbpanbn", C.c_int, [C.c_void_p, C.c_char_p, _ip]),
     ("mo_ed_solve", C.c_int, [C.c_void_p, _ip, _dp, _dp, _ip, _ip, C.c_int]),
     ("mo_ed_calc_green_ftn", C.c_int, [C.c_void_p, _dp]),
     ("mo_ed_green_coeffs", C.c_int, [C.c_void_p, _ip, _ip, _dp, C.c_int]),
@@ -424,6 +428,25 @@ class EDSolver:
         out = np.zeros(self.norb * len(om))
         self._chk(lib().mo_ed_dos(self._ctx, len(om), _d(om), float(small), int(bool(weighted)), _d(out)))
         return out.reshape(len(om), self.norb).T.copy()
+
+    # ---- files (ed_io.F90, apbpanbn.dat) ----------------------------------
+    def export_eigvec(self, directory=""):
+        """ed_io.F90 export_eigval / export_eigvec of the kept states."""
+        self._chk(lib().mo_ed_export_eigvec(self._ctx, os.fsencode(directory)))
+
+    def import_eigvec(self, directory=""):
+        """Kept states from eigenvalues.dat + eigvec files -> nev_calc."""
+        n = C.c_int()
+        self._chk(lib().mo_ed_import_eigvec(self._ctx, os.fsencode(directory), C.byref(n)))
+        return n.value
+
+    def write_apbpanbn(self, path):
+        self._chk(lib().mo_ed_write_apbpanbn(self._ctx, os.fsencode(path)))
+
+    def read_apbpanbn(self, path):
+        n = C.c_int()
+        self._chk(lib().mo_ed_read_apbpanbn(self._ctx, os.fsencode(path), C.byref(n)))
+        return n.value
 
     # ---- bath fit (func.f90, frprmn.f90) ---------------------------------
     def FUNC(self, x, Ns, nwloc, nxsize, omega, D_ev, Nbath, Norb):

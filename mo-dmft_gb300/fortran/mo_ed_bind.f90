@@ -240,6 +240,28 @@ module mo_ed_bind
             real(c_double), value :: small
             real(c_double), intent(out) :: aff(*)
         end function
+        integer(c_int) function mo_ed_export_eigvec(ctx, dir) bind(C, name="mo_ed_export_eigvec")
+            import :: c_int, c_ptr, c_char
+            type(c_ptr), value :: ctx
+            character(kind=c_char), intent(in) :: dir(*)
+        end function
+        integer(c_int) function mo_ed_import_eigvec(ctx, dir, nev_calc) bind(C, name="mo_ed_import_eigvec")
+            import :: c_int, c_ptr, c_char
+            type(c_ptr), value :: ctx
+            character(kind=c_char), intent(in) :: dir(*)
+            integer(c_int), intent(out) :: nev_calc
+        end function
+        integer(c_int) function mo_ed_write_apbpanbn(ctx, path) bind(C, name="mo_ed_write_apbpanbn")
+            import :: c_int, c_ptr, c_char
+            type(c_ptr), value :: ctx
+            character(kind=c_char), intent(in) :: path(*)
+        end function
+        integer(c_int) function mo_ed_read_apbpanbn(ctx, path, nrec) bind(C, name="mo_ed_read_apbpanbn")
+            import :: c_int, c_ptr, c_char
+            type(c_ptr), value :: ctx
+            character(kind=c_char), intent(in) :: path(*)
+            integer(c_int), intent(out) :: nrec
+        end function
         integer(c_int) function mo_ed_ev_to_x(ek, vk, ef, ns, nbath, nxsize, x) &
                 bind(C, name="mo_ed_ev_to_x")
             import :: c_int, c_double
@@ -268,6 +290,7 @@ module mo_ed_gpu
     public :: mo_ed_gpu_set_problem, mo_ed_gpu_solve, mo_ed_gpu_green
     public :: mo_ed_gpu_multiply_h, mo_ed_gpu_lanczos, mo_ed_gpu_diag
     public :: mo_ed_gpu_set_band_structure, mo_ed_gpu_delta_new, mo_ed_gpu_dos
+    public :: mo_ed_gpu_export_eigvec, mo_ed_gpu_import_eigvec, mo_ed_gpu_write_apbpanbn
 contains
 
     ! Stop with the library's message on a nonzero status (the reference's die).
@@ -380,6 +403,25 @@ contains
         double precision, intent(in) :: omega_real(Nw), small
         double precision, intent(out) :: Aff(Norb, Nw)
         call mo_ed_gpu_check(mo_ed_dos(ctx, int(Nw, c_int), omega_real, small, int(weighted, c_int), Aff), 'dos')
+    end subroutine
+
+    ! export_eigval + export_eigvec (ed_io.F90:13-56) of the kept states, in
+    ! the current directory, file names as eigvec_filename.
+    subroutine mo_ed_gpu_export_eigvec()
+        call mo_ed_gpu_check(mo_ed_export_eigvec(ctx, c_null_char), 'export_eigvec')
+    end subroutine
+
+    ! import_eigval + import_eigvec (ed_io.F90:58-138): kept states read back.
+    subroutine mo_ed_gpu_import_eigvec(nev_calc)
+        integer, intent(out) :: nev_calc
+        integer(c_int) :: n
+        call mo_ed_gpu_check(mo_ed_import_eigvec(ctx, c_null_char, n), 'import_eigvec')
+        nev_calc = n
+    end subroutine
+
+    ! apbpanbn.dat (ed_green.F90:112-115,125-128) of the last mo_ed_gpu_green.
+    subroutine mo_ed_gpu_write_apbpanbn()
+        call mo_ed_gpu_check(mo_ed_write_apbpanbn(ctx, 'apbpanbn.dat' // c_null_char), 'apbpanbn.dat')
     end subroutine
 
     ! multiply_H (ed_hamiltonian.F90:88-191) on a whole sector vector.

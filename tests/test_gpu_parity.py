@@ -430,6 +430,83 @@ def test_dos_vs_oracle(solver, oracle, pkg, weighted):
     assert np.all(np.isfinite(A))
 
 
+def _fortran_records(path):
+    """Records of a gfortran unformatted sequential file (4-byte markers)."""
+    data, out, o = open(path, "rb").read(), [], 0
+    while o < len(data):
+        n = int(np.frombuffer(data, np.int32, 1, o)[0])
+        out.append(data[o + 4:o + 4 + n])
+        assert int(np.frombuffer(data, np.int32, 1, o + 4 + n)[0]) == n
+        o += 8 + n
+    return out
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_eigvec_and_apbpanbn_files(pkg, oracle, tmp_path, precision):
+    """ed_io.F90 / apbpanbn.dat round trips on C2: the exported eigenpairs
+    have the reference's file layout and are eigenvectors of the oracle's H;
+    a fresh context that imports them (no ed_solve) gives the same G(i w_n)
+    bit for bit; apbpanbn.dat holds the same records as mo_ed_green_coeffs,
+    and a context that reads it gives the same spectral function."""
+    cfg = pkg.configs.config("C2")
+    ek, vk = cfg.model()
+
+    def fresh():
+        s = pkg.EDSolver(0)
+        s.set_options(precision=precision, nstep=cfg.nstep, nev=4, beta=cfg.beta)
+        s.set_model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
+        s.set_sectors([n for n, _ in cfg.sectors], [u for _, u in cfg.sectors])
+        s.set_omega(cfg.omega())
+        return s
+
+    s1 = fresh()
+    st = s1.ed_solve()
+    G1 = s1.ed_calc_green_ftn()
+    s1.export_eigvec(str(tmp_path))
+    s1.write_apbpanbn(str(tmp_path / "apbpanbn.dat"))
+    w = np.linspace(-3.0, 3.0, 301)
+    A1 = s1.dos(w, 0.05)
+    recs = s1.green_coeffs()
+    # eigenvalues.dat: nev_calc, then {ind, E, pev} per kept state
+    r = _fortran_records(tmp_path / "eigenvalues.dat")
+    assert len(r) == 2 and int(np.frombuffer(r[0], np.int32)[0]) == len(st)
+    ent = np.frombuffer(r[1], np.dtype([("ind", "<i4"), ("val", "<f8"), ("pev", "<f8")]))
+    assert [int(e["ind"]) for e in ent] == [(e["sector"] - 1) * 4 + e["level"] for e in st]
+    assert np.array_equal(ent["val"], [e["val"] for e in st])
+    m = oracle.Model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
+    for e in st[:3]:
+        nelec, nup = cfg.sectors[e["sector"] - 1]
+        r = _fortran_records(tmp_path / f"eigvec-{e['sector']:02d}-{e['level']:03d}-0000")
+        v = np.frombuffer(r[1], "<f8")
+        assert int(np.frombuffer(r[0], np.int32)[0]) == len(v)
+        b = oracle.Basis(m.nsite, nup, nelec - nup)
+        res = np.linalg.norm(oracle.multiply_H(m, b, v) - e["val"] * v) / np.linalg.norm(v)
+        assert res < (1e-8 if precision == "fp64" else 1e-4)
+    s1.close()
+    # import: same states, same G without ed_solve
+    s2 = fresh()
+    assert s2.import_eigvec(str(tmp_path)) == len(st)
+    assert np.array_equal(s2.ed_calc_green_ftn(), G1)
+    s2.close()
+    # apbpanbn.dat: the records of mo_ed_green_coeffs, read back for dos
+    r = _fortran_records(tmp_path / "apbpanbn.dat")
+    assert len(r) == 2 * len(recs)
+    for k, rec in enumerate(recs):
+        npp, nn = np.frombuffer(r[2 * k], np.int32)
+        assert (npp, nn) == (rec["np"], rec["nn"])
+        body = r[2 * k + 1]
+        iev, iorb = np.frombuffer(body[:8], np.int32)
+        ev, prob = np.frombuffer(body[8:24], "<f8")
+        assert 1 <= iorb <= cfg.norb and ev == st[iev - 1]["val"] and prob == st[iev - 1]["prob"]
+        coef = np.frombuffer(body[28:], "<f8")
+        want = np.concatenate([rec["ap"][:npp + 1], rec["bp"][:npp + 1], rec["an"][:nn + 1], rec["bn"][:nn + 1]])
+        assert np.array_equal(coef, want)
+    s3 = fresh()
+    assert s3.read_apbpanbn(str(tmp_path / "apbpanbn.dat")) == len(recs)
+    assert np.array_equal(s3.dos(w, 0.05), A1)
+    s3.close()
+
+
 # ---------------------------------------------------------------- bath fit
 def fit_problem(pkg, nbatch=8):
     return pkg.configs.fit_config(seed=4, nbatch=nbatch)
