@@ -117,3 +117,93 @@ def fit_config(seed=4, nbatch=256, noise=1e-4):
         X0[b, nbath + nbath * norb:] = f0
     return dict(norb=norb, nbath=nbath, nw=nw, beta=beta, omega=omega, dev=dev, X0=X0,
                 hidden=dict(eps=eps, vk=vk, ef=ef))
+
+
+# ---------------------------------------------------------------------------
+# FDF input files (ed_config.f90:43-126)
+# ---------------------------------------------------------------------------
+# Labels the reference reads, with its defaults.  FDF compares labels without
+# case and without '.', '_' and '-'.
+FDF_DEFAULTS = {
+    "DMFT.Norbs": 2, "DMFT.Nbaths": 2, "DMFT.Nsectors": 2, "DMFT.U": 1.0, "DMFT.J": 0.3,
+    "DMFT.Mu": 1.0, "DMFT.beta": 100.0, "DMFT.small": 0.05, "DMFT.ContinuedFractionSteps": 50,
+    "DMFT.MaxIterations": 100, "DMFT.ScfTolerance": 1e-4, "DMFT.Nev": 30, "DMFT.Nq": 10000,
+    "DMFT.Nw": 2000,
+}
+
+
+def _fdf_key(label):
+    return "".join(ch for ch in label.lower() if ch not in "._-")
+
+
+def read_fdf(path_or_text):
+    """Parse an FDF input with the reference's DMFT labels.
+
+    Returns a dict with every scalar of ed_config.f90:52-126 (the reference's
+    defaults where a label is absent), "sectors" [(nelec, nup)] from
+    %block DMFT.Sectors, "eps_bath" (nbath) from DMFT.Baths and "vk"
+    (norb, nbath) from DMFT.BathCouplings (one line per bath level, one column
+    per orbital).  Lines after the first Nsectors / Nbaths of a block are
+    ignored, as the reference's loops stop there."""
+    text = path_or_text
+    if "\n" not in text and not text.lstrip().startswith("DMFT"):
+        with open(path_or_text) as f:
+            text = f.read()
+    scal, blocks, cur = {}, {}, None
+    for raw in text.splitlines():
+        line = raw.split("#", 1)[0].strip()
+        if not line:
+            continue
+        words = line.split()
+        if words[0].lower() == "%block":
+            cur = _fdf_key(words[1])
+            blocks[cur] = []
+            continue
+        if words[0].lower() == "%endblock":
+            cur = None
+            continue
+        if cur is not None:
+            blocks[cur].append(words)
+        elif len(words) >= 2:
+            scal[_fdf_key(words[0])] = words[1]
+    out = {}
+    for label, dflt in FDF_DEFAULTS.items():
+        v = scal.get(_fdf_key(label))
+        if v is None:
+            out[label] = dflt
+        else:
+            v = v.replace("d", "e").replace("D", "e")
+            out[label] = int(v) if isinstance(dflt, int) else float(v)
+    norb, nbath, nsec = out["DMFT.Norbs"], out["DMFT.Nbaths"], out["DMFT.Nsectors"]
+    sec = blocks.get(_fdf_key("DMFT.Sectors"), [])[:nsec]
+    out["sectors"] = [(int(w[0]), int(w[1])) for w in sec]
+    baths = blocks.get(_fdf_key("DMFT.Baths"), [])[:nbath]
+    out["eps_bath"] = np.array([float(w[0].replace("d", "e").replace("D", "e")) for w in baths])
+    cpl = blocks.get(_fdf_key("DMFT.BathCouplings"), [])[:nbath]
+    vk = np.zeros((norb, nbath))
+    for i, w in enumerate(cpl):
+        for j in range(norb):
+            vk[j, i] = float(w[j].replace("d", "e").replace("D", "e"))
+    out["vk"] = vk
+    return out
+
+
+def write_fdf(cfg: ImpurityConfig, path, nev=30, nq=10000, mu=None, small=0.05, nloop=100, scf_tol=1e-4):
+    """Write a configuration as an FDF input the reference reads
+    (ed_config.f90:52-126).  The reference takes the impurity levels from the
+    band structure (ed_hamiltonian.F90:53-56), not from the input, so ek(1:norb)
+    of cfg.model() is not written."""
+    ek, vk = cfg.model()
+    lines = [
+        f"DMFT.Norbs {cfg.norb}", f"DMFT.Nbaths {cfg.nbath}", f"DMFT.Nsectors {len(cfg.sectors)}",
+        "%block DMFT.Sectors", *[f"  {n} {u}" for n, u in cfg.sectors], "%endblock DMFT.Sectors",
+        f"DMFT.U {cfg.U!r}", f"DMFT.J {cfg.J!r}", f"DMFT.Mu {float(cfg.mu_ph() if mu is None else mu)!r}",
+        f"DMFT.beta {cfg.beta!r}",
+        "%block DMFT.Baths", *[f"  {float(e)!r}" for e in ek[cfg.norb:]], "%endblock DMFT.Baths",
+        "%block DMFT.BathCouplings", *["  " + " ".join(repr(float(v)) for v in vk[:, i]) for i in range(cfg.nbath)],
+        "%endblock DMFT.BathCouplings",
+        f"DMFT.small {small!r}", f"DMFT.ContinuedFractionSteps {cfg.nstep}", f"DMFT.MaxIterations {nloop}",
+        f"DMFT.ScfTolerance {scf_tol!r}", f"DMFT.Nev {nev}", f"DMFT.Nq {nq}", f"DMFT.Nw {cfg.nw}",
+    ]
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")

@@ -333,3 +333,33 @@ def test_dos_records(oracle):
             R1[r["iorb"] - 1, i] += r["prob"] * (1.0 if r["even"] else 0.5) * a
     assert np.abs(A0 - R0).max() < 1e-12 * np.abs(R0).max()
     assert np.abs(A1 - R1).max() < 1e-12 * np.abs(R1).max()
+
+
+def test_fdf_round_trip_and_parsing(tmp_path):
+    """FDF input (ed_config.f90:52-126): a written configuration reads back
+    exactly; labels ignore case and '.', '_', '-'; '#' comments; absent
+    labels take the reference's defaults; D exponents."""
+    import importlib.util
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location("moed_configs", os.path.join(root, "mo-dmft_gb300", "configs.py"))
+    cf = importlib.util.module_from_spec(spec)
+    sys.modules["moed_configs"] = cf   # dataclasses resolve their module by name
+    spec.loader.exec_module(cf)
+    cfg = cf.config("C2")
+    p = tmp_path / "input.fdf"
+    cf.write_fdf(cfg, p, nev=6)
+    d = cf.read_fdf(str(p))
+    ek, vk = cfg.model()
+    assert d["DMFT.Norbs"] == 2 and d["DMFT.Nbaths"] == 6 and d["DMFT.Nev"] == 6
+    assert d["sectors"] == cfg.sectors and d["DMFT.U"] == cfg.U and d["DMFT.beta"] == cfg.beta
+    assert np.array_equal(d["eps_bath"], ek[cfg.norb:]) and np.array_equal(d["vk"], vk)
+    text = "\n".join(["dmft_norbs 1   # one orbital", "DMFT-NBATHS 2", "DMFT.Nsectors 1",
+                      "%block dmft.sectors", " 3 2", " 9 9", "%endblock dmft.sectors",
+                      "%block DMFT.Baths", " -0.5d0", " 0.5D0", "%endblock DMFT.Baths",
+                      "%block DMFT.BathCouplings", " 0.25", " 0.3", "%endblock DMFT.BathCouplings",
+                      "DMFT.U 2.0d0"])
+    d = cf.read_fdf(text)
+    assert d["DMFT.Norbs"] == 1 and d["DMFT.Nbaths"] == 2 and d["sectors"] == [(3, 2)]
+    assert np.array_equal(d["eps_bath"], [-0.5, 0.5]) and np.array_equal(d["vk"], [[0.25, 0.3]])
+    assert d["DMFT.U"] == 2.0 and d["DMFT.J"] == 0.3 and d["DMFT.Nq"] == 10000
