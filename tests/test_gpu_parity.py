@@ -507,6 +507,38 @@ def test_eigvec_and_apbpanbn_files(pkg, oracle, tmp_path, precision):
     s3.close()
 
 
+def test_dmft_loop_first_iteration(pkg, oracle, tmp_path):
+    """main.f90's DMFT loop through the C-ABI (dmft_loop) on C1 written as
+    an FDF input: the first iteration's G(i w_n), Gksum and occupations
+    against the oracle's chain (ed_solve, ed_calc_green_ftn, ed_delta_new,
+    n_from_gksum) from the same start, and a fitted bath whose chi^2 is no
+    worse than the oracle's frprmn from the same start."""
+    cfg = pkg.configs.config("C1")
+    p = tmp_path / "input.fdf"
+    pkg.configs.write_fdf(cfg, p, nev=8, nq=400)
+    inp = pkg.configs.read_fdf(str(p))
+    s = pkg.EDSolver(0)
+    out = pkg.dmft_loop(s, inp, nloop=1, precision="fp64")
+    s.close()
+    assert out["iterations"] == 1 and np.all(np.isfinite(out["Sigma"]))
+    norb, nbath, ns = cfg.norb, cfg.nbath, cfg.nsite
+    hk, ef = oracle.set_band_structure(norb, 400)
+    ek = np.concatenate([ef, inp["eps_bath"]])
+    vk = inp["vk"]
+    om = oracle.matsubara(cfg.nw, cfg.beta)
+    dev0 = oracle.calc_dev(norb, ns, om, ek, vk, ef)
+    m = oracle.Model(norb, nbath, cfg.U, cfg.J, ek, vk)
+    st_o, vecs = oracle.ed_solve(m, inp["sectors"], 8, cfg.beta)
+    Gr_o = oracle.ed_calc_green_ftn(m, inp["sectors"], st_o, vecs, cfg.nstep, om)
+    assert rel(out["Gr"], Gr_o) < 1e-8
+    dn_o, gk_o = oracle.delta_new(hk, inp["DMFT.Mu"], Gr_o, dev0)
+    assert rel(out["Gksum"], gk_o) < 1e-8
+    assert np.abs(out["nocc"] - oracle.n_from_gksum(gk_o, cfg.beta)).max() < 1e-8
+    x0 = oracle.ev_to_x(ek, vk, ef, ns, nbath)
+    _, f_o, _, _ = oracle.frprmn(x0, ns, om, dn_o, nbath, norb)
+    assert out["history"][0]["chi2"] <= 1.1 * f_o + 1e-10
+
+
 # ---------------------------------------------------------------- bath fit
 def fit_problem(pkg, nbatch=8):
     return pkg.configs.fit_config(seed=4, nbatch=nbatch)
