@@ -1,7 +1,7 @@
 /*
  * ed_oracle.c -- FP64 CPU restatement of the MO-DMFT ED hot path.
  *
- * TEST INFRASTRUCTURE ONLY (the checker and the "port" CPU baseline); see
+ * TEST INFRASTRUCTURE ONLY (the parity reference of the tests and the "port" CPU baseline); see
  * ed_oracle.h.  Nothing in the product links or loads this file.
  *
  * Each routine follows the cited reference routine loop for loop on a single

@@ -1,7 +1,7 @@
 /*
  * ed_oracle.h -- CPU restatement of the MO-DMFT exact-diagonalization hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA solver
+ * TEST INFRASTRUCTURE ONLY.  This library is the parity reference for the CUDA solver
  * and the timed CPU baseline ("port") of bench.py.  It is never linked into,
  * loaded by or called from the product library; only tests/, the smoke check
  * of __graft_entry__.py and the CPU-baseline leg of bench.py may use it.

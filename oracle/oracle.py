@@ -1,6 +1,6 @@
 """Python face of the CPU oracle (TEST INFRASTRUCTURE ONLY).
 
-This module is the checker for the CUDA solver and the "port" CPU baseline of
+This module is the parity reference for the CUDA solver and the "port" CPU baseline of
 ``bench.py``.  Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline
 leg of ``bench.py`` may import it; the product library never does.
 
