@@ -448,6 +448,14 @@ int species_dblocks(mo_ed_ctx *ctx, Species *sp, int ld)
 {
     constexpr long long kChunkElems = 1 << 16;
     if (!sp->dblk_ptr) {
+        // a build that failed part way left some tables: start over
+        cudaFree(sp->dblk_off);
+        cudaFree(sp->dblk_rows);
+        cudaFree(sp->dblk_mv_f);
+        cudaFree(sp->dblk_mv_d);
+        sp->dblk_off = sp->dblk_rows = nullptr;
+        sp->dblk_mv_f = nullptr;
+        sp->dblk_mv_d = nullptr;
         const int n = sp->n, hw = sp->hw, nsite = sp->nsite, N = sp->N;
         int nsub = 0;
         for (int v : ctx->site_subsys) nsub = std::max(nsub, v + 1);
