@@ -363,3 +363,38 @@ def test_fdf_round_trip_and_parsing(tmp_path):
     assert d["DMFT.Norbs"] == 1 and d["DMFT.Nbaths"] == 2 and d["sectors"] == [(3, 2)]
     assert np.array_equal(d["eps_bath"], [-0.5, 0.5]) and np.array_equal(d["vk"], [[0.25, 0.3]])
     assert d["DMFT.U"] == 2.0 and d["DMFT.J"] == 0.3 and d["DMFT.Nq"] == 10000
+
+
+@pytest.mark.parametrize("nsite,nu,nd", [(4, 2, 1), (5, 2, 3), (6, 3, 3)])
+def test_apply_c_dense_operator(oracle, nsite, nu, nd):
+    """apply_c (ed_operators.F90:10-61) against the creation / annihilation
+    operator built as a dense matrix in Python from the basis words: row
+    index up-rank fastest, sign (-1)^(occupied bits below the target bit of
+    the 2*Nsite-bit word, spin-down bits above the spin-up ones)."""
+    m = oracle.Model(min(2, nsite - 1), nsite - min(2, nsite - 1), 1.0, 0.2, np.zeros(nsite),
+                     np.zeros((min(2, nsite - 1), nsite - min(2, nsite - 1))))
+    b = oracle.Basis(nsite, nu, nd)
+    rng = np.random.default_rng(nsite * 10 + nu)
+    v = rng.standard_normal(b.ntot)
+    for ispin in (1, 2):
+        for iorb in range(1, m.norb + 1):
+            for pm in (1, 2):
+                tu = nu + ((1 if pm == 1 else -1) if ispin == 1 else 0)
+                td = nd + ((1 if pm == 1 else -1) if ispin == 2 else 0)
+                if not (0 <= tu <= nsite and 0 <= td <= nsite):
+                    continue
+                bo, out = oracle.apply_c(m, b, v, pm, iorb, ispin)
+                ref = np.zeros(bo.ntot)
+                bit = (ispin - 1) * nsite + iorb - 1
+                for idn in range(b.ndown):
+                    for iup in range(b.nup):
+                        w = int(b.up[iup]) | (int(b.down[idn]) << nsite)
+                        occ = (w >> bit) & 1
+                        if (pm == 1) == bool(occ):
+                            continue          # c+ on an occupied / c on an empty orbital
+                        sgn = -1.0 if bin(w & ((1 << bit) - 1)).count("1") % 2 else 1.0
+                        w2 = w ^ (1 << bit)
+                        u2, d2 = w2 & ((1 << nsite) - 1), w2 >> nsite
+                        j = (int(bo.idx_down[d2]) - 1) * bo.nup + int(bo.idx_up[u2]) - 1
+                        ref[j] += sgn * v[idn * b.nup + iup]
+                assert np.array_equal(out, ref), (ispin, iorb, pm)
