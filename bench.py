@@ -346,16 +346,25 @@ def run_ours(args):
 
     tuning, chosen = s.hv_tuning(nup, ndn, pkg.FP32)
     traffic = profile_traffic(tuning[chosen][0][3])
+    def guarded(fn, *a):
+        # a secondary measurement that fails is reported in the line instead of
+        # taking the headline number down with it
+        try:
+            return fn(*a)
+        except Exception as e:   # noqa: BLE001
+            return {"error": f"{type(e).__name__}: {e}"}
+
     lg = None
     fit = None
     if rank == 0 and not args.no_lanczos_g:
-        lg = {c: lanczos_g(pkg, c, args.lg_nev, tuple(args.lg_precisions.split(","))) for c in args.lg_config.split(",") if c}
+        lg = {c: guarded(lanczos_g, pkg, c, args.lg_nev, tuple(args.lg_precisions.split(",")))
+              for c in args.lg_config.split(",") if c}
     if rank == 0 and not args.no_fit:
-        fit = fit_bench(pkg, 0 if args.no_cpu else 2)
-    dmft = dmft_bench(pkg, not args.no_cpu) if rank == 0 and not args.no_fit else None
+        fit = guarded(fit_bench, pkg, 0 if args.no_cpu else 2)
+    dmft = guarded(dmft_bench, pkg, not args.no_cpu) if rank == 0 and not args.no_fit else None
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        cpu = cpu_baseline_sample(cfg, nup, ndn)
+        cpu = guarded(cpu_baseline_sample, cfg, nup, ndn)
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": ws, "steps": args.steps,
