@@ -95,3 +95,20 @@ def test_fortran_bindings_match_header():
         assert fname == cname and cname in decl, cname
         n = 0 if not args.strip() else len(args.split(","))
         assert n == decl[cname], (cname, n, decl[cname])
+
+
+@pytest.mark.parametrize("lang,std", [("c", "c99"), ("c++", "c++11")])
+def test_header_compiles_standalone(tmp_path, lang, std):
+    """include/mo_ed.h is plain C (and C++ through its extern "C" guard): a host
+    of either language includes it with nothing else."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc" if lang == "c" else "g++")
+    if cc is None:
+        pytest.skip("no host compiler")
+    src = tmp_path / "use_header.c"
+    src.write_text('#include "mo_ed.h"\nint main(void) { mo_ed_options o; (void)o; return 0; }\n')
+    r = subprocess.run([cc, "-x", lang, f"-std={std}", "-Wall", "-Wextra", "-pedantic", "-Werror",
+                        "-I", os.path.join(ROOT, "include"), "-c", str(src), "-o", str(tmp_path / "u.o")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
