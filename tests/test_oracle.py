@@ -398,3 +398,23 @@ def test_apply_c_dense_operator(oracle, nsite, nu, nd):
                         j = (int(bo.idx_down[d2]) - 1) * bo.nup + int(bo.idx_up[u2]) - 1
                         ref[j] += sgn * v[idn * b.nup + iup]
                 assert np.array_equal(out, ref), (ispin, iorb, pm)
+
+
+def test_sector_eigs_arpack_path_matches_dense(oracle):
+    """The oracle's diag() stand-in for large sectors (scipy ARPACK eigsh, 'SA',
+    tol = 0 as ed_solver.F90:149 asks of PARPACK) agrees with dense eigh on a
+    sector small enough for both (D = 1,225): eigenvalues to 1e-10 and
+    residuals of the returned vectors."""
+    rng = np.random.default_rng(17)
+    norb, nbath = 2, 5
+    vk = np.zeros((norb, nbath))
+    vk[0, :3] = rng.uniform(0.1, 0.5, 3)
+    vk[1, 3:] = rng.uniform(0.1, 0.5, 2)
+    m = oracle.Model(norb, nbath, 3.0, 0.5, np.concatenate([[-2.0, -2.0], rng.uniform(-1, 1, nbath)]), vk)
+    b, ev_a, vec_a = oracle.sector_eigs(m, 3, 3, 6, dense_max=0)
+    _, ev_d, _ = oracle.sector_eigs(m, 3, 3, 6, dense_max=10**6)
+    assert b.ntot == 1225
+    assert np.abs(ev_a - ev_d).max() < 1e-10
+    for i in range(6):
+        r = oracle.multiply_H(m, b, vec_a[:, i]) - ev_a[i] * vec_a[:, i]
+        assert np.linalg.norm(r) < 1e-8
