@@ -117,11 +117,20 @@ int mo_ed_basis_get(mo_ed_ctx *ctx, int ne_up, int ne_down, long long n, const l
 int mo_ed_basis_idx(mo_ed_ctx *ctx, int ne_up, int ne_down, long long n,
                     const unsigned int *state, long long *idx);
 
-/* Device layout of a sector vector: ndown rows of nup elements (the
- * reference's order) with row stride *ld = roundup(nup, 32) elements, so
- * *nelem = ndown * ld; pad elements must be zero.  The *_dev entry points
- * take vectors in this layout; host entry points use the reference layout. */
+/* Device layout of a sector vector: ndown rows (down ranks in the
+ * reference's order) of row stride *ld elements (a multiple of 32), so
+ * *nelem = ndown * ld.  Within a row the up ranks are stored in conserved-
+ * block order: words with equal electron counts in every conserved subsystem
+ * (an impurity orbital with the bath levels it couples to) are contiguous,
+ * each block padded to a multiple of 4 columns.  mo_ed_vector_columns gives
+ * the column of every up rank; every other element is a pad and must be
+ * zero.  The *_dev entry points take vectors in this layout; host entry
+ * points use the reference layout (ed_basis.F90:120-123). */
 int mo_ed_vector_layout(mo_ed_ctx *ctx, int ne_up, int ne_down, int *ld, long long *nelem);
+/* col[iup-1] = 0-based device column of up rank iup (1..nup) in the layout
+ * above; capacity >= nup (no reference counterpart: the reference stores
+ * the sector vector in basis order). */
+int mo_ed_vector_columns(mo_ed_ctx *ctx, int ne_up, int ne_down, int *col, int capacity);
 
 /* ---- a6-a10: matrix-free H*v (ed_hamiltonian.F90:88-191 multiply_H) ------ */
 /* B = H*A on host FP64 arrays of ntot entries, computed on the FP64 device path. */
@@ -183,10 +192,13 @@ int mo_ed_lanczos_iteration(mo_ed_ctx *ctx, int ne_up, int ne_down, const double
  * MO_ED_ERR_CAPACITY.  The sector must have been prepared in the same
  * precision by an earlier mo_ed_lanczos_iteration, mo_ed_multiply_h_dev or
  * mo_ed_hv_tuning call (those build its tables and may allocate); otherwise
- * MO_ED_ERR_STATE.  The first call on a device looks up the region's address;
- * make it before any stream capture.  All calls share the region, which keeps
- * the previous call's contents (this call clears what must start at zero);
- * calls that overlap on the GPU race on it, so serialise them. */
+ * MO_ED_ERR_STATE.  mo_ed_create looks up the region's address on its
+ * device, which commits the region there before the host's pool takes the
+ * device; if that look-up failed, the first call on the device repeats it,
+ * so make that call before any stream capture.  A device reset after the
+ * look-up is not supported.  All calls share the region, which keeps the
+ * previous call's contents (this call clears what must start at zero); calls
+ * that overlap on the GPU race on it, so serialise them. */
 int mo_ed_lanczos_iteration_noalloc(mo_ed_ctx *ctx, int ne_up, int ne_down, const double *vec,
                                     int *nstep_calc, double *a, double *b);
 

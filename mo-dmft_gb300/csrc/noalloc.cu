@@ -37,8 +37,12 @@ std::mutex g_region_mu;
 void *g_region_addr[kNoAllocMaxDevices];
 
 // Device address of the region on the context's device; looked up once per
-// device, on the first call made on it (that device is current: every entry
-// point makes the context's device current).
+// device, with that device current.  mo_ed_create does the look-up, so the
+// region is committed on the device when the first context on it is created
+// (lazy module loading would otherwise load the module, and reserve the 32
+// MiB, on the first no-allocation call).  The cached address belongs to the
+// device's primary context: a device reset after the look-up is not
+// supported.
 int region_address(mo_ed_ctx *ctx, void **out)
 {
     if (ctx->device < 0 || ctx->device >= kNoAllocMaxDevices)
@@ -58,6 +62,15 @@ int region_address(mo_ed_ctx *ctx, void **out)
 }
 }  // namespace
 
+namespace moed {
+int noalloc_prepare(mo_ed_ctx *ctx)
+{
+    void *p = nullptr;
+    if (int rc = region_address(ctx, &p)) return rc;
+    return lanczos_region_preload(ctx);
+}
+}  // namespace moed
+
 using namespace moed;
 
 extern "C" {
@@ -74,10 +87,10 @@ int mo_ed_lanczos_iteration_noalloc(mo_ed_ctx *ctx, int ne_up, int ne_down, cons
     Sector s;
     if (int rc = find_sector(ctx, ne_up, ne_down, &s)) return rc;
     const int prec = ctx->opt.precision;
-    int v = 0, R = 0;
-    if (int rc = hv_lookup(ctx, s, prec == MO_ED_FP32 ? HV_F32 : HV_F64, &v, &R)) return rc;
+    int v = 0, nparts = 0;
+    if (int rc = hv_lookup(ctx, s, prec == MO_ED_FP32 ? HV_F32 : HV_F64, &v, &nparts)) return rc;
     const int nstep = ctx->opt.nstep;
-    const size_t need = lanczos_region_bytes(s, prec, nstep, R);
+    const size_t need = lanczos_region_bytes(s, prec, nstep, nparts);
     if (need > kNoAllocBytes)
         return fail(ctx, MO_ED_ERR_CAPACITY,
                     "sector needs " + std::to_string(need) + " bytes, the no-allocation region holds " +

@@ -36,18 +36,30 @@ def c3_model(pkg):
     return cfg, ek, vk
 
 
+def free_device_bytes():
+    import torch
+    torch.cuda.synchronize()
+    return torch.cuda.mem_get_info()[0]
+
+
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_noalloc_matches_lanczos_iteration(fresh, pkg, precision):
+    """Same a, b, nstep_calc as the allocating entry point on two calls in a
+    row, and no device memory taken by either call: the 32 MiB region was
+    committed when the context was created."""
     cfg, ek, vk = c3_model(pkg)
     fresh.set_options(precision=precision, nstep=60)
     fresh.set_model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
     nu = nd = 6
     D = fresh.sector_dims(nu, nd)[2]
     rng = np.random.default_rng(21)
+    vs = [rng.standard_normal(D) for _ in range(2)]
+    ref = [fresh.lanczos_iteration(nu, nd, v) for v in vs]   # also prepares the sector
     for call in range(2):
-        v = rng.standard_normal(D)
-        n0, a0, b0 = fresh.lanczos_iteration(nu, nd, v)   # also prepares the sector
-        n1, a1, b1 = fresh.lanczos_iteration_noalloc(nu, nd, v)
+        free0 = free_device_bytes()
+        n1, a1, b1 = fresh.lanczos_iteration_noalloc(nu, nd, vs[call])
+        assert free_device_bytes() == free0, call
+        n0, a0, b0 = ref[call]
         assert n1 == n0 == 60, call
         assert rel(a1, a0) < 1e-12 and rel(b1, b0) < 1e-12, (call, rel(a1, a0), rel(b1, b0))
         assert b1[0] == 0.0
