@@ -68,6 +68,12 @@ constexpr int kMaxCoef = 1 + 2 * kMaxHop;   // coupling table: 0, then +-V per c
 // schedule header (4 per 128-column chunk, one per column k = 0..3 of a quad).
 struct UpBlock {
     int col0, W4, hdr0, W;
+    // the block's gather schedule in 16-bit form (0 bytes when a target or a
+    // coupling index does not fit): offset in 16-byte units into
+    // Species::sched16 and size.  Layout: one word per (64-column chunk, k) =
+    // first entry (in entries from the first entry word) << 8 | slots, then
+    // the entries: target column | coupling index << 10.
+    int s16_off, s16_bytes, pad0, pad1;
 };
 
 // Row-set geometry of one down-spin block (host): at level j the rows are
@@ -78,8 +84,23 @@ struct DownBlock {
     int rs0[kMaxSub + 1];         // first row set of each level
     int rs_rows[kMaxSub + 1];     // rows per set at each level
     int nset[kMaxSub + 1];        // sets at each level
+    int blob_max[kMaxSub + 1];    // largest metadata blob of a set at each level (bytes)
     int cnt[kMaxSub];             // electrons per subsystem (block key)
 };
+
+// Metadata blob of one row set (16-byte aligned sections), copied into
+// shared memory with the tile:
+//   int4 header {rows g, byte offset of the moves, byte offset of the
+//                4-operator terms, total bytes}
+//   int4 info[g] {impurity pattern | moves in the set << 8 | moves to other
+//                 rows << 16 | 4-operator terms << 24, first move, first
+//                 4-operator term, row rank}
+//   double diag[g]    species diagonal of the row
+//   unsigned moves[]  row (index within the set for moves inside it, rank
+//                     otherwise) | coupling index << 16; moves inside the set first
+//   unsigned q4[]     4-operator terms: partner rank | pair << 16 | pair hop
+//                     << 21 | negative sign << 22 (spin-flip uses T_{j<-i},
+//                     pair hop T_{i<-j} of the row)
 
 struct Species {
     int nsite = 0, N = 0, n = 0;
@@ -95,13 +116,16 @@ struct Species {
     std::vector<UpBlock> h_ublk;
     std::vector<int> h_ublk_cnt;  // [nblk * kMaxSub] electrons per subsystem
     UpBlock *ublk = nullptr;
-    // gather schedule: header (block, 128-column chunk, k) = {first entry,
-    // slots}; entry (slot s, quad l) at first + 32*s + l = target column
-    // within the block | coupling index << 16 (index 0: no move, coupling 0).
-    // The 32 targets of one slot fall in 32 different shared-memory banks.
+    // gather schedule: header (block, 64-column chunk, k) = {first entry,
+    // slots}; entry (slot s, quad l) at first + 16*s + l = target column
+    // within the block | coupling index << 16 (index 0: no move, coupling 0)
+    // of column 4*l + k of the chunk.  The 16 targets of one slot are
+    // distinct mod 16: with shared-memory row pitches = 16 (mod 32), the two
+    // half-warps reading two rows hit 32 different banks.
     int2 *sched_hdr = nullptr;
     unsigned *sched_ent = nullptr;
     int sched_slots_max = 0;
+    unsigned char *sched16 = nullptr;   // 16-bit schedules of the blocks (UpBlock::s16_off)
     double *up_diag_d = nullptr;  // [ld] species diagonal per column (pads 0)
     float *up_diag_f = nullptr;
     unsigned char *up_imp = nullptr;  // [ld] impurity pattern per column
@@ -113,17 +137,9 @@ struct Species {
     int nrs = 0, nrec = 0;
     int2 *rs = nullptr;           // [nrs] {first row record, rows}
     int *rs_row = nullptr;        // [nrec] row (rank)
-    // [nrec] {impurity pattern | moves in the set << 8 | moves to other rows
-    // << 16 | 4-operator terms << 24, first move, first 4-operator term, 0}
-    int4 *rs_info = nullptr;
-    double *rs_diag_d = nullptr;  // [nrec] species diagonal of the row
-    float *rs_diag_f = nullptr;
-    // moves of a row: row (index within the set for moves inside it, rank
-    // otherwise) | coupling index << 16; moves inside the set first
-    unsigned *rs_mv = nullptr;
-    // 4-operator terms of a row: partner rank | pair << 16 | pair hop << 21 |
-    // negative sign << 22 (spin-flip uses T_{j<-i}, pair hop T_{i<-j} of the row)
-    unsigned *rs_q4 = nullptr;
+    int2 *rs_blob = nullptr;      // [nrs] {byte offset / 16, bytes} of the set's metadata blob
+    unsigned char *blob = nullptr;
+    std::vector<int2> h_rs, h_rs_blob;   // host copies (tile descriptors)
     ~Species();
 };
 
@@ -140,7 +156,9 @@ struct Sector {
 // ---------------------------------------------------------------------------
 // A tile: one row set of the down species times one up block.
 struct HvTile {
-    int rs, ub;
+    int rs0, rows, blob16, blob_bytes;   // row set: first row record, rows, metadata blob (16-byte units, bytes)
+    int col0, W4, hdr0, s16_off;         // up block (UpBlock fields)
+    int s16_bytes, ub, pad0, pad1;
 };
 
 template <typename TA>
@@ -155,15 +173,14 @@ struct HvJobT {
     const UpBlock *ublk;
     const int2 *sched_hdr;
     const unsigned *sched_ent;
+    const unsigned char *sched16;
     const TA *up_diag;
     const unsigned char *up_imp;
     const unsigned *up4;
     const int2 *rs;
     const int *rs_row;
-    const int4 *rs_info;
-    const TA *rs_diag;
-    const unsigned *rs_mv;
-    const unsigned *rs_q4;
+    const int2 *rs_blob;
+    const unsigned char *blob;
 };
 
 // ---------------------------------------------------------------------------
@@ -333,7 +350,7 @@ int hv_launch_f64(mo_ed_ctx *ctx, int kind, int v, const HvJobT<double> *jobs, i
 // capture), its number of dot-product partials (the grid size), and the tile
 // list of the sector.
 int hv_prepare(mo_ed_ctx *ctx, const Sector &s, int kind, int *v, int *nparts);
-// autotuner record of a shape: per variant (RG, NT, MINB, stage KB) and time in ms
+// autotuner record of a shape: per variant (RG, threads, MINB, stage rows) and time in ms
 int hv_tuning(mo_ed_ctx *ctx, const Sector &s, int kind, int cap, int *nvar, int *shape, float *ms, int *chosen);
 // tile list of variant v for a sector batched with the one v was tuned on
 int hv_prepare_rows(mo_ed_ctx *ctx, const Sector &s, int kind, int v);
@@ -344,8 +361,8 @@ int hv_lookup(mo_ed_ctx *ctx, const Sector &s, int kind, int *v, int *nparts);
 int hv_set_variant(mo_ed_ctx *ctx, const Sector &s, int kind, int v);
 // Convenience: one vector.
 int hv_single(mo_ed_ctx *ctx, const Sector &s, int kind, const void *x, void *y);
-// Tile list of a sector for a stage budget of `elems` elements (built once).
-int hv_tile_list(mo_ed_ctx *ctx, const Sector &s, int elems, const HvTile **tiles, int *ntiles);
+// Tile list of a sector for tile-shape variant v of `kind` (built once).
+int hv_tile_list(mo_ed_ctx *ctx, const Sector &s, int kind, int v, const HvTile **tiles, int *ntiles);
 
 // ---- Krylov (krylov.cu) -----------------------------------------------------
 int lanczos_reference(mo_ed_ctx *ctx, const Sector &s, const double *h_vec, int nstep,

@@ -47,17 +47,15 @@ Species::~Species()
     cudaFree(ublk);
     cudaFree(sched_hdr);
     cudaFree(sched_ent);
+    cudaFree(sched16);
     cudaFree(up_diag_d);
     cudaFree(up_diag_f);
     cudaFree(up_imp);
     cudaFree(up4);
     cudaFree(rs);
     cudaFree(rs_row);
-    cudaFree(rs_info);
-    cudaFree(rs_diag_d);
-    cudaFree(rs_diag_f);
-    cudaFree(rs_mv);
-    cudaFree(rs_q4);
+    cudaFree(rs_blob);
+    cudaFree(blob);
 }
 
 // ---------------------------------------------------------------------------
@@ -487,6 +485,7 @@ int get_species(mo_ed_ctx *ctx, int N, Species **out)
         u.W = W;
         u.W4 = (W + 3) & ~3;
         u.hdr0 = 0;
+        u.s16_off = u.s16_bytes = u.pad0 = u.pad1 = 0;
         col += u.W4;
     }
     s->ncol = col;
@@ -560,14 +559,16 @@ int get_species(mo_ed_ctx *ctx, int N, Species **out)
     std::vector<unsigned> ent;
     for (int b = 0; b < nblk; ++b) {
         UpBlock &u = s->h_ublk[b];
-        const int nq = u.W4 / 4, nch = (nq + 31) / 32;
+        const int nq = u.W4 / 4, nch = (nq + 15) / 16;
         u.hdr0 = (int)hdr.size();
         for (int ch = 0; ch < nch; ++ch)
             for (int k = 0; k < 4; ++k) {
+                // lanes: the 16 columns 4*l + k of the chunk; banks: target mod 32 (the
+                // two half-warps read two rows, which may then meet in a bank)
                 std::vector<int> el, eb, et, ec;
-                int ldeg[32] = {0}, bdeg[32] = {0};
-                for (int l = 0; l < 32; ++l) {
-                    const int c = 4 * (32 * ch + l) + k;
+                int ldeg[16] = {0}, bdeg[32] = {0};
+                for (int l = 0; l < 16; ++l) {
+                    const int c = 4 * (16 * ch + l) + k;
                     if (c >= u.W) continue;
                     const int r = s->h_rank_at[u.col0 + c];
                     for (const Hop &h : hops[r]) {
@@ -582,19 +583,20 @@ int get_species(mo_ed_ctx *ctx, int N, Species **out)
                     }
                 }
                 int delta = 0;
-                for (int t = 0; t < 32; ++t) delta = std::max(delta, std::max(ldeg[t], bdeg[t]));
+                for (int t = 0; t < 16; ++t) delta = std::max(delta, ldeg[t]);
+                for (int t = 0; t < 32; ++t) delta = std::max(delta, bdeg[t]);
                 std::vector<int> colour;
                 if (!el.empty()) colour_chunk(el, eb, delta, colour);
                 const int first = (int)ent.size();
-                ent.resize(ent.size() + (size_t)32 * delta, 0xffffffffu);
+                ent.resize(ent.size() + (size_t)16 * delta, 0xffffffffu);
                 std::vector<unsigned> used((size_t)delta, 0u);
                 for (size_t e = 0; e < el.size(); ++e) {
-                    ent[first + 32 * colour[e] + el[e]] = (unsigned)et[e] | ((unsigned)ec[e] << 16);
+                    ent[first + 16 * colour[e] + el[e]] = (unsigned)et[e] | ((unsigned)ec[e] << 16);
                     used[colour[e]] |= 1u << eb[e];
                 }
                 for (int sl = 0; sl < delta; ++sl)
-                    for (int l = 0; l < 32; ++l) {
-                        unsigned &x = ent[first + 32 * sl + l];
+                    for (int l = 0; l < 16; ++l) {
+                        unsigned &x = ent[first + 16 * sl + l];
                         if (x != 0xffffffffu) continue;
                         // no move: read a bank no other lane of the slot uses
                         int t = -1;
@@ -604,7 +606,7 @@ int get_species(mo_ed_ctx *ctx, int N, Species **out)
                                 used[sl] |= 1u << bb;
                                 break;
                             }
-                        if (t < 0) t = std::min(4 * (32 * ch + l) + k, u.W4 - 1);
+                        if (t < 0) t = std::min(4 * (16 * ch + l) + k, u.W4 - 1);
                         x = (unsigned)t;
                     }
                 hdr.push_back(make_int2(first, delta));
@@ -612,16 +614,39 @@ int get_species(mo_ed_ctx *ctx, int N, Species **out)
             }
     }
 
-    // ---- down-spin role: row sets at every level ----
+    // 16-bit copies of the block schedules (staged into shared memory by the
+    // H*v kernel) where every target and coupling index fits
+    std::vector<unsigned char> s16;
+    for (int b = 0; b < nblk; ++b) {
+        UpBlock &u = s->h_ublk[b];
+        const int nh = (u.W4 / 4 + 15) / 16 * 4;
+        if (u.W4 > 1024 || 2 * m.ncpl + 1 > 64) continue;
+        const int e0 = hdr[u.hdr0].x;
+        const int e1 = hdr[u.hdr0 + nh - 1].x + 16 * hdr[u.hdr0 + nh - 1].y;
+        const size_t bytes = ((size_t)4 * nh + 2 * (size_t)(e1 - e0) + 15) & ~(size_t)15;
+        std::vector<unsigned char> bl(bytes, 0);
+        for (int h = 0; h < nh; ++h) {
+            const unsigned w = ((unsigned)(hdr[u.hdr0 + h].x - e0) << 8) | (unsigned)hdr[u.hdr0 + h].y;
+            memcpy(&bl[4 * h], &w, 4);
+        }
+        for (int e = e0; e < e1; ++e) {
+            const unsigned x = ent[e];
+            const unsigned short v = (unsigned short)((x & 0xffffu) | ((x >> 16) << 10));
+            memcpy(&bl[4 * nh + 2 * (size_t)(e - e0)], &v, 2);
+        }
+        u.s16_off = (int)(s16.size() / 16);
+        u.s16_bytes = (int)bytes;
+        s16.insert(s16.end(), bl.begin(), bl.end());
+    }
+
+    // ---- down-spin role: row sets at every level, with their metadata blobs ----
     s->h_dblk.assign(nblk, DownBlock());
     std::vector<std::vector<int>> members(nblk);
     for (int r = 0; r < n; ++r) members[blk_of[r]].push_back(r);
-    std::vector<int2> rsv;
+    std::vector<int2> rsv, rblob;
     std::vector<int> rrow;
-    std::vector<int4> rinfo;
-    std::vector<double> rdd;
-    std::vector<float> rdf;
-    std::vector<unsigned> rmv, rq4;
+    std::vector<unsigned char> blob;
+    auto a16 = [](size_t v) { return (v + 15) & ~(size_t)15; };
     for (int b = 0; b < nblk; ++b) {
         DownBlock &db = s->h_dblk[b];
         db.size = (int)members[b].size();
@@ -642,12 +667,7 @@ int get_species(mo_ed_ctx *ctx, int N, Species **out)
             db.rs0[j] = (int)rsv.size();
             db.nset[j] = nset;
             db.rs_rows[j] = rows;
-            const int rec0 = (int)rrow.size();
-            for (int q = 0; q < nset; ++q) rsv.push_back(make_int2(rec0 + q * rows, rows));
-            rrow.resize(rrow.size() + (size_t)nset * rows, -1);
-            rinfo.resize(rrow.size());
-            rdd.resize(rrow.size());
-            rdf.resize(rrow.size());
+            db.blob_max[j] = 0;
             // set index / index in the set of a word of this block
             auto place = [&](unsigned w, int *set, int *row) {
                 int sv = 0, rv = 0;
@@ -659,51 +679,76 @@ int get_species(mo_ed_ctx *ctx, int N, Species **out)
                 *set = sv;
                 *row = rv;
             };
+            std::vector<int> at((size_t)nset * rows, -1);
             for (int r : members[b]) {
-                const unsigned w = (unsigned)s->h_words[r];
                 int sv, rv;
-                place(w, &sv, &rv);
-                const int rec = rec0 + sv * rows + rv;
-                rrow[rec] = r;
-                rdd[rec] = diag[r];
-                rdf[rec] = (float)diag[r];
-                const int mv0 = (int)rmv.size();
-                int nin = 0, nopen = 0;
-                for (const Hop &h : hops[r])
-                    if (inpos[h.sub] >= j) {
-                        int s2, r2;
-                        place((unsigned)s->h_words[h.tgt], &s2, &r2);
-                        rmv.push_back((unsigned)r2 | ((unsigned)h.cidx << 16));
-                        ++nin;
-                    }
-                for (const Hop &h : hops[r])
-                    if (inpos[h.sub] < j) {
-                        rmv.push_back((unsigned)h.tgt | ((unsigned)h.cidx << 16));
-                        ++nopen;
-                    }
-                const int q0 = (int)rq4.size();
-                int n4 = 0;
-                if (four)
-                    for (int i = 0; i < norb; ++i)
-                        for (int jj = 0; jj < norb; ++jj) {
-                            if (i == jj) continue;
-                            const int p = pidx[i][jj];
-                            unsigned w2;
-                            int neg;
-                            // spin-flip: the down spin moves i -> j (T_{j<-i})
-                            if (transfer(w, jj, i, &w2, &neg)) {
-                                rq4.push_back((unsigned)rank[w2] | ((unsigned)p << 16) | ((unsigned)neg << 22));
-                                ++n4;
-                            }
-                            // pair hopping: the down spin moves j -> i (T_{i<-j})
-                            if (transfer(w, i, jj, &w2, &neg)) {
-                                rq4.push_back((unsigned)rank[w2] | ((unsigned)p << 16) | (1u << 21) |
-                                              ((unsigned)neg << 22));
-                                ++n4;
-                            }
+                place((unsigned)s->h_words[r], &sv, &rv);
+                at[(size_t)sv * rows + rv] = r;
+            }
+            for (int q = 0; q < nset; ++q) {
+                const int rec0 = (int)rrow.size();
+                rsv.push_back(make_int2(rec0, rows));
+                std::vector<int4> info(rows);
+                std::vector<double> dg(rows);
+                std::vector<unsigned> mvs, q4s;
+                for (int rv = 0; rv < rows; ++rv) {
+                    const int r = at[(size_t)q * rows + rv];
+                    if (r < 0) return fail(ctx, MO_ED_ERR_ARG, "row set with a missing row");
+                    rrow.push_back(r);
+                    const unsigned w = (unsigned)s->h_words[r];
+                    dg[rv] = diag[r];
+                    const int mv0 = (int)mvs.size();
+                    int nin = 0, nopen = 0;
+                    for (const Hop &h : hops[r])
+                        if (inpos[h.sub] >= j) {
+                            int s2, r2;
+                            place((unsigned)s->h_words[h.tgt], &s2, &r2);
+                            mvs.push_back((unsigned)r2 | ((unsigned)h.cidx << 16));
+                            ++nin;
                         }
-                rinfo[rec] = make_int4((int)(w & (unsigned)(m.nimp - 1)) | (nin << 8) | (nopen << 16) | (n4 << 24),
-                                       mv0, q0, 0);
+                    for (const Hop &h : hops[r])
+                        if (inpos[h.sub] < j) {
+                            mvs.push_back((unsigned)h.tgt | ((unsigned)h.cidx << 16));
+                            ++nopen;
+                        }
+                    const int q0 = (int)q4s.size();
+                    int n4 = 0;
+                    if (four)
+                        for (int i = 0; i < norb; ++i)
+                            for (int jj = 0; jj < norb; ++jj) {
+                                if (i == jj) continue;
+                                const int p = pidx[i][jj];
+                                unsigned w2;
+                                int neg;
+                                // spin-flip: the down spin moves i -> j (T_{j<-i})
+                                if (transfer(w, jj, i, &w2, &neg)) {
+                                    q4s.push_back((unsigned)rank[w2] | ((unsigned)p << 16) | ((unsigned)neg << 22));
+                                    ++n4;
+                                }
+                                // pair hopping: the down spin moves j -> i (T_{i<-j})
+                                if (transfer(w, i, jj, &w2, &neg)) {
+                                    q4s.push_back((unsigned)rank[w2] | ((unsigned)p << 16) | (1u << 21) |
+                                                  ((unsigned)neg << 22));
+                                    ++n4;
+                                }
+                            }
+                    info[rv] = make_int4((int)(w & (unsigned)(m.nimp - 1)) | (nin << 8) | (nopen << 16) | (n4 << 24),
+                                         mv0, q0, r);
+                }
+                const size_t off_info = 16, off_diag = off_info + 16 * (size_t)rows;
+                const size_t off_mv = a16(off_diag + 8 * (size_t)rows);
+                const size_t off_q4 = a16(off_mv + 4 * mvs.size());
+                const size_t total = a16(off_q4 + 4 * q4s.size());
+                const size_t base = blob.size();
+                blob.resize(base + total, 0);
+                const int4 head = make_int4(rows, (int)off_mv, (int)off_q4, (int)total);
+                memcpy(&blob[base], &head, 16);
+                memcpy(&blob[base + off_info], info.data(), 16 * (size_t)rows);
+                memcpy(&blob[base + off_diag], dg.data(), 8 * (size_t)rows);
+                if (!mvs.empty()) memcpy(&blob[base + off_mv], mvs.data(), 4 * mvs.size());
+                if (!q4s.empty()) memcpy(&blob[base + off_q4], q4s.data(), 4 * q4s.size());
+                rblob.push_back(make_int2((int)(base / 16), (int)total));
+                db.blob_max[j] = std::max(db.blob_max[j], (int)total);
             }
         }
     }
@@ -730,13 +775,14 @@ int get_species(mo_ed_ctx *ctx, int N, Species **out)
     if (int rc = upload_vec(ctx, &s->up_diag_f, updf)) return rc;
     if (int rc = upload_vec(ctx, &s->up_imp, upimp)) return rc;
     if (int rc = upload_vec(ctx, &s->up4, up4)) return rc;
+    if (blob.size() / 16 > (size_t)0x7fffffff) return fail(ctx, MO_ED_ERR_ARG, "row-set metadata too large");
+    s->h_rs = rsv;
+    s->h_rs_blob = rblob;
+    if (int rc = upload_vec(ctx, &s->sched16, s16)) return rc;
     if (int rc = upload_vec(ctx, &s->rs, rsv)) return rc;
     if (int rc = upload_vec(ctx, &s->rs_row, rrow)) return rc;
-    if (int rc = upload_vec(ctx, &s->rs_info, rinfo)) return rc;
-    if (int rc = upload_vec(ctx, &s->rs_diag_d, rdd)) return rc;
-    if (int rc = upload_vec(ctx, &s->rs_diag_f, rdf)) return rc;
-    if (int rc = upload_vec(ctx, &s->rs_mv, rmv)) return rc;
-    if (int rc = upload_vec(ctx, &s->rs_q4, rq4)) return rc;
+    if (int rc = upload_vec(ctx, &s->rs_blob, rblob)) return rc;
+    if (int rc = upload_vec(ctx, &s->blob, blob)) return rc;
     MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     *out = s.get();
     ctx->species[N] = std::move(s);
