@@ -46,13 +46,13 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic(variant):
-    """DRAM bytes of one H*v with the given tuner variant of the block-tiled
-    kernel from the committed ncu summary, or None."""
+def profile_traffic(kind):
+    """DRAM bytes of one H*v with the given kernel kind (hv_tuning's fourth
+    field) from the committed ncu summary, or None."""
     p = os.path.join(ROOT, "profiles", "hv_c4_traffic.json")
     if os.path.exists(p):
         with open(p) as f:
-            return json.load(f).get("by_variant", {}).get(str(variant))
+            return json.load(f).get("by_kind", {}).get(str(kind))
     return None
 
 
@@ -145,6 +145,11 @@ def cpu_baseline_sample(cfg, nup, ndn, seconds=3.0):
     dt = time.perf_counter() - t0
     return dict(value=2.0 * done * 8 / dt / 1e9, unit="GB/s", cores=os.cpu_count(), kind="port",
                 sample=f"{done} of {b.ntot} rows of one FP64 H*v (oracle C port, OpenMP over rows), {dt:.2f} s")
+
+
+# H*v kernel of each tile-shape variant kind (hv_tuning's fourth field)
+KERNEL_NAMES = {0: "k_hv", 1: "k_hv_async", 2: "k_hv_down (128-byte slices) + k_hv_async<split>",
+                3: "k_hv_down (64-byte slices) + k_hv_async<split>"}
 
 
 def lanczos_g(pkg, name, nev, precisions=("fp32", "fp32+g64", "fp64")):
@@ -278,11 +283,9 @@ def run_ours(args):
         s.hv_set_variant(nup, ndn, args.hv_variant, pkg.FP32)
     nu_, nd_, D = s.sector_dims(nup, ndn)
     ld, nelem = s.vector_layout(nup, ndn)
-    # device layout: nd rows of stride ld (128-byte aligned rows), up ranks at
-    # their conserved-block columns, zero pads
-    cols = torch.from_numpy(s.vector_columns(nup, ndn).astype(np.int64)).cuda()
+    # device layout: nd rows of stride ld (128-byte aligned rows), zero pads
     x = torch.zeros((nd_, ld), dtype=torch.float32, device="cuda")
-    x[:, cols] = torch.randn((nd_, nu_), dtype=torch.float32, device="cuda",
+    x[:, :nu_] = torch.randn((nd_, nu_), dtype=torch.float32, device="cuda",
                              generator=torch.Generator("cuda").manual_seed(rank))
     y = torch.empty_like(x)
 
@@ -317,7 +320,7 @@ def run_ours(args):
 
     # end to end through the C-ABI with pinned host buffers
     xh = torch.empty(D, dtype=torch.float32, pin_memory=True)
-    xh.copy_(x[:, cols].reshape(-1).cpu())
+    xh.copy_(x[:, :nu_].reshape(-1).cpu())
     xn = xh.numpy()
     yn = torch.empty(D, dtype=torch.float32, pin_memory=True).numpy()
     import ctypes
@@ -338,11 +341,11 @@ def run_ours(args):
     # the e2e output equals the device-resident result
     step()
     torch.cuda.synchronize()
-    assert np.array_equal(yn, y[:, cols].reshape(-1).cpu().numpy()), "e2e result differs from the device path"
+    assert np.array_equal(yn, y[:, :nu_].reshape(-1).cpu().numpy()), "e2e result differs from the device path"
 
 
     tuning, chosen = s.hv_tuning(nup, ndn, pkg.FP32)
-    traffic = profile_traffic(chosen)
+    traffic = profile_traffic(tuning[chosen][0][3])
     def guarded(fn, *a):
         # a secondary measurement that fails is reported in the line instead of
         # taking the headline number down with it
@@ -378,10 +381,9 @@ def run_ours(args):
                     "h2d_bytes_per_step": D * 4, "d2h_bytes_per_step": D * 4,
                     "ms_per_step": round(t_e2e * 1e3, 4)},
             "gpu_launches": launches,
-            "hv_autotune": {"kernel": "k_hvt (block-tiled, one pass)",
-                            "variants": [{"rows_per_thread": v[0][0], "threads": v[0][1], "ctas_per_sm": v[0][2],
-                                          "stage_kb": v[0][3], "ms": round(v[1], 4)} for v in tuning],
-                            "chosen": chosen},
+            "hv_autotune": {"variants": [{"rows_per_item": v[0][0], "threads": v[0][1], "ctas_per_sm": v[0][2],
+                                          "kernel": KERNEL_NAMES[v[0][3]],
+                                          "ms": round(v[1], 4)} for v in tuning], "chosen": chosen},
             "clocks": clocks,
             "lanczos_g": lg,
             "fit": fit,

@@ -117,20 +117,11 @@ int mo_ed_basis_get(mo_ed_ctx *ctx, int ne_up, int ne_down, long long n, const l
 int mo_ed_basis_idx(mo_ed_ctx *ctx, int ne_up, int ne_down, long long n,
                     const unsigned int *state, long long *idx);
 
-/* Device layout of a sector vector: ndown rows (down ranks in the
- * reference's order) of row stride *ld elements (a multiple of 32), so
- * *nelem = ndown * ld.  Within a row the up ranks are stored in conserved-
- * block order: words with equal electron counts in every conserved subsystem
- * (an impurity orbital with the bath levels it couples to) are contiguous,
- * each block padded to a multiple of 4 columns.  mo_ed_vector_columns gives
- * the column of every up rank; every other element is a pad and must be
- * zero.  The *_dev entry points take vectors in this layout; host entry
- * points use the reference layout (ed_basis.F90:120-123). */
+/* Device layout of a sector vector: ndown rows of nup elements (the
+ * reference's order) with row stride *ld = roundup(nup, 32) elements, so
+ * *nelem = ndown * ld; pad elements must be zero.  The *_dev entry points
+ * take vectors in this layout; host entry points use the reference layout. */
 int mo_ed_vector_layout(mo_ed_ctx *ctx, int ne_up, int ne_down, int *ld, long long *nelem);
-/* col[iup-1] = 0-based device column of up rank iup (1..nup) in the layout
- * above; capacity >= nup (no reference counterpart: the reference stores
- * the sector vector in basis order). */
-int mo_ed_vector_columns(mo_ed_ctx *ctx, int ne_up, int ne_down, int *col, int capacity);
 
 /* ---- a6-a10: matrix-free H*v (ed_hamiltonian.F90:88-191 multiply_H) ------ */
 /* B = H*A on host FP64 arrays of ntot entries, computed on the FP64 device path. */

@@ -1,6 +1,5 @@
 // context.cu -- context lifecycle, configuration and the C-ABI entry points
 // for the basis, H*v and apply_c.
-#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -47,106 +46,21 @@ int ensure(mo_ed_ctx *ctx, DevBuf &b, size_t bytes)
     return dev_alloc(ctx, b, bytes);
 }
 
-// reference layout (D contiguous, up rank fastest) -> device layout: every
-// device element, pads included, is written (pads zero)
-template <typename TI, typename TO>
-__global__ void k_to_dev(const TI *__restrict__ ref, TO *__restrict__ dev, int nu, int ld, long long n,
-                         const int *__restrict__ rank_at)
+int upload_padded(mo_ed_ctx *ctx, const Sector &s, const void *host, void *dev, size_t es)
 {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const long long d = i / ld;
-        const int c = (int)(i - d * ld);
-        const int r = rank_at[c];
-        dev[i] = r >= 0 ? (TO)ref[d * nu + r] : TO(0);
-    }
-}
-
-// device layout -> reference layout
-template <typename T>
-__global__ void k_to_ref(const T *__restrict__ dev, T *__restrict__ ref, int nu, int ld, long long n,
-                         const int *__restrict__ pos)
-{
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const long long d = i / nu;
-        const int u = (int)(i - d * nu);
-        ref[i] = dev[d * ld + pos[u]];
-    }
-}
-
-static unsigned perm_grid(const mo_ed_ctx *ctx, long long n)
-{
-    return (unsigned)std::max(1LL, std::min((n + 255) / 256, (long long)ctx->num_sms * 16));
-}
-
-int to_device_layout(mo_ed_ctx *ctx, const Sector &s, const void *ref, void *dev, size_t es)
-{
-    const long long n = s.Dpad();
-    if (n == 0) return MO_ED_OK;
-    if (es == sizeof(float))
-        k_to_dev<float, float><<<perm_grid(ctx, n), 256, 0, ctx->stream>>>((const float *)ref, (float *)dev,
-                                                                           s.up->n, s.ld(), n, s.up->rank_at);
-    else
-        k_to_dev<double, double><<<perm_grid(ctx, n), 256, 0, ctx->stream>>>((const double *)ref, (double *)dev,
-                                                                             s.up->n, s.ld(), n, s.up->rank_at);
-    MOED_CHECK_LAUNCH(ctx);
+    const size_t nu = s.up->n, ld = s.ld(), nd = s.dn->n;
+    if (ld > nu)
+        MOED_CUDA(ctx, cudaMemset2DAsync((char *)dev + nu * es, ld * es, 0, (ld - nu) * es, nd, ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpy2DAsync(dev, ld * es, host, nu * es, nu * es, nd, cudaMemcpyHostToDevice,
+                                     ctx->stream));
     return MO_ED_OK;
 }
 
-int to_device_layout_f64_f32(mo_ed_ctx *ctx, const Sector &s, const double *ref, float *dev)
+int download_padded(mo_ed_ctx *ctx, const Sector &s, const void *dev, void *host, size_t es)
 {
-    const long long n = s.Dpad();
-    if (n == 0) return MO_ED_OK;
-    k_to_dev<double, float><<<perm_grid(ctx, n), 256, 0, ctx->stream>>>(ref, dev, s.up->n, s.ld(), n,
-                                                                        s.up->rank_at);
-    MOED_CHECK_LAUNCH(ctx);
-    return MO_ED_OK;
-}
-
-int to_reference_layout(mo_ed_ctx *ctx, const Sector &s, const void *dev, void *ref, size_t es)
-{
-    const long long n = s.D();
-    if (n == 0) return MO_ED_OK;
-    if (es == sizeof(float))
-        k_to_ref<float><<<perm_grid(ctx, n), 256, 0, ctx->stream>>>((const float *)dev, (float *)ref, s.up->n,
-                                                                    s.ld(), n, s.up->pos);
-    else
-        k_to_ref<double><<<perm_grid(ctx, n), 256, 0, ctx->stream>>>((const double *)dev, (double *)ref, s.up->n,
-                                                                     s.ld(), n, s.up->pos);
-    MOED_CHECK_LAUNCH(ctx);
-    return MO_ED_OK;
-}
-
-int upload_padded(mo_ed_ctx *ctx, const Sector &s, const void *host, void *dev, size_t es, void *stage)
-{
-    const size_t bytes = es * (size_t)s.D();
-    if (!stage) {
-        if (int rc = ensure(ctx, ctx->stage, bytes)) return rc;
-        stage = ctx->stage.p;
-    }
-    if (bytes) MOED_CUDA(ctx, cudaMemcpyAsync(stage, host, bytes, cudaMemcpyHostToDevice, ctx->stream));
-    return to_device_layout(ctx, s, stage, dev, es);
-}
-
-int upload_f64_to_f32(mo_ed_ctx *ctx, const Sector &s, const double *host, float *dev, void *stage)
-{
-    const size_t bytes = sizeof(double) * (size_t)s.D();
-    if (!stage) {
-        if (int rc = ensure(ctx, ctx->stage, bytes)) return rc;
-        stage = ctx->stage.p;
-    }
-    if (bytes) MOED_CUDA(ctx, cudaMemcpyAsync(stage, host, bytes, cudaMemcpyHostToDevice, ctx->stream));
-    return to_device_layout_f64_f32(ctx, s, (const double *)stage, dev);
-}
-
-int download_padded(mo_ed_ctx *ctx, const Sector &s, const void *dev, void *host, size_t es, void *stage)
-{
-    const size_t bytes = es * (size_t)s.D();
-    if (!stage) {
-        if (int rc = ensure(ctx, ctx->stage, bytes)) return rc;
-        stage = ctx->stage.p;
-    }
-    if (int rc = to_reference_layout(ctx, s, dev, stage, es)) return rc;
-    if (bytes) MOED_CUDA(ctx, cudaMemcpyAsync(host, stage, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    const size_t nu = s.up->n, ld = s.ld(), nd = s.dn->n;
+    MOED_CUDA(ctx, cudaMemcpy2DAsync(host, nu * es, dev, ld * es, nu * es, nd, cudaMemcpyDeviceToHost,
+                                     ctx->stream));
     return MO_ED_OK;
 }
 
@@ -322,16 +236,6 @@ int mo_ed_vector_layout(mo_ed_ctx *ctx, int ne_up, int ne_down, int *ld, long lo
     if (int rc = get_sector(ctx, ne_up, ne_down, &s)) return rc;
     if (ld) *ld = s.ld();
     if (nelem) *nelem = s.Dpad();
-    return MO_ED_OK;
-}
-
-int mo_ed_vector_columns(mo_ed_ctx *ctx, int ne_up, int ne_down, int *col, int capacity)
-{
-    CTX_CHECK(ctx);
-    Sector s;
-    if (int rc = get_sector(ctx, ne_up, ne_down, &s)) return rc;
-    if (!col || capacity < s.up->n) return fail(ctx, MO_ED_ERR_CAPACITY, "col capacity below nup");
-    std::copy(s.up->h_pos.begin(), s.up->h_pos.end(), col);
     return MO_ED_OK;
 }
 

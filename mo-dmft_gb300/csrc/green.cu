@@ -24,22 +24,22 @@ namespace moed {
 // element with the operator's sign; zero where the operator annihilates the
 // state (ed_operators.F90:44-58).
 template <typename T>
-__global__ void k_apply_c_up(const T *__restrict__ x, T *__restrict__ y, int ld_out, int nd, int ld_in,
-                             const int *__restrict__ out_words, const int *__restrict__ out_rank_at,
-                             const int *__restrict__ in_rank, const int *__restrict__ in_pos, int bit, int pm)
+__global__ void k_apply_c_up(const T *__restrict__ x, T *__restrict__ y, int nu_out, int ld_out, int nd,
+                             int ld_in, const int *__restrict__ out_words, const int *__restrict__ in_rank,
+                             int bit, int pm)
 {
     const long long n = (long long)ld_out * nd;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
+        const int u = (int)(i % ld_out);
         const long long d = i / ld_out;
-        const int u = out_rank_at[i - d * ld_out];
         T v = T(0);
-        if (u >= 0) {
+        if (u < nu_out) {
             const unsigned w = (unsigned)out_words[u];
             const bool occ = (w >> bit) & 1u;
             if ((pm == 1) == occ) {
                 const int sgn = __popc(w & ((1u << bit) - 1u)) & 1;
-                const int j = in_pos[in_rank[w ^ (1u << bit)]];
+                const int j = in_rank[w ^ (1u << bit)];
                 const T src = x[d * ld_in + j];
                 v = sgn ? -src : src;
             }
@@ -49,10 +49,9 @@ __global__ void k_apply_c_up(const T *__restrict__ x, T *__restrict__ y, int ld_
 }
 
 // spin down: the sign also counts every up-spin bit (bitidx = nsite + iorb - 1),
-// i.e. a factor (-1)^(N_up) on top of the down-word parity.  Columns (up
-// ranks) are unchanged; pads of the source are zero.
+// i.e. a factor (-1)^(N_up) on top of the down-word parity.
 template <typename T>
-__global__ void k_apply_c_dn(const T *__restrict__ x, T *__restrict__ y, int ld, int nd_out,
+__global__ void k_apply_c_dn(const T *__restrict__ x, T *__restrict__ y, int nu, int ld, int nd_out,
                              const int *__restrict__ out_words, const int *__restrict__ in_rank,
                              int bit, int pm, int up_parity)
 {
@@ -64,7 +63,7 @@ __global__ void k_apply_c_dn(const T *__restrict__ x, T *__restrict__ y, int ld,
         const unsigned w = (unsigned)out_words[d];
         const bool occ = (w >> bit) & 1u;
         T v = T(0);
-        if ((pm == 1) == occ) {
+        if (u < nu && (pm == 1) == occ) {
             const int sgn = (__popc(w & ((1u << bit) - 1u)) + up_parity) & 1;
             const int j = in_rank[w ^ (1u << bit)];
             const T src = x[(long long)j * ld + u];
@@ -84,21 +83,19 @@ int apply_c_dev(mo_ed_ctx *ctx, const Sector &in, const Sector &out, int prec, c
     const int bit = iorb - 1;
     if (ispin == 1) {
         if (prec == MO_ED_FP32)
-            k_apply_c_up<float><<<g, T, 0, ctx->stream>>>((const float *)x, (float *)y, out.ld(), out.dn->n, in.ld(),
-                                                         out.up->words, out.up->rank_at, in.up->rank, in.up->pos,
-                                                         bit, pm);
+            k_apply_c_up<float><<<g, T, 0, ctx->stream>>>((const float *)x, (float *)y, out.up->n, out.ld(),
+                                                         out.dn->n, in.ld(), out.up->words, in.up->rank, bit, pm);
         else
-            k_apply_c_up<double><<<g, T, 0, ctx->stream>>>((const double *)x, (double *)y, out.ld(), out.dn->n,
-                                                          in.ld(), out.up->words, out.up->rank_at, in.up->rank,
-                                                          in.up->pos, bit, pm);
+            k_apply_c_up<double><<<g, T, 0, ctx->stream>>>((const double *)x, (double *)y, out.up->n, out.ld(),
+                                                          out.dn->n, in.ld(), out.up->words, in.up->rank, bit, pm);
     } else {
         const int upar = out.ne_up & 1;
         if (prec == MO_ED_FP32)
-            k_apply_c_dn<float><<<g, T, 0, ctx->stream>>>((const float *)x, (float *)y, out.ld(), out.dn->n,
-                                                         out.dn->words, in.dn->rank, bit, pm, upar);
+            k_apply_c_dn<float><<<g, T, 0, ctx->stream>>>((const float *)x, (float *)y, out.up->n, out.ld(),
+                                                         out.dn->n, out.dn->words, in.dn->rank, bit, pm, upar);
         else
-            k_apply_c_dn<double><<<g, T, 0, ctx->stream>>>((const double *)x, (double *)y, out.ld(), out.dn->n,
-                                                          out.dn->words, in.dn->rank, bit, pm, upar);
+            k_apply_c_dn<double><<<g, T, 0, ctx->stream>>>((const double *)x, (double *)y, out.up->n, out.ld(),
+                                                          out.dn->n, out.dn->words, in.dn->rank, bit, pm, upar);
     }
     MOED_CHECK_LAUNCH(ctx);
     return MO_ED_OK;

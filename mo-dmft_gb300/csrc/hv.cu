@@ -1,44 +1,44 @@
 // hv.cu -- matrix-free Kanamori H*v on a (Nup, Ndn) sector.
 //
 // Replaces multiply_H (ed_hamiltonian.F90:88-191).  For output element
-// (d, u) (down rank d, up rank u) the reference sums
+// (d, u) (down rank d, up rank u, X[d][u]) the reference sums
 //   diagonal       onsite + dens_dens                      (:112-141)
 //   hybridisation  V c+_o c_k and V c+_k c_o, both spins     (:146-161)
 //   spin-flip      -J c+_{i up} c_{i dn} c+_{j dn} c_{j up}  (:163-174)
 //   pair hop       -J c+_{i up} c+_{i dn} c_{j up} c_{j dn}  (:176-187)
 // gathering A at the state each operator maps row (d, u) to.  Here:
-//   * diagonal = Dup[u] + Ddn[d] + Cross[imp(u)][imp(d)];
-//   * up-spin hops move inside the up block of u (conserved subsystem
-//     counts), i.e. inside one contiguous column range of a row;
-//   * down-spin hops are row AXPYs from rows d' of the same down block;
+//   * diagonal = Dup[u] + Ddn[d] + Cross[imp(u)][imp(d)] (tables.cu);
+//   * up-spin hops gather X[d][u'] for the precomputed moves (u', +-V) of u;
+//   * down-spin hops are whole-row AXPYs from rows d';
 //   * spin-flip / pair hop factor into an up-spin transfer T_{i<-j}(u) and a
 //     down-spin transfer (T_{j<-i}(d) for spin-flip, T_{i<-j}(d) for pair
 //     hopping) with coefficient +J t_up t_dn: reordering the four operators
 //     of ed_operators.F90:183-213 / 236-266 gives a factor -1 that cancels
-//     the -J.
+//     the -J.  Both transfers stay inside a bath group (rank offsets that
+//     depend only on the impurity bits).
 //
-// Work decomposition.  A tile is one row set of the down species (rows of a
-// down block with equal local states in its leading subsystems, so the moves
-// of the trailing subsystems stay inside the set) times one whole up block.
-// One persistent kernel walks the tiles of a batch of jobs (vectors of
-// possibly different sectors).  Per tile:
-//   * one warp issues a cp.async.bulk copy per row segment (the block's
-//     columns of one row) into a shared-memory stage, completing on an
-//     mbarrier; the next tile's copies run while the current tile computes
-//     (two stages);
-//   * a thread owns 4 consecutive columns (a quad) of up to RG rows; a warp
-//     covers 32 quads of one row group, or for narrow blocks several row
-//     groups of fewer quads;
-//   * up-spin moves read the stage through the block's gather schedule
-//     (edge-coloured so the 32 lanes of a slot hit 32 banks), one schedule
-//     entry serving all RG rows;
-//   * down-spin moves inside the set read the stage (16-byte loads of the
-//     quad), the others read the neighbour row from global memory (L2: the
-//     tiles of one block pair run together), as do spin-flip / pair hopping;
-//   * optionally the FP64 sum of x*y (the Lanczos alpha) is accumulated per
-//     CTA and job.
-// HBM traffic is one read of x and one write of y; the CTAs also zero the
-// row tails past the last block (pads).
+// Work decomposition (both kernels).  An item is up to R rows made of whole
+// down-spin bath groups, so the partner rows of spin-flip / pair hopping are
+// in the item.  Items are ordered by the bath occupations of the conserved
+// subsystems, so the down-spin neighbours of the rows in flight stay
+// L2-resident.  A kernel walks a batch of jobs (vectors of possibly different
+// sectors) so that all excitation vectors of a Lanczos step share one launch;
+// optionally each item writes the FP64 partial of x*y for the Lanczos alpha.
+//
+// k_hv (first design): a CTA stages its rows in shared memory transposed,
+// S[u][r], by blocking loads; one shared load of S[u'] serves the up-spin move
+// u -> u' for all rows of the item.  Each thread owns 4 consecutive columns:
+// 16-byte global loads for the down-spin row AXPYs and 16-byte stores of y
+// (rows are padded to a 128-byte stride); its column moves come from a
+// chunk-major table, one contiguous block per slot.
+//
+// k_hv_async (below): double-buffered asynchronous stage, conflict-free
+// scheduled up-spin gathers, precomputed item descriptors.
+//
+// Split (below): k_hv_down computes the down-spin hybridisation over
+// down-spin blocks x column slices from shared memory, then k_hv_async<SPLIT>
+// adds the other terms.  The autotuner picks among all of them per
+// (precision, sector).
 #include <algorithm>
 
 #include "internal.h"
@@ -46,896 +46,1412 @@
 namespace moed {
 
 constexpr int kMaxJobs = 24;
-constexpr long long kTuneMinElems = 1 << 18;
 
 template <typename TA>
 struct HvBatch {
-    int njobs, total;
-    int *err;
+    int njobs, total_items;
     HvJobT<TA> job[kMaxJobs];
 };
 
-// ---------------------------------------------------------------------------
-// PTX helpers: mbarrier and bulk global->shared copies
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(unsigned long long *b, unsigned count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_tx(unsigned long long *b, unsigned bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try(unsigned long long *b, unsigned parity)
-{
-    unsigned ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(b)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *b)
-{
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(b))
-                 : "memory");
-}
-
-__device__ __forceinline__ unsigned long long global_ns()
-{
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-// ---------------------------------------------------------------------------
-// 4-element loads and stores
-// ---------------------------------------------------------------------------
 template <typename T>
-__device__ __forceinline__ void lds4(const T *p, T (&v)[4])
-{
-    if constexpr (sizeof(T) == 4) {
-        const float4 a = *reinterpret_cast<const float4 *>(p);
-        v[0] = a.x;
-        v[1] = a.y;
-        v[2] = a.z;
-        v[3] = a.w;
-    } else {
-        const double2 a = reinterpret_cast<const double2 *>(p)[0];
-        const double2 b = reinterpret_cast<const double2 *>(p)[1];
-        v[0] = a.x;
-        v[1] = a.y;
-        v[2] = b.x;
-        v[3] = b.y;
-    }
-}
+struct alignas(16) Vec4 {
+    T v[4];
+};
+
+template <typename T, int R>
+struct alignas(8) RowVec {
+    T v[R];
+};
+
+// Spin-flip / pair-hop terms of one (row, column impurity pattern) pair: at
+// most 2 for up to three orbitals.  Term t reads the staged partner row
+// src[t] at column u + du[t] with coefficient c[t] (+-J with both transfer
+// signs folded in).
+template <typename TA>
+struct alignas(16) Quad {
+    int cnt;
+    signed char du[2];
+    unsigned char src[2];
+    TA c[2];
+};
 
 template <typename T>
-__device__ __forceinline__ void ldcg4(const T *p, T (&v)[4])
+__device__ __forceinline__ Vec4<T> ldg4(const T *p)
 {
-    if constexpr (sizeof(T) == 4) {
-        const float4 a = __ldcg(reinterpret_cast<const float4 *>(p));
-        v[0] = a.x;
-        v[1] = a.y;
-        v[2] = a.z;
-        v[3] = a.w;
-    } else {
-        const double2 a = __ldcg(reinterpret_cast<const double2 *>(p));
-        const double2 b = __ldcg(reinterpret_cast<const double2 *>(p) + 1);
-        v[0] = a.x;
-        v[1] = a.y;
-        v[2] = b.x;
-        v[3] = b.y;
-    }
-}
-
-template <typename T>
-__device__ __forceinline__ void ldg4(const T *p, T (&v)[4])
-{
+    Vec4<T> r;
     if constexpr (sizeof(T) == 4) {
         const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
-        v[0] = a.x;
-        v[1] = a.y;
-        v[2] = a.z;
-        v[3] = a.w;
+        r.v[0] = a.x;
+        r.v[1] = a.y;
+        r.v[2] = a.z;
+        r.v[3] = a.w;
     } else {
         const double2 a = __ldg(reinterpret_cast<const double2 *>(p));
         const double2 b = __ldg(reinterpret_cast<const double2 *>(p) + 1);
-        v[0] = a.x;
-        v[1] = a.y;
-        v[2] = b.x;
-        v[3] = b.y;
+        r.v[0] = a.x;
+        r.v[1] = a.y;
+        r.v[2] = b.x;
+        r.v[3] = b.y;
     }
+    return r;
 }
 
-template <typename T, typename TA>
-__device__ __forceinline__ void stg4(T *p, const TA (&v)[4])
+__device__ __forceinline__ int4 ldg_i4(const int *p) { return __ldg(reinterpret_cast<const int4 *>(p)); }
+
+template <typename T>
+__device__ __forceinline__ void stg4(T *p, const T (&v)[4])
 {
     if constexpr (sizeof(T) == 4) {
-        *reinterpret_cast<float4 *>(p) = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
+        *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
     } else {
-        reinterpret_cast<double2 *>(p)[0] = make_double2((double)v[0], (double)v[1]);
-        reinterpret_cast<double2 *>(p)[1] = make_double2((double)v[2], (double)v[3]);
+        reinterpret_cast<double2 *>(p)[0] = make_double2(v[0], v[1]);
+        reinterpret_cast<double2 *>(p)[1] = make_double2(v[2], v[3]);
     }
 }
 
-// Shared-memory row pitch of a tile with W4 columns: W4 rounded up to 16 (mod
-// 32), so that two half-warps reading two consecutive rows at 16 distinct
-// (mod 16) columns hit 32 different banks.  Tiles of 64..1024 columns (the
-// fast path) all use the fixed pitch kPit, which turns the row offsets of a
-// thread into immediates.
-constexpr int kPit = 1040;
-constexpr int kFastMinW4 = 64, kFastMaxW4 = 1024;
-constexpr int kSeg = 4;           // consecutive tiles per CTA turn
-constexpr int kNBuf = 2;
-constexpr int kMaxCW = 32;        // consumer warps at most (dot-product slots)
-
-__host__ __device__ inline int tile_pitch(int W4)
-{
-    return (W4 >= kFastMinW4 && W4 <= kFastMaxW4) ? kPit : W4 + ((48 - (W4 & 31)) & 31);
-}
-
-struct TileDesc {             // one per stage buffer, written by the producer warp
-    int job, g, W4, col0, hdr0, pitch, on, flags;   // flags: 1 schedule staged, 2 partner columns staged
-};
-
-struct StageSizes {           // bytes per stage buffer of each region; consumer warps
-    int stage, meta, up4, s16, ncw;
-};
-
+// the 4 moves of slot s of one 4-column chunk
 template <typename TA>
-struct SmemLayout {
-    size_t stage, meta, up4, s16, desc, cf, cross, dot, bar, total;
-};
-
-template <typename TA>
-__host__ __device__ inline SmemLayout<TA> smem_layout(const StageSizes &Z, int nimp)
+__device__ __forceinline__ void ld_moves(const HopEnt<TA> *p, HopEnt<TA> (&e)[4])
 {
-    SmemLayout<TA> L;
-    size_t o = 0;
-    L.stage = o;
-    o += (size_t)kNBuf * Z.stage;
-    L.meta = o;
-    o += (size_t)kNBuf * Z.meta;
-    L.up4 = o;
-    o += (size_t)kNBuf * Z.up4;
-    L.s16 = o;
-    o += (size_t)kNBuf * Z.s16;
-    L.desc = o;
-    o += kNBuf * sizeof(TileDesc);
-    L.cf = o;
-    o += ((size_t)kMaxCoef * sizeof(TA) + 15) & ~(size_t)15;
-    L.cross = o;
-    o += ((size_t)nimp * nimp * sizeof(TA) + 15) & ~(size_t)15;
-    L.dot = o;
-    o += sizeof(double) * kMaxJobs * Z.ncw;
-    L.bar = o;
-    o += 2 * kNBuf * sizeof(unsigned long long);
-    L.total = o;
-    return L;
-}
-
-__device__ __forceinline__ void mbar_expect_tx(unsigned long long *b, unsigned bytes)
-{
-    asm volatile("mbarrier.expect_tx.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(unsigned long long *b)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
-}
-
-// Wait for a phase; false when the wait ran out (about 2 s): the error word
-// is set and the caller leaves its loop.
-__device__ __forceinline__ bool bar_wait(unsigned long long *bar, unsigned parity, int *err)
-{
-    int spins = 0;
-    unsigned long long t0 = 0;
-    while (!mbar_try(bar, parity)) {
-        ++spins;
-        if (spins == 32) {
-            t0 = global_ns();
-        } else if (spins > 32 && (spins & 31) == 0 && global_ns() - t0 > 2000000000ull) {
-            if (err) atomicExch(err, 1);
-            return false;
+    if constexpr (sizeof(TA) == 4) {
+        const int4 a = __ldg(reinterpret_cast<const int4 *>(p));
+        const int4 b = __ldg(reinterpret_cast<const int4 *>(p) + 1);
+        e[0].t = a.x;
+        e[0].v = __int_as_float(a.y);
+        e[1].t = a.z;
+        e[1].v = __int_as_float(a.w);
+        e[2].t = b.x;
+        e[2].v = __int_as_float(b.y);
+        e[3].t = b.z;
+        e[3].v = __int_as_float(b.w);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int4 a = __ldg(reinterpret_cast<const int4 *>(p + k));
+            e[k].t = a.x;
+            e[k].v = __hiloint2double(a.w, a.z);
         }
     }
-    return true;
 }
 
+template <typename TX, typename TA, typename TY, int R, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+k_hv(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict__ mdl)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int npair = mdl->npair, nimp = mdl->nimp;
+    int ldmax = 0;
+    for (int i = 0; i < batch.njobs; ++i) ldmax = max(ldmax, batch.job[i].ld);
+    // dynamic shared memory: staged rows transposed, S[u] = row values of
+    // column u; then the interspecies diagonal and the 4-operator table
+    RowVec<TX, R> *S = reinterpret_cast<RowVec<TX, R> *>(smem_raw);
+    TA *s_cross = reinterpret_cast<TA *>(smem_raw + ((sizeof(RowVec<TX, R>) * (size_t)ldmax + 15) & ~(size_t)15));
+    int *s_t4 = reinterpret_cast<int *>(s_cross + nimp * nimp);
+
+    __shared__ unsigned s_pmask[kMaxImp];
+    __shared__ RowVec<TA, R> s_crossT[kMaxImp];   // per item: cross[iu][id_r] for the R rows
+    __shared__ int s_d[R], s_id[R], s_dcnt[R];
+    __shared__ TA s_ddiag[R];
+    __shared__ int s_dtgt[R][kMaxHop];
+    __shared__ TA s_dval[R][kMaxHop];
+    // per (row, pair): spin-flip / pair-hop partner as an item slot (>= 0) or
+    // as -(1 + global row) when the partner row is not staged, and the
+    // coefficient +-J; s_sfm[r] / s_phm[r]: pairs valid for row r
+    __shared__ unsigned s_sfm[R], s_phm[R];
+    __shared__ unsigned s_rowmask[kMaxPair];   // generic path: bit r spin-flip, bit 16+r pair hop
+    __shared__ unsigned s_itemmask;
+    __shared__ Quad<TA> s_q[R * kMaxImp];      // fast path table
+    __shared__ int s_slow;                     // 1: an item needs the generic path
+    __shared__ int s_sfsrc[R][kMaxPair], s_phsrc[R][kMaxPair];
+    __shared__ TA s_sfc[R][kMaxPair], s_phc[R][kMaxPair];
+    __shared__ double s_red[NT / 32];
+
+    const int tid = threadIdx.x;
+    for (int i = tid; i < npair * nimp; i += NT) s_t4[i] = mdl->t4[i];
+    for (int i = tid; i < nimp; i += NT) s_pmask[i] = mdl->pairmask[i];
+    for (int i = tid; i < nimp * nimp; i += NT) s_cross[i] = (TA)mdl->cross[i];
+    const TA Jc = (TA)mdl->J;
+
+    for (int item = blockIdx.x; item < batch.total_items; item += gridDim.x) {
+        int j = 0;
+        while (j + 1 < batch.njobs && item >= batch.job[j + 1].item0) ++j;
+        const HvJobT<TA> &jb = batch.job[j];
+        if (jb.active && *jb.active == 0) continue;
+        const int it = item - jb.item0;
+        const int nd = jb.nd, ld = jb.ld, nchunk = ld >> 2;
+        const TX *__restrict__ x = (const TX *)jb.x;
+        TY *__restrict__ y = (TY *)jb.y;
+
+        __syncthreads();  // the previous item is done with S and the row tables
+        if (tid < R) {
+            const int r = tid;
+            const int d = jb.items[it * R + r];
+            if (d >= 0) {
+                const int inf = jb.dn_info[d];
+                s_d[r] = d;
+                s_id[r] = (inf >> 8) & 0xff;
+                s_dcnt[r] = inf & 0xff;
+                s_ddiag[r] = jb.dn_diag[d];
+            } else {
+                s_d[r] = -1;
+                s_id[r] = 0;
+                s_dcnt[r] = 0;
+                s_ddiag[r] = TA(0);
+            }
+            s_sfm[r] = 0u;
+            s_phm[r] = 0u;
+        }
+        for (int p = tid; p < kMaxPair; p += NT) s_rowmask[p] = 0u;
+        if (tid == 0) {
+            s_itemmask = 0u;
+            s_slow = 0;
+        }
+        __syncthreads();
+        for (int i = tid; i < nimp * R; i += NT) {
+            const int iu = i / R, r = i - iu * R;
+            s_crossT[iu].v[r] = s_cross[iu * nimp + s_id[r]];
+        }
+        for (int i = tid; i < R * jb.dn_maxcnt; i += NT) {
+            const int r = i / jb.dn_maxcnt, s = i - r * jb.dn_maxcnt;
+            if (s < s_dcnt[r]) {
+                s_dtgt[r][s] = jb.dn_tgt[(size_t)s * nd + s_d[r]];
+                s_dval[r][s] = jb.dn_val[(size_t)s * nd + s_d[r]];
+            }
+        }
+        if (tid < R * npair) {
+            const int r = tid / npair, p = tid - r * npair;
+            if (s_d[r] >= 0) {
+                const int esf = s_t4[mdl->pair_rev[p] * nimp + s_id[r]];   // spin-flip: T_{j<-i}(d)
+                const int eph = s_t4[p * nimp + s_id[r]];                  // pair hop:  T_{i<-j}(d)
+                if (esf < 0) {
+                    const int off = (int)(short)(esf & 0xffff), dp = s_d[r] + off, rp = r + off;
+                    const bool local = rp >= 0 && rp < R && s_d[rp] == dp;
+                    s_sfsrc[r][p] = local ? rp : -(1 + dp);
+                    s_sfc[r][p] = (esf & 0x40000000) ? -Jc : Jc;
+                    atomicOr(&s_sfm[r], 1u << p);
+                    atomicOr(&s_rowmask[p], 1u << r);
+                    atomicOr(&s_itemmask, 1u << p);
+                    if (!local) s_slow = 1;
+                }
+                if (eph < 0) {
+                    const int off = (int)(short)(eph & 0xffff), dp = s_d[r] + off, rp = r + off;
+                    const bool local = rp >= 0 && rp < R && s_d[rp] == dp;
+                    s_phsrc[r][p] = local ? rp : -(1 + dp);
+                    s_phc[r][p] = (eph & 0x40000000) ? -Jc : Jc;
+                    atomicOr(&s_phm[r], 1u << p);
+                    atomicOr(&s_rowmask[p], 1u << (16 + r));
+                    atomicOr(&s_itemmask, 1u << p);
+                    if (!local) s_slow = 1;
+                }
+            }
+        }
+        __syncthreads();
+        // fast-path table: terms of every (row, column impurity pattern)
+        for (int i = tid; i < R * nimp; i += NT) {
+            const int r = i / nimp, iu = i - r * nimp;
+            Quad<TA> q;
+            q.cnt = 0;
+#pragma unroll
+            for (int t = 0; t < 2; ++t) {
+                q.du[t] = 0;
+                q.src[t] = 0;
+                q.c[t] = TA(0);
+            }
+            if (s_d[r] >= 0) {
+                for (int p = 0; p < npair; ++p) {
+                    const int e = s_t4[p * nimp + iu];
+                    if (e >= 0) continue;
+                    const int du = (int)(short)(e & 0xffff);
+                    const TA tu = (e & 0x40000000) ? TA(-1) : TA(1);
+                    if ((s_sfm[r] >> p) & 1u) {
+                        if (q.cnt == 2) s_slow = 1;
+                        else {
+                            q.du[q.cnt] = (signed char)du;
+                            q.src[q.cnt] = (unsigned char)max(s_sfsrc[r][p], 0);
+                            q.c[q.cnt] = tu * s_sfc[r][p];
+                            ++q.cnt;
+                        }
+                    }
+                    if ((s_phm[r] >> p) & 1u) {
+                        if (q.cnt == 2) s_slow = 1;
+                        else {
+                            q.du[q.cnt] = (signed char)du;
+                            q.src[q.cnt] = (unsigned char)max(s_phsrc[r][p], 0);
+                            q.c[q.cnt] = tu * s_phc[r][p];
+                            ++q.cnt;
+                        }
+                    }
+                }
+            }
+            s_q[i] = q;
+        }
+        // stage the rows, transposed (pad rows staged as zeros)
+        for (int c = tid; c < nchunk; c += NT) {
+            Vec4<TX> v[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int d = jb.items[it * R + r];
+                if (d >= 0) {
+                    v[r] = ldg4(x + (size_t)d * ld + 4 * c);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) v[r].v[k] = TX(0);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                RowVec<TX, R> t;
+#pragma unroll
+                for (int r = 0; r < R; ++r) t.v[r] = v[r].v[k];
+                S[4 * c + k] = t;
+            }
+        }
+        __syncthreads();
+
+        // item-uniform row data in registers
+        TA ddiag[R];
+        bool live[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            ddiag[r] = s_ddiag[r];
+            live[r] = s_d[r] >= 0;
+        }
+        const bool slow = s_slow != 0;
+        const bool want_dot = jb.dot_partial != nullptr;
+        const unsigned imask = s_itemmask;
+        double dacc = 0.0;
+        int4 nx_inf = tid < nchunk ? ldg_i4(jb.up_info + 4 * tid) : make_int4(0, 0, 0, 0);
+        Vec4<TA> nx_ud = tid < nchunk ? ldg4(jb.up_diag + 4 * tid) : Vec4<TA>{};
+        for (int c = tid; c < nchunk; c += NT) {
+            const int u0 = 4 * c;
+            const int4 inf4 = nx_inf;
+            const Vec4<TA> ud = nx_ud;
+            if (c + NT < nchunk) {   // prefetch the next chunk's column data
+                nx_inf = ldg_i4(jb.up_info + u0 + 4 * NT);
+                nx_ud = ldg4(jb.up_diag + u0 + 4 * NT);
+            }
+            const int inf[4] = {inf4.x, inf4.y, inf4.z, inf4.w};
+            TA acc[4][R];
+            int cnt[4], iu[4];
+            int maxc = 0;
+            // diagonal
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                iu[k] = (inf[k] >> 8) & 0xff;
+                cnt[k] = inf[k] & 0xff;
+                maxc = max(maxc, cnt[k]);
+                const RowVec<TX, R> sx = S[u0 + k];
+                const RowVec<TA, R> cr = s_crossT[iu[k]];
+#pragma unroll
+                for (int r = 0; r < R; ++r) acc[k][r] = (ud.v[k] + ddiag[r] + cr.v[r]) * (TA)sx.v[r];
+            }
+            // up-spin hybridisation: shared-memory gathers, all rows at once
+            // The moves of SB slots are loaded together so that their L2
+            // latencies overlap; a gather is issued only for a column's own
+            // moves (no shared-memory traffic for padded slots).
+            constexpr int SB = R > 4 ? 2 : 4;
+            const HopEnt<TA> *tab = jb.up_tab + (size_t)c * jb.up_hw * 4;
+            for (int s0 = 0; s0 < maxc; s0 += SB) {
+                HopEnt<TA> e[SB][4];
+#pragma unroll
+                for (int t = 0; t < SB; ++t) {
+                    if (s0 + t < maxc) ld_moves<TA>(tab + (size_t)(s0 + t) * 4, e[t]);
+                }
+#pragma unroll
+                for (int t = 0; t < SB; ++t) {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        if (s0 + t < cnt[k]) {
+                            const RowVec<TX, R> g = S[e[t][k].t];
+#pragma unroll
+                            for (int r = 0; r < R; ++r) acc[k][r] += e[t][k].v * (TA)g.v[r];
+                        }
+                    }
+                }
+            }
+            // down-spin hybridisation: row AXPYs (16-byte loads)
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int n = s_dcnt[r];
+#pragma unroll 4
+                for (int s = 0; s < n; ++s) {
+                    const TA v = s_dval[r][s];
+                    const Vec4<TX> g = ldg4(x + (size_t)s_dtgt[r][s] * ld + u0);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) acc[k][r] += v * (TA)g.v[k];
+                }
+            }
+            // spin-flip and pair hopping (partner rows are in the stage)
+            if (!slow) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        const Quad<TA> q = s_q[r * nimp + iu[k]];
+#pragma unroll
+                        for (int t = 0; t < 2; ++t)
+                            if (t < q.cnt)
+                                acc[k][r] += q.c[t] * (TA)reinterpret_cast<const TX *>(&S[u0 + k + q.du[t]])[q.src[t]];
+                    }
+                }
+            } else {
+                // generic: pairs valid for this column and for some row of the item
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    unsigned pm = s_pmask[iu[k]] & imask;
+                    while (pm) {
+                        const int p = __ffs(pm) - 1;
+                        pm &= pm - 1;
+                        const int e = s_t4[p * nimp + iu[k]];
+                        const int uu = u0 + k + (int)(short)(e & 0xffff);
+                        const bool neg = (e & 0x40000000) != 0;
+                        const unsigned rm = s_rowmask[p];
+                        const TX *su = reinterpret_cast<const TX *>(&S[uu]);
+#pragma unroll
+                        for (int r = 0; r < R; ++r) {
+                            if ((rm >> r) & 1u) {
+                                const int src = s_sfsrc[r][p];
+                                const TX xv = src >= 0 ? su[src] : __ldg(x + (size_t)(-1 - src) * ld + uu);
+                                const TA cf = neg ? -s_sfc[r][p] : s_sfc[r][p];
+                                acc[k][r] += cf * (TA)xv;
+                            }
+                            if ((rm >> (16 + r)) & 1u) {
+                                const int src = s_phsrc[r][p];
+                                const TX xv = src >= 0 ? su[src] : __ldg(x + (size_t)(-1 - src) * ld + uu);
+                                const TA cf = neg ? -s_phc[r][p] : s_phc[r][p];
+                                acc[k][r] += cf * (TA)xv;
+                            }
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                if (live[r]) {
+                    TY o[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) o[k] = (TY)acc[k][r];
+                    stg4(y + (size_t)s_d[r] * ld + u0, o);
+                }
+            }
+            if (want_dot) {   // x (re-read from the stage) . y of this chunk
+                TA part = TA(0);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const RowVec<TX, R> sx = S[u0 + k];
+#pragma unroll
+                    for (int r = 0; r < R; ++r) part += (TA)sx.v[r] * (TA)(TY)acc[k][r];
+                }
+                dacc += (double)part;
+            }
+        }
+        if (jb.dot_partial) {
+            for (int off = 16; off > 0; off >>= 1) dacc += __shfl_down_sync(0xffffffffu, dacc, off);
+            if ((tid & 31) == 0) s_red[tid >> 5] = dacc;
+            __syncthreads();
+            if (tid == 0) {
+                double t = 0.0;
+                for (int w = 0; w < NT / 32; ++w) t += s_red[w];
+                jb.dot_partial[it] = t;
+            }
+        }
+    }
+}
+
+template <typename TX, typename TA, int R>
+static size_t dyn_smem_bytes(int ld, const ModelDev &m)
+{
+    return ((sizeof(RowVec<TX, R>) * (size_t)ld + 15) & ~(size_t)15) + sizeof(TA) * (size_t)m.nimp * m.nimp +
+           sizeof(int) * (size_t)m.npair * m.nimp;
+}
+
+// ---------------------------------------------------------------------------
+// staged variant (k_hv_async)
+// ---------------------------------------------------------------------------
+// The same sum per element, organised for latency hiding and few instructions:
+//   * stage layout [tile][r][32]: column u of staged row r sits at
+//     ((u >> 5) * R + r) * 32 + (u & 31).  The R values of a column are 32
+//     elements apart, so one address serves every row (immediate offsets),
+//     and column u is in bank u mod 32 for every row;
+//   * the rows of the next item and its descriptor (the row data k_hv
+//     computes per item: row indices, down-spin moves, interspecies diagonal,
+//     spin-flip / pair-hop terms; built once by k_item_desc) are copied
+//     (cp.async, 16 bytes per thread, L2 only) into the second of two stage
+//     buffers while the current item is computed: two barriers per item;
+//   * warp w owns chunks c = w + NW * (kHvCh * i + q) (32 columns each, one
+//     column per lane), so every global load and store of a warp covers one
+//     128-byte line and the kHvCh chunks of an iteration share their address
+//     arithmetic (immediate offsets);
+//   * up-spin moves follow the conflict-free schedule (species_sched): the
+//     entries hold the stage offset of the target, one bank-conflict-free
+//     shared load per staged row and slot, no predication;
+//   * down-spin row AXPYs: one row offset per move serves the kHvCh chunks.
+constexpr int kHvCh = 4;
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all_but_newest() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
 template <typename TA>
-__device__ __forceinline__ int find_job(const HvBatch<TA> &B, int t)
+__device__ __forceinline__ int hv_find_job(const HvBatch<TA> &b, int item)
 {
     int j = 0;
-    while (j + 1 < B.njobs && t >= B.job[j + 1].tile0) ++j;
+    while (j + 1 < b.njobs && item >= b.job[j + 1].item0) ++j;
     return j;
 }
 
-// Quads per warp row (log2) and row slots of a tile: the fast path covers 32
-// quads (two 16-quad schedule chunks, one per half-warp) of the same rows, so
-// the per-row loops are warp-uniform; other tiles use 16 quads x 2 rows, or
-// spread narrower tiles over more rows.
-__host__ __device__ inline int tile_lqw(int nq, bool fast)
+// next item of this CTA at or after `from` (stride gridDim.x) whose job is active
+template <typename TA>
+__device__ __forceinline__ int hv_next_item(const HvBatch<TA> &b, int from)
 {
-    if (fast) return 5;
-    if (nq >= 16) return 4;
-    int l = 0;
-    while ((1 << l) < nq) ++l;
-    return l;
+    for (int item = from; item < b.total_items; item += gridDim.x) {
+        const HvJobT<TA> &jb = b.job[hv_find_job(b, item)];
+        if (!jb.active || *jb.active != 0) return item;
+    }
+    return -1;
 }
 
-// One warp task: a chunk of quads times a batch of rows of the tile in
-// stage S (pitch P; FAST: P == kPit and two half-warps per row pair).
-template <bool FAST, typename TX, typename TA, typename TY, int RG>
-__device__ __forceinline__ double hv_task_body(const HvJobT<TA> &jb, const TileDesc &D, const TX *__restrict__ S,
-                                          const unsigned char *__restrict__ meta,
-                                          const unsigned *__restrict__ up4s, const unsigned char *__restrict__ s16,
-                                          const TA *__restrict__ s_cf, const TA *__restrict__ s_cross, int nimp,
-                                          TA Jc, int task, int lane, bool want_dot)
-{
-    const int W4 = D.W4, nq = W4 >> 2, g = D.g, ld = jb.ld;
-    const int P = FAST ? kPit : D.pitch;
-    const int lqw = tile_lqw(nq, FAST);
-    const int qw = 1 << lqw, rs = 32 >> lqw;
-    const int nch = (nq + qw - 1) >> lqw;
-    const int ch = task % nch, rb = task / nch;
-    const int ql = lane & (qw - 1), slot = lane >> lqw;
-    // schedule chunk (16 quads) and lane within it
-    const int sch = FAST ? 2 * ch + (lane >> 4) : ch, sql = FAST ? (lane & 15) : ql;
-    const int q = (ch << lqw) + ql;
-    const bool act = q < nq;
-    const int c = act ? 4 * q : 0;
-    const int rbase = rb * rs * RG + slot;
-    const int4 *info = reinterpret_cast<const int4 *>(meta + 16);
-    const double *dgv = reinterpret_cast<const double *>(meta + 16 + 16 * (size_t)g);
-    const int4 mh = *reinterpret_cast<const int4 *>(meta);
-    const unsigned *mv = reinterpret_cast<const unsigned *>(meta + mh.y);
-    const unsigned *q4 = reinterpret_cast<const unsigned *>(meta + mh.z);
-    const TX *__restrict__ x = (const TX *)jb.x;
-    TY *__restrict__ y = (TY *)jb.y;
-
-    // column tables of the quad (consumed after the up-spin moves, so their
-    // latency overlaps them)
-    TA dup[4];
-    ldg4<TA>(jb.up_diag + D.col0 + c, dup);
-    const unsigned imq = __ldg(reinterpret_cast<const unsigned *>(jb.up_imp + D.col0 + c));
-    // rows r_i = rbase + rs*i; row pointers at offsets roff[i] from Sb
-    // (FAST: compile-time offsets; invalid rows read inside the stage and
-    // are not stored)
-    const TX *Sb = S + (size_t)rbase * P;
-    int roff[RG];
-    unsigned vmask = 0;
-    TA acc[RG][4];
-#pragma unroll
-    for (int i = 0; i < RG; ++i) {
-        const int r = rbase + rs * i;
-        const bool ok = act && r < g;
-        vmask |= ok ? 1u << i : 0u;
-        roff[i] = FAST ? i * kPit : ((ok ? r : 0) - rbase) * P;
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk) acc[i][kk] = TA(0);
-    }
-    // first open-move loads of row 0, issued before the up-spin moves so that
-    // their L2 latency overlaps them; row i+1's are issued once row i's are
-    // consumed
-    constexpr int OPB = sizeof(TA) == 8 ? 2 : 4;
-    const TX *xc = x + D.col0 + c;
-    TX ov[OPB][4];
-    auto issue_open = [&](int i, TX (&o)[OPB][4]) {
-        const int r = rbase + rs * i;
-        const bool ok = (vmask >> i) & 1u;
-        const int4 inf = info[ok ? r : 0];
-        const int nin = (inf.x >> 8) & 0xff, nopen = ok ? (inf.x >> 16) & 0xff : 0;
-        const unsigned *m1 = mv + inf.y + nin;
-#pragma unroll
-        for (int t = 0; t < OPB; ++t) {
-            if (t < nopen) {
-                ldcg4<TX>(xc + (size_t)(m1[t] & 0xffffu) * ld, o[t]);
-            } else {
-#pragma unroll
-                for (int kk = 0; kk < 4; ++kk) o[t][kk] = TX(0);
-            }
-        }
-    };
-    issue_open(0, ov);
-    // up-spin moves: one schedule entry per slot serves every row
-    if (FAST && (D.flags & 1)) {
-        // 16-bit schedule staged in shared memory
-        const int nch16 = (nq + 15) >> 4;
-        const unsigned *sh = reinterpret_cast<const unsigned *>(s16);
-        const unsigned short *se = reinterpret_cast<const unsigned short *>(s16 + 16 * (size_t)nch16);
-        const bool live = sch < nch16;
-        // one column of the quad at a time on acc[.][0]; the columns rotate
-        // after each, so the loop body exists once
-#pragma unroll 1
-        for (int kk = 0; kk < 4; ++kk) {
-            const unsigned hw = live ? sh[sch * 4 + kk] : 0u;
-            const int ns = hw & 255;
-            const unsigned short *E = se + (hw >> 8) + sql;
-            for (int sl = 0; sl < ns; sl += 4) {
-#pragma unroll
-                for (int t = 0; t < 4; ++t) {
-                    if (sl + t < ns) {
-                        const unsigned e = E[16 * (sl + t)];
-                        const TA cf = s_cf[e >> 10];
-                        const TX *col = Sb + (e & 1023u);
-#pragma unroll
-                        for (int i = 0; i < RG; ++i) acc[i][0] += cf * (TA)col[roff[i]];
-                    }
-                }
-            }
-#pragma unroll
-            for (int i = 0; i < RG; ++i) {
-                const TA a0 = acc[i][0];
-                acc[i][0] = acc[i][1];
-                acc[i][1] = acc[i][2];
-                acc[i][2] = acc[i][3];
-                acc[i][3] = a0;
-            }
-        }
-    } else {
-        const int nch16 = (nq + 15) >> 4;
-        const bool live = sch < nch16;
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-            const int2 h = live ? __ldg(jb.sched_hdr + D.hdr0 + sch * 4 + kk) : make_int2(0, 0);
-            const unsigned *E = jb.sched_ent + h.x + sql;
-            for (int sl = 0; sl < h.y; sl += 8) {
-                unsigned e[8];
-#pragma unroll
-                for (int t = 0; t < 8; ++t) e[t] = sl + t < h.y ? __ldg(E + 16 * (sl + t)) : 0u;
-#pragma unroll
-                for (int t = 0; t < 8; ++t) {
-                    if (sl + t < h.y) {
-                        const TA cf = s_cf[e[t] >> 16];
-                        const TX *col = Sb + (e[t] & 0xffffu);
-#pragma unroll
-                        for (int i = 0; i < RG; ++i) acc[i][kk] += cf * (TA)col[roff[i]];
-                    }
-                }
-            }
-        }
-    }
-    // diagonal, down-spin moves, 4-operator terms, store
-    int iu[4];
-#pragma unroll
-    for (int kk = 0; kk < 4; ++kk) iu[kk] = (imq >> (8 * kk)) & 0xff;
-    double dsum = 0.0;
-    // rows in a runtime loop on acc[0], rotating acc after each row (register
-    // moves), so the per-row code exists once in the kernel
-#pragma unroll 1
-    for (int i = 0; i < RG; ++i) {
-        const bool ok = (vmask >> i) & 1u;
-        const int r = rbase + rs * i;
-        const int4 inf = info[ok ? r : 0];
-        const int nin = (inf.x >> 8) & 0xff, nopen = (inf.x >> 16) & 0xff, n4 = (inf.x >> 24) & 0xff;
-        const unsigned *m0 = mv + inf.y;
-        const unsigned *m1 = m0 + nin;
-        TA a[4];
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk) a[kk] = acc[0][kk];
-        // the prefetched open moves of this row
-        if (ok) {
-#pragma unroll
-            for (int t = 0; t < OPB; ++t)
-                if (t < nopen) {
-                    const TA cf = s_cf[m1[t] >> 16];
-#pragma unroll
-                    for (int kk = 0; kk < 4; ++kk) a[kk] += cf * (TA)ov[t][kk];
-                }
-        }
-        if (i + 1 < RG) issue_open(i + 1, ov);
-        if (ok) {
-            const TX *xrow = S + (size_t)r * P + c;
-            {
-                const TA ddn = (TA)dgv[r];
-                const int id = inf.x & 0xff;
-                TX xs[4];
-                lds4<TX>(xrow, xs);
-#pragma unroll
-                for (int kk = 0; kk < 4; ++kk) a[kk] += (dup[kk] + ddn + s_cross[iu[kk] * nimp + id]) * (TA)xs[kk];
-            }
-            for (int m = 0; m < nin; ++m) {
-                const unsigned e = m0[m];
-                const TA cf = s_cf[e >> 16];
-                TX v[4];
-                lds4<TX>(S + (size_t)(e & 0xffffu) * P + c, v);
-#pragma unroll
-                for (int kk = 0; kk < 4; ++kk) a[kk] += cf * (TA)v[kk];
-            }
-            for (int m = OPB; m < nopen; ++m) {
-                TX v[4];
-                ldcg4<TX>(xc + (size_t)(m1[m] & 0xffffu) * ld, v);
-                const TA cf = s_cf[m1[m] >> 16];
-#pragma unroll
-                for (int kk = 0; kk < 4; ++kk) a[kk] += cf * (TA)v[kk];
-            }
-            for (int mm = 0; mm < n4; ++mm) {
-                const unsigned e = q4[inf.z + mm];
-                const int p = (e >> 16) & 31;
-                const uint4 u4 = (D.flags & 2)
-                                     ? *reinterpret_cast<const uint4 *>(up4s + (size_t)p * W4 + c)
-                                     : __ldg(reinterpret_cast<const uint4 *>(jb.up4 + (size_t)p * ld + D.col0 + c));
-                const unsigned ue[4] = {u4.x, u4.y, u4.z, u4.w};
-                const TX *xr = x + (size_t)(e & 0xffffu) * ld;
-                TX v[4];
-#pragma unroll
-                for (int kk = 0; kk < 4; ++kk) v[kk] = (ue[kk] >> 31) ? __ldg(xr + (ue[kk] & 0xffffu)) : TX(0);
-#pragma unroll
-                for (int kk = 0; kk < 4; ++kk) {
-                    const bool neg = ((ue[kk] >> 30) ^ (e >> 22)) & 1u;
-                    a[kk] += (neg ? -Jc : Jc) * (TA)v[kk];
-                }
-            }
-            stg4<TY, TA>(y + (size_t)inf.w * ld + D.col0 + c, a);
-            if (want_dot) {
-                TX xs[4];
-                lds4<TX>(xrow, xs);
-                TA part = TA(0);
-#pragma unroll
-                for (int kk = 0; kk < 4; ++kk) part += (TA)xs[kk] * a[kk];
-                dsum += (double)part;
-            }
-        }
-        // rotate: the next row's accumulators move to acc[0]
-#pragma unroll
-        for (int j2 = 0; j2 + 1 < RG; ++j2)
-#pragma unroll
-            for (int kk = 0; kk < 4; ++kk) acc[j2][kk] = acc[j2 + 1][kk];
-    }
-    return dsum;
-}
-
-// The fast path inlined into the consumer loop; the other tiles (narrow or
-// very wide blocks) through an out-of-line call, to keep the hot loop small.
-template <bool FAST, typename TX, typename TA, typename TY, int RG>
-__device__ __forceinline__ double hv_task(const HvJobT<TA> &jb, const TileDesc &D, const TX *__restrict__ S,
-                                          const unsigned char *__restrict__ meta,
-                                          const unsigned *__restrict__ up4s, const unsigned char *__restrict__ s16,
-                                          const TA *__restrict__ s_cf, const TA *__restrict__ s_cross, int nimp,
-                                          TA Jc, int task, int lane, bool want_dot)
-{
-    return hv_task_body<FAST, TX, TA, TY, RG>(jb, D, S, meta, up4s, s16, s_cf, s_cross, nimp, Jc, task, lane,
-                                              want_dot);
-}
-
-template <typename TX, typename TA, typename TY, int RG>
-__device__ __noinline__ double hv_task_generic(const HvJobT<TA> &jb, const TileDesc &D, const TX *__restrict__ S,
-                                               const unsigned char *__restrict__ meta,
-                                               const unsigned *__restrict__ up4s,
-                                               const unsigned char *__restrict__ s16, const TA *__restrict__ s_cf,
-                                               const TA *__restrict__ s_cross, int nimp, TA Jc, int task, int lane,
-                                               bool want_dot)
-{
-    return hv_task_body<false, TX, TA, TY, RG>(jb, D, S, meta, up4s, s16, s_cf, s_cross, nimp, Jc, task, lane,
-                                               want_dot);
-}
-
-__host__ __device__ inline int tile_ntasks(int g, int W4, int pitch, int RG)
-{
-    const int nq = W4 >> 2;
-    const int lqw = tile_lqw(nq, pitch == kPit);
-    const int qw = 1 << lqw, rs = 32 >> lqw;
-    const int nch = (nq + qw - 1) >> lqw;
-    const int rpt = rs * RG;
-    return nch * ((g + rpt - 1) / rpt);
-}
-
-// Persistent H*v over a batch of jobs.  Warp 0 produces (bulk copies of the
-// next tiles' row segments and metadata blobs), warps 1..NCW consume; each
-// consumer warp walks one stream of tasks across tile boundaries, so a tile
-// with fewer tasks than warps leaves no warp idle.  Tiles run in turns of
-// kSeg consecutive tiles per CTA, round-robin over the grid, so the tiles in
-// flight over the GPU stay close in the (L2-ordered) tile list.
-template <typename TX, typename TA, typename TY, int RG, int NCW, int MINB>
-__global__ void __launch_bounds__(32 * (NCW + 1), MINB)
-k_hvt(const __grid_constant__ HvBatch<TA> B, const ModelDev *__restrict__ mdl, const StageSizes Z)
-{
-    extern __shared__ __align__(128) unsigned char smem[];
-    constexpr int NT = 32 * (NCW + 1);
-    static_assert(NCW <= kMaxCW, "too many consumer warps");
-    const int nimp = mdl->nimp, npair = mdl->npair;
-    const SmemLayout<TA> L = smem_layout<TA>(Z, nimp);
-    TA *s_cf = reinterpret_cast<TA *>(smem + L.cf);
-    TA *s_cross = reinterpret_cast<TA *>(smem + L.cross);
-    double *s_dot = reinterpret_cast<double *>(smem + L.dot);
-    TileDesc *s_desc = reinterpret_cast<TileDesc *>(smem + L.desc);
-    unsigned long long *full = reinterpret_cast<unsigned long long *>(smem + L.bar);
-    unsigned long long *empty = full + kNBuf;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-
-    for (int i = tid; i < kMaxCoef; i += NT) {
-        TA v = TA(0);
-        if (i > 0 && (i - 1) / 2 < mdl->ncpl) {
-            const double cv = mdl->cval[(i - 1) >> 1];
-            v = (TA)(((i - 1) & 1) ? -cv : cv);
-        }
-        s_cf[i] = v;
-    }
-    for (int i = tid; i < nimp * nimp; i += NT) s_cross[i] = (TA)mdl->cross[i];
-    // x.y partials: one slot per (job, consumer warp), each written by its
-    // warp only and summed in a fixed order, so the result is reproducible
-    for (int i = tid; i < kMaxJobs * NCW; i += NT) s_dot[i] = 0.0;
-    if (tid == 0) {
-        for (int b = 0; b < kNBuf; ++b) {
-            mbar_init(&full[b], 1);
-            mbar_init(&empty[b], NCW);
-        }
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    const TA Jc = (TA)mdl->J;
-    const bool four = mdl->J != 0.0 && npair > 0;
-    // this CTA's tiles: turns of kSeg consecutive tiles, round-robin over the grid
-    auto next_tile = [&](int t) {
-        const int t1 = min(B.total, (t / kSeg + 1) * kSeg);
-        return t + 1 < t1 ? t + 1 : (t / kSeg + (int)gridDim.x) * kSeg;
-    };
-    const int tfirst = blockIdx.x * kSeg;
-
-    if (warp == 0) {
-        // ---- producer ----
-        const void *c_sp[kNBuf];
-        int c_ub[kNBuf];
-        for (int b = 0; b < kNBuf; ++b) {
-            c_sp[b] = nullptr;
-            c_ub[b] = -1;
-        }
-        auto load_tile = [&](int t, int *j, HvTile *T, int *rr) {
-            *j = find_job(B, t);
-            const HvJobT<TA> &jb = B.job[*j];
-            const int4 *tp = reinterpret_cast<const int4 *>(jb.tiles + (t - jb.tile0));
-            const int4 a = __ldg(tp), b2 = __ldg(tp + 1), c2 = __ldg(tp + 2);
-            *T = HvTile{a.x, a.y, a.z, a.w, b2.x, b2.y, b2.z, b2.w, c2.x, c2.y, c2.z, c2.w};
-            *rr = lane < T->rows ? __ldg(jb.rs_row + T->rs0 + lane) : 0;
-        };
-        int k = 0, t = tfirst, j = 0, rr = 0;
-        HvTile T;
-        if (t < B.total) load_tile(t, &j, &T, &rr);
-        while (t < B.total) {
-            // prefetch the next tile's descriptor and row ranks
-            const int tn = next_tile(t);
-            int jn = 0, rrn = 0;
-            HvTile Tn;
-            if (tn < B.total) load_tile(tn, &jn, &Tn, &rrn);
-            const int buf = k & 1;
-            if (k >= kNBuf && !bar_wait(&empty[buf], (unsigned)((k >> 1) - 1) & 1u, B.err)) break;
-            const HvJobT<TA> &jb = B.job[j];
-            const bool on = !jb.active || *jb.active != 0;
-            const int pitch = tile_pitch(T.W4);
-            const unsigned rowb = (unsigned)T.W4 * (unsigned)sizeof(TX);
-            const bool s16_ok = pitch == kPit && T.s16_bytes > 0 && T.s16_bytes <= Z.s16;
-            const bool up4_ok = four && npair * T.W4 * 4 <= Z.up4;
-            const bool fresh = c_sp[buf] != (const void *)jb.up4 || c_ub[buf] != T.ub;
-            const bool copy_up = on && (s16_ok || up4_ok) && fresh;
-            unsigned bytes = 0;
-            if (on) {
-                bytes = (unsigned)T.blob_bytes + (unsigned)T.rows * rowb;
-                if (copy_up) bytes += (s16_ok ? (unsigned)T.s16_bytes : 0u) + (up4_ok ? (unsigned)(npair * T.W4 * 4) : 0u);
-            }
-            if (lane == 0) {
-                s_desc[buf] = TileDesc{j, T.rows, T.W4, T.col0, T.hdr0, pitch, on ? 1 : 0,
-                                       (s16_ok ? 1 : 0) | (up4_ok ? 2 : 0)};
-                mbar_expect_tx(&full[buf], bytes);
-            }
-            __syncwarp();
-            if (on) {
-                if (lane == 0)
-                    bulk_g2s(smem + L.meta + (size_t)buf * Z.meta, jb.blob + (size_t)T.blob16 * 16,
-                             (unsigned)T.blob_bytes, &full[buf]);
-                if (copy_up) {
-                    if (s16_ok && lane == 31)
-                        bulk_g2s(smem + L.s16 + (size_t)buf * Z.s16, jb.sched16 + (size_t)T.s16_off * 16,
-                                 (unsigned)T.s16_bytes, &full[buf]);
-                    if (up4_ok)
-                        for (int p = lane; p < npair; p += 32)
-                            bulk_g2s(smem + L.up4 + (size_t)buf * Z.up4 + (size_t)p * T.W4 * 4,
-                                     jb.up4 + (size_t)p * jb.ld + T.col0, (unsigned)T.W4 * 4u, &full[buf]);
-                    c_sp[buf] = (const void *)jb.up4;
-                    c_ub[buf] = T.ub;
-                }
-                unsigned char *st = smem + L.stage + (size_t)buf * Z.stage;
-                const TX *x = (const TX *)jb.x + T.col0;
-                for (int r = lane; r < T.rows; r += 32) {
-                    const int d = r < 32 ? rr : __ldg(jb.rs_row + T.rs0 + r);
-                    bulk_g2s(st + (size_t)r * pitch * sizeof(TX), x + (size_t)d * jb.ld, rowb, &full[buf]);
-                }
-            }
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&full[buf]);
-            t = tn;
-            j = jn;
-            T = Tn;
-            rr = rrn;
-            ++k;
-        }
-    } else {
-        // ---- consumers ----
-        const int cw = warp - 1;
-        int k = 0, tk = cw, cur = -1;
-        double dsum = 0.0;
-        for (int t = tfirst; t < B.total; t = next_tile(t), ++k) {
-            const int buf = k & 1;
-            if (!bar_wait(&full[buf], (unsigned)(k >> 1) & 1u, B.err)) break;
-            const TileDesc D = s_desc[buf];
-            const int nt = D.on ? tile_ntasks(D.g, D.W4, D.pitch, RG) : 0;
-            if (nt > tk && D.job != cur) {
-                if (cur >= 0 && B.job[cur].dot_partial) {
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
-                    if (lane == 0) s_dot[cur * NCW + cw] += dsum;
-                }
-                dsum = 0.0;
-                cur = D.job;
-            }
-            const HvJobT<TA> &jb = B.job[D.job];
-            const TX *S = reinterpret_cast<const TX *>(smem + L.stage + (size_t)buf * Z.stage);
-            const unsigned char *meta = smem + L.meta + (size_t)buf * Z.meta;
-            const unsigned *up4s = reinterpret_cast<const unsigned *>(smem + L.up4 + (size_t)buf * Z.up4);
-            const unsigned char *s16 = smem + L.s16 + (size_t)buf * Z.s16;
-            const bool want_dot = jb.dot_partial != nullptr;
-            for (; tk < nt; tk += NCW) {
-                if (D.pitch == kPit)
-                    dsum += hv_task<true, TX, TA, TY, RG>(jb, D, S, meta, up4s, s16, s_cf, s_cross, nimp, Jc, tk,
-                                                          lane, want_dot);
-                else
-                    dsum += hv_task_generic<TX, TA, TY, RG>(jb, D, S, meta, up4s, s16, s_cf, s_cross, nimp, Jc, tk,
-                                                            lane, want_dot);
-            }
-            tk -= nt;
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&empty[buf]);
-        }
-        if (cur >= 0 && B.job[cur].dot_partial) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
-            if (lane == 0) s_dot[cur * NCW + cw] += dsum;
-        }
-        // the row tails past the last block are pads: zero them
-        for (int j = 0; j < B.njobs; ++j) {
-            const HvJobT<TA> &jb = B.job[j];
-            if (jb.active && *jb.active == 0) continue;
-            const int tail = jb.ld - jb.ncol;
-            if (tail <= 0) continue;
-            TY *y = (TY *)jb.y + jb.ncol;
-            const long long n = (long long)jb.nrow * tail;
-            for (long long i = ((long long)blockIdx.x * NCW + cw) * 32 + lane; i < n;
-                 i += (long long)gridDim.x * NCW * 32) {
-                const long long d = i / tail;
-                y[d * jb.ld + (i - d * tail)] = TY(0);
-            }
-        }
-    }
-    __syncthreads();
-    for (int j = tid; j < B.njobs; j += NT)
-        if (B.job[j].dot_partial) {
-            double v = 0.0;
-            for (int w = 0; w < NCW; ++w) v += s_dot[j * NCW + w];
-            B.job[j].dot_partial[blockIdx.x] = v;
-        }
-}
-
-// ---------------------------------------------------------------------------
-// host side: variants, tile lists, launch, autotuner
-// ---------------------------------------------------------------------------
-struct HvVariant {
-    int RG;      // rows per thread and task
-    int NCW;     // consumer warps (plus one producer warp)
-    int MINB;    // CTAs per SM
-    int TR;      // fast-path stage rows (a multiple of RG)
-    int meta_kb; // metadata blob budget per stage
-    int up4_kb;  // staged spin-flip / pair-hop partner columns per stage (0: read from L2)
-    int s16_kb;  // staged 16-bit gather schedule per stage (0: read from L2)
+// Item descriptor: the per-item row data of k_hv (row indices, impurity
+// patterns, down-spin moves, interspecies diagonal of the rows, spin-flip /
+// pair-hop terms), computed once per (down species, R, precision) by
+// k_item_desc and staged next to the rows.  Offsets are in 4-byte words.
+struct DescGeom {
+    int words, dm, nimp, npair;
+    int o_d, o_id, o_dcnt, o_flags, o_ddiag, o_dtgt, o_dval, o_cross, o_quad;
+    int o_sfsrc, o_phsrc, o_sfc, o_phc, o_rowmask;
 };
 
-// FP32 (TX = float): 10 stage rows of pitch 1040 hold the 10-row fibres of the
-// largest block pairs of the 3-orbital x 4-bath ground sector.
-static const HvVariant kVarF32[] = {{5, 15, 1, 10, 12, 24, 28}, {2, 31, 1, 12, 10, 20, 24},
-                                    {3, 15, 1, 12, 10, 20, 24}, {3, 23, 1, 12, 10, 20, 24}};
-// FP64 and FP32 -> FP64 (TA = double)
-static const HvVariant kVarF64[] = {{3, 15, 1, 6, 8, 20, 28}, {5, 15, 1, 10, 8, 0, 0}, {3, 7, 2, 6, 4, 0, 0}};
+template <typename TA, int R>
+static DescGeom desc_geom(int dm, const ModelDev &m)
+{
+    const int ts = sizeof(TA) / 4;
+    auto al = [](int w, int a) { return (w + a - 1) / a * a; };
+    DescGeom g;
+    g.dm = std::max(dm, 1);
+    g.nimp = m.nimp;
+    g.npair = std::max(m.npair, 1);
+    int w = 0;
+    g.o_d = w;       w += R;
+    g.o_id = w;      w += R;
+    g.o_dcnt = w;    w += R;
+    g.o_flags = w;   w += 2;            // slow, item pair mask
+    w = al(w, 2);
+    g.o_ddiag = w;   w += R * ts;
+    g.o_dtgt = w;    w += R * g.dm;
+    w = al(w, 2);
+    g.o_dval = w;    w += R * g.dm * ts;
+    g.o_cross = w;   w += g.nimp * R * ts;
+    w = al(w, 4);
+    g.o_quad = w;    w += R * g.nimp * (int)(sizeof(Quad<TA>) / 4);
+    g.o_sfsrc = w;   w += R * g.npair;
+    g.o_phsrc = w;   w += R * g.npair;
+    w = al(w, 2);
+    g.o_sfc = w;     w += R * g.npair * ts;
+    g.o_phc = w;     w += R * g.npair * ts;
+    g.o_rowmask = w; w += g.npair;
+    g.words = al(w, 4);
+    return g;
+}
+
+// one thread per item: the row data the k_hv setup computes per item
+template <typename TA, int R>
+__global__ void k_item_desc(int nitems, const int *__restrict__ items, const int *__restrict__ dn_info,
+                            const TA *__restrict__ dn_diag, const int *__restrict__ dn_tgt,
+                            const TA *__restrict__ dn_val, int nd, const ModelDev *__restrict__ mdl, DescGeom g,
+                            unsigned *__restrict__ out)
+{
+    const int it = blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= nitems) return;
+    unsigned *rec = out + (size_t)it * g.words;
+    for (int i = 0; i < g.words; ++i) rec[i] = 0u;
+    int *od = (int *)(rec + g.o_d), *oid = (int *)(rec + g.o_id), *ocnt = (int *)(rec + g.o_dcnt);
+    int *oflags = (int *)(rec + g.o_flags);
+    TA *oddiag = (TA *)(rec + g.o_ddiag);
+    int *odtgt = (int *)(rec + g.o_dtgt);
+    TA *odval = (TA *)(rec + g.o_dval);
+    TA *ocross = (TA *)(rec + g.o_cross);
+    Quad<TA> *oquad = (Quad<TA> *)(rec + g.o_quad);
+    int *osfsrc = (int *)(rec + g.o_sfsrc), *ophsrc = (int *)(rec + g.o_phsrc);
+    TA *osfc = (TA *)(rec + g.o_sfc), *ophc = (TA *)(rec + g.o_phc);
+    unsigned *orowmask = rec + g.o_rowmask;
+    const int nimp = mdl->nimp, npair = mdl->npair;
+    const TA Jc = (TA)mdl->J;
+    int d[R], id[R];
+    unsigned sfm[R], phm[R];
+    int slow = 0;
+    unsigned itemmask = 0u;
+    for (int r = 0; r < R; ++r) {
+        d[r] = items[it * R + r];
+        id[r] = 0;
+        sfm[r] = phm[r] = 0u;
+        int cnt = 0;
+        TA dg = TA(0);
+        if (d[r] >= 0) {
+            const int inf = dn_info[d[r]];
+            id[r] = (inf >> 8) & 0xff;
+            cnt = inf & 0xff;
+            dg = dn_diag[d[r]];
+            for (int s = 0; s < cnt; ++s) {
+                odtgt[r * g.dm + s] = dn_tgt[(size_t)s * nd + d[r]];
+                odval[r * g.dm + s] = dn_val[(size_t)s * nd + d[r]];
+            }
+        }
+        od[r] = d[r];
+        oid[r] = id[r];
+        ocnt[r] = cnt;
+        oddiag[r] = dg;
+    }
+    for (int iu = 0; iu < nimp; ++iu)
+        for (int r = 0; r < R; ++r) ocross[iu * R + r] = (TA)mdl->cross[iu * nimp + id[r]];
+    for (int r = 0; r < R; ++r) {
+        if (d[r] < 0) continue;
+        for (int p = 0; p < npair; ++p) {
+            const int esf = mdl->t4[mdl->pair_rev[p] * nimp + id[r]];   // spin-flip: T_{j<-i}(d)
+            const int eph = mdl->t4[p * nimp + id[r]];                  // pair hop:  T_{i<-j}(d)
+            if (esf < 0) {
+                const int off = (int)(short)(esf & 0xffff), dp = d[r] + off, rp = r + off;
+                const bool local = rp >= 0 && rp < R && d[rp] == dp;
+                osfsrc[r * g.npair + p] = local ? rp : -(1 + dp);
+                osfc[r * g.npair + p] = (esf & 0x40000000) ? -Jc : Jc;
+                sfm[r] |= 1u << p;
+                orowmask[p] |= 1u << r;
+                itemmask |= 1u << p;
+                if (!local) slow = 1;
+            }
+            if (eph < 0) {
+                const int off = (int)(short)(eph & 0xffff), dp = d[r] + off, rp = r + off;
+                const bool local = rp >= 0 && rp < R && d[rp] == dp;
+                ophsrc[r * g.npair + p] = local ? rp : -(1 + dp);
+                ophc[r * g.npair + p] = (eph & 0x40000000) ? -Jc : Jc;
+                phm[r] |= 1u << p;
+                orowmask[p] |= 1u << (16 + r);
+                itemmask |= 1u << p;
+                if (!local) slow = 1;
+            }
+        }
+    }
+    for (int r = 0; r < R; ++r)
+        for (int iu = 0; iu < nimp; ++iu) {
+            Quad<TA> q;
+            q.cnt = 0;
+            for (int t = 0; t < 2; ++t) {
+                q.du[t] = 0;
+                q.src[t] = 0;
+                q.c[t] = TA(0);
+            }
+            if (d[r] >= 0) {
+                for (int p = 0; p < npair; ++p) {
+                    const int e = mdl->t4[p * nimp + iu];
+                    if (e >= 0) continue;
+                    const int du = (int)(short)(e & 0xffff);
+                    const TA tu = (e & 0x40000000) ? TA(-1) : TA(1);
+                    if ((sfm[r] >> p) & 1u) {
+                        if (q.cnt == 2) slow = 1;
+                        else {
+                            q.du[q.cnt] = (signed char)du;
+                            q.src[q.cnt] = (unsigned char)max(osfsrc[r * g.npair + p], 0);
+                            q.c[q.cnt] = tu * osfc[r * g.npair + p];
+                            ++q.cnt;
+                        }
+                    }
+                    if ((phm[r] >> p) & 1u) {
+                        if (q.cnt == 2) slow = 1;
+                        else {
+                            q.du[q.cnt] = (signed char)du;
+                            q.src[q.cnt] = (unsigned char)max(ophsrc[r * g.npair + p], 0);
+                            q.c[q.cnt] = tu * ophc[r * g.npair + p];
+                            ++q.cnt;
+                        }
+                    }
+                }
+            }
+            oquad[r * nimp + iu] = q;
+        }
+    oflags[0] = slow;
+    oflags[1] = (int)itemmask;
+}
+
+// all threads: copy the rows and the descriptor of `item` into a stage
+// buffer and its descriptor buffer, and commit the group
+template <typename TX, typename TA, int R, int NT>
+__device__ __forceinline__ void hv_stage_item(const HvBatch<TA> &b, int item, TX *stage, unsigned *desc,
+                                              int dwords)
+{
+    const HvJobT<TA> &jb = b.job[hv_find_job(b, item)];
+    const int it = item - jb.item0;
+    const int ld = jb.ld;
+    constexpr int EPV = 16 / sizeof(TX);   // elements per 16-byte copy
+    const int nv = ld / EPV;
+    const TX *x = (const TX *)jb.x;
+    const unsigned *src_desc = jb.desc + (size_t)it * dwords;
+    for (int q = threadIdx.x; q < dwords / 4; q += NT) cp_async16(desc + 4 * q, src_desc + 4 * q);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int d = jb.items[it * R + r];
+        if (d < 0) continue;
+        const TX *src = x + (size_t)d * ld;
+        for (int q = threadIdx.x; q < nv; q += NT) {
+            const int u = q * EPV;
+            cp_async16(stage + ((u >> 5) * R + r) * 32 + (u & 31), src + u);
+        }
+    }
+    cp_async_commit();
+}
+
+// SPLIT: k_hv_down has already written the down-spin hybridisation into y;
+// this kernel adds the other terms to it instead of computing the row AXPYs.
+template <typename TX, typename TA, typename TY, int R, int NT, int MINB, bool SPLIT>
+__global__ void __launch_bounds__(NT, MINB)
+k_hv_async(const __grid_constant__ HvBatch<TA> batch, const ModelDev *__restrict__ mdl, const DescGeom g)
+{
+    extern __shared__ __align__(16) unsigned char smem_async[];
+    const int nimp = mdl->nimp;
+    int ldmax = 0;
+    for (int i = 0; i < batch.njobs; ++i) ldmax = max(ldmax, batch.job[i].ld);
+    const int stage_elems = R * ldmax;
+    TX *stage0 = reinterpret_cast<TX *>(smem_async);
+    TX *stage1 = stage0 + stage_elems;
+    unsigned *desc0 = reinterpret_cast<unsigned *>(smem_async + ((2 * (size_t)stage_elems * sizeof(TX) + 15) & ~(size_t)15));
+    unsigned *desc1 = desc0 + g.words;
+    int *s_t4 = reinterpret_cast<int *>(desc1 + g.words);
+    __shared__ unsigned s_pmask[kMaxImp];
+    __shared__ double s_red[NT / 32];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NW = NT / 32;
+    for (int i = tid; i < mdl->npair * nimp; i += NT) s_t4[i] = mdl->t4[i];
+    for (int i = tid; i < nimp; i += NT) s_pmask[i] = mdl->pairmask[i];
+    __syncthreads();
+
+    int cur = hv_next_item(batch, (int)blockIdx.x);
+    if (cur >= 0) hv_stage_item<TX, TA, R, NT>(batch, cur, stage0, desc0, g.words);
+    int k = 0;
+    while (cur >= 0) {
+        const int buf = k & 1;
+        const int nxt = hv_next_item(batch, cur + (int)gridDim.x);
+        // buffers (k+1)&1 were released by the barrier that ended item k-1;
+        // one commit group per iteration either way
+        if (nxt >= 0) hv_stage_item<TX, TA, R, NT>(batch, nxt, buf ? stage0 : stage1, buf ? desc0 : desc1, g.words);
+        else cp_async_commit();
+
+        const HvJobT<TA> &jb = batch.job[hv_find_job(batch, cur)];
+        const int it = cur - jb.item0;
+        const int ld = jb.ld, nch = ld >> 5;
+        const TX *__restrict__ x = (const TX *)jb.x;
+        TY *__restrict__ y = (TY *)jb.y;
+        cp_async_wait_all_but_newest();   // this thread's copies of the current item
+        __syncthreads();                  // everyone's
+        const TX *S = buf ? stage1 : stage0;
+        const unsigned *dsc = buf ? desc1 : desc0;
+        const int *s_d = (const int *)(dsc + g.o_d);
+        const int *s_dcnt = (const int *)(dsc + g.o_dcnt);
+        const int *s_dtgt = (const int *)(dsc + g.o_dtgt);
+        const TA *s_dval = (const TA *)(dsc + g.o_dval);
+        const TA *s_crossT = (const TA *)(dsc + g.o_cross);
+        const Quad<TA> *s_q = (const Quad<TA> *)(dsc + g.o_quad);
+        const int *s_sfsrc = (const int *)(dsc + g.o_sfsrc), *s_phsrc = (const int *)(dsc + g.o_phsrc);
+        const TA *s_sfc = (const TA *)(dsc + g.o_sfc), *s_phc = (const TA *)(dsc + g.o_phc);
+        const unsigned *s_rowmask = dsc + g.o_rowmask;
+        const bool slow = ((const int *)(dsc + g.o_flags))[0] != 0;
+        const unsigned imask = (unsigned)((const int *)(dsc + g.o_flags))[1];
+        const int dm = g.dm, npr = g.npair;
+
+        TA ddiag[R];
+        bool live[R];
+        int dcnt[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            ddiag[r] = ((const TA *)(dsc + g.o_ddiag))[r];
+            live[r] = s_d[r] >= 0;
+            dcnt[r] = s_dcnt[r];
+        }
+        const bool want_dot = jb.dot_partial != nullptr;
+        double dacc = 0.0;
+        constexpr int SB = 4;
+        constexpr int DB = 2;
+        for (int cb = warp; cb < nch; cb += NW * kHvCh) {
+            // chunks cb + NW*q, q < kHvCh; column of this lane in chunk q: ub + 32*NW*q
+            const int ub = 32 * cb + lane;
+            bool has[kHvCh];
+            int iu[kHvCh];
+            int2 h[kHvCh];
+            TA acc[kHvCh][R];
+#pragma unroll
+            for (int q = 0; q < kHvCh; ++q) {
+                has[q] = cb + NW * q < nch;
+                h[q] = has[q] ? __ldg(jb.up_sched_hdr + cb + NW * q) : make_int2(0, 0);
+            }
+            // the first DB down-spin moves of every row (SPLIT: the down-spin
+            // part already in y): loads in flight early
+            TX gd[R][DB][kHvCh];
+            TY yp[R][kHvCh];
+            if constexpr (SPLIT) {
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const TY *yr = y + (size_t)(live[r] ? s_d[r] : 0) * ld + ub;
+#pragma unroll
+                    for (int q = 0; q < kHvCh; ++q) yp[r][q] = (live[r] && has[q]) ? yr[32 * NW * q] : TY(0);
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < R; ++r)
+#pragma unroll
+                    for (int t = 0; t < DB; ++t) {
+                        const bool mv = t < dcnt[r];
+                        const TX *xr = x + (size_t)s_dtgt[r * dm + (mv ? t : 0)] * ld + ub;
+#pragma unroll
+                        for (int q = 0; q < kHvCh; ++q)
+                            gd[r][t][q] = (mv && has[q]) ? __ldg(xr + 32 * NW * q) : TX(0);
+                    }
+            }
+            // first SB schedule entries of every chunk
+            HopEnt<TA> e0[kHvCh][SB];
+#pragma unroll
+            for (int q = 0; q < kHvCh; ++q)
+#pragma unroll
+                for (int t = 0; t < SB; ++t)
+                    e0[q][t] = (t < h[q].y) ? jb.up_sched[h[q].x + 32 * t + lane] : HopEnt<TA>{};
+            // diagonal
+#pragma unroll
+            for (int q = 0; q < kHvCh; ++q) {
+                const int u = ub + 32 * NW * q;
+                int inf = 0;
+                TA ud = TA(0);
+                if (has[q]) {
+                    inf = __ldg(jb.up_info + u);
+                    ud = __ldg(jb.up_diag + u);
+                }
+                iu[q] = (inf >> 8) & 0xff;
+#pragma unroll
+                for (int r = 0; r < R; ++r) acc[q][r] = TA(0);
+                if (has[q]) {
+                    const TX *so = S + ((u >> 5) * R) * 32 + (u & 31);
+#pragma unroll
+                    for (int r = 0; r < R; ++r)
+                        acc[q][r] = (ud + ddiag[r] + s_crossT[iu[q] * R + r]) * (TA)so[32 * r];
+                }
+            }
+            // up-spin hybridisation: scheduled conflict-free gathers
+#pragma unroll
+            for (int q = 0; q < kHvCh; ++q) {
+                const int ns = h[q].y;
+                const HopEnt<TA> *tab = jb.up_sched + h[q].x + lane;
+                HopEnt<TA> e[SB];
+#pragma unroll
+                for (int t = 0; t < SB; ++t) e[t] = e0[q][t];
+                for (int s0 = 0; s0 < ns; s0 += SB) {
+                    HopEnt<TA> f[SB];
+#pragma unroll
+                    for (int t = 0; t < SB; ++t) f[t] = (s0 + SB + t < ns) ? tab[32 * (s0 + SB + t)] : HopEnt<TA>{};
+#pragma unroll
+                    for (int t = 0; t < SB; ++t) {
+                        if (s0 + t < ns) {
+                            const TX *st = S + e[t].t;
+#pragma unroll
+                            for (int r = 0; r < R; ++r) acc[q][r] += e[t].v * (TA)st[32 * r];
+                        }
+                    }
+#pragma unroll
+                    for (int t = 0; t < SB; ++t) e[t] = f[t];
+                }
+            }
+            // spin-flip and pair hopping (partner rows staged)
+#pragma unroll
+            for (int q = 0; q < kHvCh; ++q) {
+                if (!has[q]) continue;
+                const int u = ub + 32 * NW * q;
+                if (!slow) {
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        const Quad<TA> qd = s_q[r * nimp + iu[q]];
+                        if (qd.cnt > 0) {
+#pragma unroll
+                            for (int t = 0; t < 2; ++t) {
+                                if (t < qd.cnt) {
+                                    const int w = u + qd.du[t];
+                                    acc[q][r] += qd.c[t] * (TA)S[((w >> 5) * R + qd.src[t]) * 32 + (w & 31)];
+                                }
+                            }
+                        }
+                    }
+                } else {
+                    unsigned pm = s_pmask[iu[q]] & imask;
+                    while (pm) {
+                        const int p = __ffs(pm) - 1;
+                        pm &= pm - 1;
+                        const int e = s_t4[p * nimp + iu[q]];
+                        const int w = u + (int)(short)(e & 0xffff);
+                        const bool neg = (e & 0x40000000) != 0;
+                        const unsigned rm = s_rowmask[p];
+#pragma unroll
+                        for (int r = 0; r < R; ++r) {
+                            if ((rm >> r) & 1u) {
+                                const int src = s_sfsrc[r * npr + p];
+                                const TX xv = src >= 0 ? S[((w >> 5) * R + src) * 32 + (w & 31)]
+                                                       : __ldg(x + (size_t)(-1 - src) * ld + w);
+                                const TA cf = neg ? -s_sfc[r * npr + p] : s_sfc[r * npr + p];
+                                acc[q][r] += cf * (TA)xv;
+                            }
+                            if ((rm >> (16 + r)) & 1u) {
+                                const int src = s_phsrc[r * npr + p];
+                                const TX xv = src >= 0 ? S[((w >> 5) * R + src) * 32 + (w & 31)]
+                                                       : __ldg(x + (size_t)(-1 - src) * ld + w);
+                                const TA cf = neg ? -s_phc[r * npr + p] : s_phc[r * npr + p];
+                                acc[q][r] += cf * (TA)xv;
+                            }
+                        }
+                    }
+                }
+            }
+            // down-spin hybridisation: the early loads, then the remaining moves
+            if constexpr (SPLIT) {
+#pragma unroll
+                for (int r = 0; r < R; ++r)
+#pragma unroll
+                    for (int q = 0; q < kHvCh; ++q) acc[q][r] += (TA)yp[r][q];
+            } else {
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+#pragma unroll
+                for (int t = 0; t < DB; ++t) {
+                    if (t < dcnt[r]) {
+                        const TA v = s_dval[r * dm + t];
+#pragma unroll
+                        for (int q = 0; q < kHvCh; ++q) acc[q][r] += v * (TA)gd[r][t][q];
+                    }
+                }
+                for (int t0 = DB; t0 < dcnt[r]; t0 += DB) {
+                    TX g2[DB][kHvCh];
+#pragma unroll
+                    for (int t = 0; t < DB; ++t) {
+                        const bool mv = t0 + t < dcnt[r];
+                        const TX *xr = x + (size_t)s_dtgt[r * dm + (mv ? t0 + t : t0)] * ld + ub;
+#pragma unroll
+                        for (int q = 0; q < kHvCh; ++q) g2[t][q] = (mv && has[q]) ? __ldg(xr + 32 * NW * q) : TX(0);
+                    }
+#pragma unroll
+                    for (int t = 0; t < DB; ++t) {
+                        if (t0 + t < dcnt[r]) {
+                            const TA v = s_dval[r * dm + t0 + t];
+#pragma unroll
+                            for (int q = 0; q < kHvCh; ++q) acc[q][r] += v * (TA)g2[t][q];
+                        }
+                    }
+                }
+            }
+            }
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                if (!live[r]) continue;
+                TY *yr = y + (size_t)s_d[r] * ld + ub;
+#pragma unroll
+                for (int q = 0; q < kHvCh; ++q)
+                    if (has[q]) yr[32 * NW * q] = (TY)acc[q][r];
+            }
+            if (want_dot) {
+                TA part = TA(0);
+#pragma unroll
+                for (int q = 0; q < kHvCh; ++q) {
+                    if (!has[q]) continue;
+                    const int u = ub + 32 * NW * q;
+                    const TX *so = S + ((u >> 5) * R) * 32 + (u & 31);
+#pragma unroll
+                    for (int r = 0; r < R; ++r)
+                        if (live[r]) part += (TA)so[32 * r] * (TA)(TY)acc[q][r];
+                }
+                dacc += (double)part;
+            }
+        }
+        if (want_dot) {
+            for (int off = 16; off > 0; off >>= 1) dacc += __shfl_down_sync(0xffffffffu, dacc, off);
+            if (lane == 0) s_red[warp] = dacc;
+        }
+        __syncthreads();   // item done: its buffers are free
+        if (want_dot && tid == 0) {
+            double t = 0.0;
+            for (int w = 0; w < NW; ++w) t += s_red[w];
+            jb.dot_partial[it] = t;
+        }
+        cur = nxt;
+        ++k;
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
+// ---------------------------------------------------------------------------
+// k_hv_down: the down-spin hybridisation of the split H*v,
+//   y[d][u] = sum over moves (d -> d', t) of t * x[d'][u],
+// for every row d, written (not accumulated) into y; k_hv_async<SPLIT> then
+// adds the other terms.  The rows of a down-spin block (equal electron counts
+// in every conserved subsystem) are closed under the moves, so a chunk = one
+// block x a range of columns is independent of all others.  A CTA stages the
+// block's move list once ({target index within the block, signed coupling})
+// and then walks the chunk's column slices, staged by cp.async and double-
+// buffered when two slices fit.  A slice is kb groups of WB bytes (one 64- or
+// 128-byte line segment) of every row of the block, kb as large as the buffer
+// allows, so small blocks take wide slices.  Every element of x is read from
+// memory once per H*v and the moves read shared memory only.  CTAs take
+// contiguous chunk ranges, so consecutive chunks usually share the block and
+// its move list.
+// ---------------------------------------------------------------------------
+template <typename TA>
+__device__ __forceinline__ int hv_tile_job(const HvBatch<TA> &b, int tile)
+{
+    int j = 0;
+    while (j + 1 < b.njobs && tile >= b.job[j + 1].tile0) ++j;
+    return j;
+}
+
+struct DownLayout {        // shared-memory layout of k_hv_down, in bytes
+    int ptr, rows, mv, x0, x1;
+};
+
+// stage columns [col, col + kw * W) of the block's rows: row i at buf + i * kw * W
+template <typename TX, int NT, int WB>
+__device__ __forceinline__ void hv_down_slice(const TX *__restrict__ x, const int *s_rows, int nr, int ld,
+                                              int col, int kw, TX *buf)
+{
+    constexpr int CPG = WB / 16;                // 16-byte copies per group of a row
+    constexpr int EPV = 16 / (int)sizeof(TX);
+    const int cpr = kw * CPG;
+    for (int q = threadIdx.x; q < nr * cpr; q += NT) {
+        const int i = q / cpr, c = q - i * cpr;
+        cp_async16(buf + (size_t)i * cpr * EPV + c * EPV, x + (size_t)s_rows[i] * ld + col + c * EPV);
+    }
+}
+
+template <typename TX, typename TA, typename TY, int NT, int WB>
+__global__ void __launch_bounds__(NT, 1)
+k_hv_down(const __grid_constant__ HvBatch<TA> batch, int total, const DownLayout L, int cap_rows, int dbuf)
+{
+    extern __shared__ __align__(16) unsigned char smem_down[];
+    constexpr int W = WB / (int)sizeof(TX);   // columns per group (one WB-byte segment of a row)
+    constexpr int RPW = 32 / W;               // groups per warp pass
+    constexpr int NW = NT / 32;
+    int *s_ptr = reinterpret_cast<int *>(smem_down + L.ptr);
+    int *s_rows = reinterpret_cast<int *>(smem_down + L.rows);
+    HopEnt<TA> *s_mv = reinterpret_cast<HopEnt<TA> *>(smem_down + L.mv);
+    TX *const xb0 = reinterpret_cast<TX *>(smem_down + L.x0);
+    TX *const xb1 = reinterpret_cast<TX *>(smem_down + L.x1);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int sub = lane / W, c = lane - sub * W;
+    const int c_begin = (int)((long long)total * blockIdx.x / gridDim.x);
+    const int c_end = (int)((long long)total * (blockIdx.x + 1) / gridDim.x);
+    int have_job = -1, have_blk = -1;
+    for (int ch = c_begin; ch < c_end; ++ch) {
+        const int jid = hv_tile_job(batch, ch);
+        const HvJobT<TA> &jb = batch.job[jid];
+        if (jb.active && *jb.active == 0) continue;
+        const int lc = ch - jb.tile0;
+        // block of this chunk: last b with chunks[b].x <= lc
+        int lo = 0, hi = jb.dblk_n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(&jb.dblk_chunks[mid].x) <= lc) lo = mid;
+            else hi = mid - 1;
+        }
+        const int blk = lo;
+        const int2 cinfo = jb.dblk_chunks[blk];
+        const int ld = jb.ld;
+        const int col0 = (lc - cinfo.x) * cinfo.y * 32;
+        const int col1 = min(ld, col0 + cinfo.y * 32);
+        const int p0 = __ldg(jb.dblk_off + blk), nr = __ldg(jb.dblk_off + blk + 1) - p0;
+        const TX *x = (const TX *)jb.x;
+        TY *y = (TY *)jb.y;
+        __syncthreads();   // the previous chunk is done with shared memory
+        if (jid != have_job || blk != have_blk) {
+            const int m0 = __ldg(jb.dblk_ptr + p0), nm = __ldg(jb.dblk_ptr + p0 + nr) - m0;
+            for (int i = tid; i <= nr; i += NT) s_ptr[i] = __ldg(jb.dblk_ptr + p0 + i) - m0;
+            for (int i = tid; i < nr; i += NT) s_rows[i] = __ldg(jb.dblk_rows + p0 + i);
+            for (int i = tid; i < nm; i += NT) s_mv[i] = jb.dblk_mv[m0 + i];
+            have_job = jid;
+            have_blk = blk;
+            __syncthreads();
+        }
+        // a slice = kb groups of W columns of every row (small blocks: wide slices)
+        const int ngr = (col1 - col0) / W;
+        const int kb = max(1, min(cap_rows / nr, ngr));
+        const int ns = (ngr + kb - 1) / kb;
+        hv_down_slice<TX, NT, WB>(x, s_rows, nr, ld, col0, min(kb, ngr), xb0);
+        cp_async_commit();
+        for (int sl = 0; sl < ns; ++sl) {
+            const TX *S = (dbuf && (sl & 1)) ? xb1 : xb0;
+            const int kw = min(kb, ngr - sl * kb);   // groups in this slice
+            if (dbuf && sl + 1 < ns) {
+                hv_down_slice<TX, NT, WB>(x, s_rows, nr, ld, col0 + (sl + 1) * kb * W, min(kb, ngr - (sl + 1) * kb),
+                                          (sl & 1) ? xb0 : xb1);
+                cp_async_commit();
+                cp_async_wait_all_but_newest();
+            } else {
+                asm volatile("cp.async.wait_all;" ::: "memory");
+            }
+            __syncthreads();
+            const int ws = kw * W;               // row stride of the staged slice
+            TY *ys = y + col0 + sl * kb * W + c;
+            if (kw == 1) {
+                // one group per row (large blocks): 4 moves in flight
+                for (int i = warp * RPW + sub; i < nr; i += NW * RPW) {
+                    const int b1 = s_ptr[i], e1 = s_ptr[i + 1];
+                    const TX *Sc = S + c;
+                    TA a = TA(0);
+                    int e = b1;
+                    for (; e + 4 <= e1; e += 4) {
+                        const HopEnt<TA> m0 = s_mv[e], m1 = s_mv[e + 1], m2 = s_mv[e + 2], m3 = s_mv[e + 3];
+                        const TX x0 = Sc[m0.t * W], x1 = Sc[m1.t * W], x2 = Sc[m2.t * W], x3 = Sc[m3.t * W];
+                        a += m0.v * (TA)x0;
+                        a += m1.v * (TA)x1;
+                        a += m2.v * (TA)x2;
+                        a += m3.v * (TA)x3;
+                    }
+                    for (; e < e1; ++e) {
+                        const HopEnt<TA> m = s_mv[e];
+                        a += m.v * (TA)Sc[m.t * W];
+                    }
+                    ys[(size_t)s_rows[i] * ld] = (TY)a;
+                }
+            } else {
+                // several groups per row (small blocks, wide slices): each move
+                // serves up to KQ groups
+                constexpr int KQ = 4;
+                const int npass = (kw + KQ - 1) / KQ;
+                for (int it = warp * RPW + sub; it < nr * npass; it += NW * RPW) {
+                    const int i = it / npass, g0 = (it - i * npass) * KQ;
+                    const int b1 = s_ptr[i], e1 = s_ptr[i + 1];
+                    const TX *Sc = S + g0 * W + c;
+                    TA a[KQ];
+#pragma unroll
+                    for (int q = 0; q < KQ; ++q) a[q] = TA(0);
+                    for (int e = b1; e < e1; ++e) {
+                        const HopEnt<TA> m = s_mv[e];
+                        const TX *Sm = Sc + m.t * ws;
+#pragma unroll
+                        for (int q = 0; q < KQ; ++q)
+                            if (g0 + q < kw) a[q] += m.v * (TA)Sm[q * W];
+                    }
+                    TY *yr = ys + (size_t)s_rows[i] * ld + g0 * W;
+#pragma unroll
+                    for (int q = 0; q < KQ; ++q)
+                        if (g0 + q < kw) yr[q * W] = (TY)a[q];
+                }
+            }
+            __syncthreads();   // slice done: its buffer is free
+            if (!dbuf && sl + 1 < ns) {
+                hv_down_slice<TX, NT, WB>(x, s_rows, nr, ld, col0 + (sl + 1) * kb * W, min(kb, ngr - (sl + 1) * kb),
+                                          xb0);
+                cp_async_commit();
+            }
+        }
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
+template <typename TX, typename TA, int R>
+static size_t dyn_smem_bytes_async(int ld, const ModelDev &m, const DescGeom &g)
+{
+    return ((2 * (size_t)R * ld * sizeof(TX) + 15) & ~(size_t)15) + sizeof(unsigned) * 2 * (size_t)g.words +
+           sizeof(int) * (size_t)m.npair * m.nimp;
+}
+
+// ---------------------------------------------------------------------------
+// tile-shape variants and the autotuner
+// ---------------------------------------------------------------------------
+// A variant fixes the kernel (k_hv or k_hv_async), the rows per item R, the CTA
+// size NT and the CTAs per SM the register budget is cut for (MINB).  The
+// k_hv variants compute every element with the same sequence of operations
+// (bit-identical outputs); k_hv_async adds the up-spin terms in the order of
+// the gather schedule, so FP32 outputs of the two kernels agree to rounding.
+// The first H*v of a (kind, Nup, Ndn) shape times each variant on that sector
+// (scratch vectors, CUDA events on the context stream) and keeps the fastest.
+struct HvVariant {
+    int R, NT, MINB;
+    // 0: k_hv; 1: k_hv_async (double-buffered asynchronous stage);
+    // 2 / 3: split, k_hv_down on 128- / 64-byte row slices + k_hv_async<SPLIT>
+    int staged;
+};
+static const HvVariant kVarF32[] = {{3, 512, 2, 0}, {4, 256, 2, 0}, {6, 512, 1, 0}, {3, 256, 3, 0},
+                                    {8, 512, 1, 0}, {4, 512, 1, 1}, {3, 512, 1, 1}, {2, 512, 2, 1},
+                                    {2, 256, 2, 1}, {3, 512, 1, 2}, {4, 512, 1, 2}, {3, 512, 1, 3}};
+static const HvVariant kVarF64[] = {{2, 256, 2, 0}, {3, 256, 1, 0}, {2, 512, 1, 0}, {2, 512, 1, 1},
+                                    {4, 512, 1, 1}, {2, 512, 1, 2}, {2, 512, 1, 3}};
 static const int kNVarF32 = sizeof(kVarF32) / sizeof(kVarF32[0]);
 static const int kNVarF64 = sizeof(kVarF64) / sizeof(kVarF64[0]);
 
 static const HvVariant &variant(int kind, int v) { return kind == HV_F32 ? kVarF32[v] : kVarF64[v]; }
 static int nvariants(int kind) { return kind == HV_F32 ? kNVarF32 : kNVarF64; }
-static size_t x_size(int kind) { return kind == HV_F64 ? sizeof(double) : sizeof(float); }
-static StageSizes sizes_of(int kind, int v)
-{
-    const HvVariant &h = variant(kind, v);
-    return StageSizes{h.TR * kPit * (int)x_size(kind), h.meta_kb * 1024, h.up4_kb * 1024, h.s16_kb * 1024, h.NCW};
-}
+
+constexpr long long kTuneMinElems = 1ll << 18;   // smaller sectors take variant 0 untimed
+
 static long long shape_key(int kind, const Sector &s) { return ((long long)kind << 32) | (s.ne_up << 16) | s.ne_down; }
-static long long tile_key(const Sector &s, int kind, int v)
-{
-    const HvVariant &h = variant(kind, v);
-    const long long sel = (((long long)x_size(kind) * 64 + h.TR) * 256 + h.meta_kb) * 64 + h.RG;
-    return (sel << 32) | ((long long)s.ne_up << 16) | s.ne_down;
-}
-
-// Tiles of a sector: for every (down block, up block) pair the row sets of
-// the first level whose sets fit the stage (fast path: at most TR rows;
-// others: rows x pitch elements) and whose metadata blob fits its budget.
-// Tiles are ordered by the total electron count per subsystem (spin-flip
-// keeps it, so its partner tiles run together), then by block pair, so the
-// neighbour rows that moves between row sets read are recent in L2.
-int hv_tile_list(mo_ed_ctx *ctx, const Sector &s, int kind, int v, const HvTile **tiles, int *ntiles)
-{
-    const long long key = tile_key(s, kind, v);
-    auto it = ctx->hv_tiles.find(key);
-    if (it == ctx->hv_tiles.end()) {
-        const Species &dn = *s.dn, &up = *s.up;
-        const int nsub = dn.nsub;
-        const HvVariant &hv = variant(kind, v);
-        const StageSizes Z = sizes_of(kind, v);
-        const long long sbytes = Z.stage, mbytes = Z.meta;
-        const long long es = (long long)x_size(kind);
-        struct Ent {
-            long long orbit;
-            int bd, bu;
-            HvTile tile;
-        };
-        std::vector<Ent> ents;
-        for (int bd = 0; bd < (int)dn.h_dblk.size(); ++bd) {
-            const DownBlock &db = dn.h_dblk[bd];
-            for (int bu = 0; bu < (int)up.h_ublk.size(); ++bu) {
-                const UpBlock &ub = up.h_ublk[bu];
-                const int pitch = tile_pitch(ub.W4);
-                const bool fast = pitch == kPit;
-                int lev = -1;
-                for (int j = 0; j <= nsub; ++j) {
-                    const bool rows_ok = fast ? db.rs_rows[j] <= hv.TR : db.rs_rows[j] * (long long)pitch * es <= sbytes;
-                    if (rows_ok && db.blob_max[j] <= mbytes) {
-                        lev = j;
-                        break;
-                    }
-                }
-                if (lev < 0) return fail(ctx, MO_ED_ERR_ARG, "an up-spin block is wider than the H*v stage");
-                long long orbit = 0;
-                for (int k = 0; k < nsub; ++k) orbit = orbit * 64 + db.cnt[k] + up.h_ublk_cnt[(size_t)bu * kMaxSub + k];
-                for (int q = 0; q < db.nset[lev]; ++q) {
-                    const int set = db.rs0[lev] + q;
-                    const int2 r = dn.h_rs[set], b = dn.h_rs_blob[set];
-                    ents.push_back({orbit, bd, bu,
-                                    HvTile{r.x, r.y, b.x, b.y, ub.col0, ub.W4, ub.hdr0, ub.s16_off, ub.s16_bytes, bu, 0, 0}});
-                }
-            }
-        }
-        std::stable_sort(ents.begin(), ents.end(), [](const Ent &a, const Ent &b) {
-            if (a.orbit != b.orbit) return a.orbit < b.orbit;
-            if (a.bd != b.bd) return a.bd < b.bd;
-            return a.bu < b.bu;
-        });
-        std::vector<HvTile> h(ents.size());
-        for (size_t i = 0; i < ents.size(); ++i) h[i] = ents[i].tile;
-        DevBuf d;
-        if (int rc = dev_alloc(ctx, d, sizeof(HvTile) * std::max<size_t>(1, h.size()))) return rc;
-        MOED_CUDA(ctx, cudaMemcpyAsync(d.p, h.data(), sizeof(HvTile) * h.size(), cudaMemcpyHostToDevice, ctx->stream));
-        MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        it = ctx->hv_tiles.emplace(key, std::make_pair(std::move(d), (int)h.size())).first;
-    }
-    *tiles = (const HvTile *)it->second.first.p;
-    *ntiles = it->second.second;
-    return MO_ED_OK;
-}
-
-static int ensure_err(mo_ed_ctx *ctx)
-{
-    if (ctx->d_err.p) return MO_ED_OK;
-    if (int rc = dev_alloc(ctx, ctx->d_err, sizeof(int))) return rc;
-    MOED_CUDA(ctx, cudaMemsetAsync(ctx->d_err.p, 0, sizeof(int), ctx->stream));
-    return MO_ED_OK;
-}
 
 template <typename TA>
-void hv_fill_job(const mo_ed_ctx *ctx, const Sector &s, int kind, int v, const void *x, void *y, HvJobT<TA> &j)
+void hv_fill_job(const mo_ed_ctx *ctx, const Sector &s, int R, const void *x, void *y, HvJobT<TA> &j)
 {
-    memset(&j, 0, sizeof(j));
+    const bool f32 = sizeof(TA) == 4;
+    (void)ctx;
     j.x = x;
     j.y = y;
+    j.dot_partial = nullptr;
+    j.active = nullptr;
+    j.nu = s.up->n;
+    j.nd = s.dn->n;
     j.ld = s.ld();
-    j.ncol = s.up->ncol;
-    j.nrow = s.dn->n;
-    auto it = ctx->hv_tiles.find(tile_key(s, kind, v));
-    if (it != ctx->hv_tiles.end()) {
-        j.tiles = (const HvTile *)it->second.first.p;
-        j.ntiles = it->second.second;
+    auto it = s.dn->items.find(R);
+    j.items = it != s.dn->items.end() ? it->second : nullptr;
+    j.nitems = it != s.dn->items.end() ? s.dn->nitems.at(R) : 0;
+    j.item0 = 0;
+    j.up_info = s.up->info;
+    j.up_tab = f32 ? (const HopEnt<TA> *)s.up->tab_f : (const HopEnt<TA> *)s.up->tab_d;
+    j.up_diag = f32 ? (const TA *)s.up->diag_f : (const TA *)s.up->diag_d;
+    j.up_hw = s.up->hw;
+    j.up_maxcnt = s.up->max_cnt;
+    j.dn_info = s.dn->info;
+    j.dn_tgt = s.dn->hop_tgt;
+    j.dn_val = f32 ? (const TA *)s.dn->hop_val_f : (const TA *)s.dn->hop_val_d;
+    j.dn_diag = f32 ? (const TA *)s.dn->diag_f : (const TA *)s.dn->diag_d;
+    j.dn_maxcnt = s.dn->max_cnt;
+    j.pad = 0;
+    j.up_sched_hdr = s.up->sched_hdr;
+    j.up_sched_ent = s.up->sched_ent;
+    {
+        auto dsc = s.dn->desc.find(R * 2 + (f32 ? 0 : 1));
+        j.desc = dsc != s.dn->desc.end() ? dsc->second : nullptr;
     }
-    const Species &up = *s.up, &dn = *s.dn;
-    j.ublk = up.ublk;
-    j.sched_hdr = up.sched_hdr;
-    j.sched_ent = up.sched_ent;
-    j.sched16 = up.sched16;
-    j.up_imp = up.up_imp;
-    j.up4 = up.up4;
-    j.rs = dn.rs;
-    j.rs_row = dn.rs_row;
-    j.rs_blob = dn.rs_blob;
-    j.blob = dn.blob;
-    if constexpr (sizeof(TA) == 4)
-        j.up_diag = up.up_diag_f;
-    else
-        j.up_diag = up.up_diag_d;
+    j.dblk_off = s.dn->dblk_off;
+    j.dblk_rows = s.dn->dblk_rows;
+    j.dblk_ptr = s.dn->dblk_ptr;
+    j.dblk_mv = f32 ? (const HopEnt<TA> *)s.dn->dblk_mv_f : (const HopEnt<TA> *)s.dn->dblk_mv_d;
+    {
+        auto ch = s.dn->dblk_chunks.find(s.ld());
+        j.dblk_chunks = ch != s.dn->dblk_chunks.end() ? ch->second : nullptr;
+        j.ntiles = ch != s.dn->dblk_chunks.end() ? s.dn->dblk_nchunks.at(s.ld()) : 0;
+    }
+    j.dblk_n = s.dn->dblk_n;
+    j.dblk_max = s.dn->dblk_max;
+    j.dblk_mvmax = s.dn->dblk_mvmax;
+    j.tile0 = 0;
+    if (f32) {
+        auto sf = s.up->sched_rf.find(R);
+        j.up_sched = sf != s.up->sched_rf.end() ? (const HopEnt<TA> *)sf->second : nullptr;
+    } else {
+        auto sd = s.up->sched_rd.find(R);
+        j.up_sched = sd != s.up->sched_rd.end() ? (const HopEnt<TA> *)sd->second : nullptr;
+    }
 }
-template void hv_fill_job<float>(const mo_ed_ctx *, const Sector &, int, int, const void *, void *, HvJobT<float> &);
-template void hv_fill_job<double>(const mo_ed_ctx *, const Sector &, int, int, const void *, void *, HvJobT<double> &);
+template void hv_fill_job<float>(const mo_ed_ctx *, const Sector &, int, const void *, void *, HvJobT<float> &);
+template void hv_fill_job<double>(const mo_ed_ctx *, const Sector &, int, const void *, void *, HvJobT<double> &);
 
-template <typename TX, typename TA, typename TY, int RG, int NCW, int MINB>
-static int launch_batch(mo_ed_ctx *ctx, const StageSizes &Z, const HvBatch<TA> &b)
+template <typename TX, typename TA, typename TY, int R, int NT, int MINB>
+static int launch_batch(mo_ed_ctx *ctx, const HvBatch<TA> &b)
 {
-    const SmemLayout<TA> L = smem_layout<TA>(Z, ctx->mdl.nimp);
-    auto kern = k_hvt<TX, TA, TY, RG, NCW, MINB>;
-    int optin = 0;
-    MOED_CUDA(ctx, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
-    if ((size_t)optin < L.total) return fail(ctx, MO_ED_ERR_ARG, "H*v variant needs more shared memory than a CTA has");
-    static size_t attr_set = 0;   // per instantiation
-    if (attr_set < L.total) {
-        MOED_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total));
-        attr_set = L.total;
+    if (b.total_items <= 0) return MO_ED_OK;
+    int ldmax = 0;
+    for (int i = 0; i < b.njobs; ++i) {
+        ldmax = std::max(ldmax, b.job[i].ld);
+        if (!b.job[i].items) return fail(ctx, MO_ED_ERR_STATE, "H*v item table missing");
     }
-    const int grid = ctx->num_sms * MINB;
-    kern<<<grid, 32 * (NCW + 1), L.total, ctx->stream>>>(b, ctx->d_mdl, Z);
+    const size_t smem = dyn_smem_bytes<TX, TA, R>(ldmax, ctx->mdl);
+    auto kern = k_hv<TX, TA, TY, R, NT, MINB>;
+    MOED_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MOED_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    int per_sm = 0;
+    MOED_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem));
+    if (per_sm < 1) return fail(ctx, MO_ED_ERR_ARG, "sector rows too long for the shared-memory stage");
+    const int grid = std::min(b.total_items, ctx->num_sms * per_sm);
+    kern<<<grid, NT, smem, ctx->stream>>>(b, ctx->d_mdl);
     MOED_CHECK_LAUNCH(ctx);
     return MO_ED_OK;
+}
+
+template <typename TX, typename TA, typename TY, int R, int NT, int MINB = 1, bool SPLIT = false>
+static int launch_batch_async(mo_ed_ctx *ctx, const HvBatch<TA> &b)
+{
+    if (b.total_items <= 0) return MO_ED_OK;
+    int ldmax = 0;
+    for (int i = 0; i < b.njobs; ++i) {
+        ldmax = std::max(ldmax, b.job[i].ld);
+        if (!b.job[i].items || !b.job[i].up_sched_hdr || !b.job[i].up_sched || !b.job[i].desc)
+            return fail(ctx, MO_ED_ERR_STATE, "H*v tables missing");
+    }
+    const DescGeom g = desc_geom<TA, R>(ctx->mdl.ncpl, ctx->mdl);
+    const size_t smem = dyn_smem_bytes_async<TX, TA, R>(ldmax, ctx->mdl, g);
+    auto kern = k_hv_async<TX, TA, TY, R, NT, MINB, SPLIT>;
+    MOED_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MOED_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    int per_sm = 0;
+    MOED_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem));
+    if (per_sm < 1) return fail(ctx, MO_ED_ERR_ARG, "sector rows too long for the shared-memory stage");
+    const int grid = std::min(b.total_items, ctx->num_sms * per_sm);
+    kern<<<grid, NT, smem, ctx->stream>>>(b, ctx->d_mdl, g);
+    MOED_CHECK_LAUNCH(ctx);
+    return MO_ED_OK;
+}
+
+constexpr int kDownNT = 1024;
+constexpr size_t kDownSmemMax = 220 * 1024;   // dynamic shared memory of one k_hv_down CTA
+
+static size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
+
+// shared-memory layout of k_hv_down for blocks of up to `rows` rows and `mv`
+// moves and slices of wb bytes per row; nbuf = 1 or 2 slice buffers
+static DownLayout down_layout(int rows, int mv, size_t wb, int nbuf, size_t ent_bytes, size_t *total)
+{
+    DownLayout L;
+    size_t o = 0;
+    L.ptr = (int)o;
+    o = align16(o + sizeof(int) * ((size_t)rows + 1));
+    L.rows = (int)o;
+    o = align16(o + sizeof(int) * (size_t)rows);
+    L.mv = (int)o;
+    o = align16(o + ent_bytes * (size_t)std::max(mv, 1));
+    L.x0 = (int)o;
+    o += (size_t)rows * wb;
+    L.x1 = (int)o;
+    if (nbuf == 2) o += (size_t)rows * wb;
+    *total = o;
+    return L;
+}
+
+// Split H*v: k_hv_down writes the down-spin hybridisation into y, then
+// k_hv_async<SPLIT> adds the other terms (both on the context stream).
+template <typename TX, typename TA, typename TY, int R, int NT, int MINB, int WB>
+static int launch_batch_split(mo_ed_ctx *ctx, const HvBatch<TA> &b0)
+{
+    if (b0.total_items <= 0) return MO_ED_OK;
+    HvBatch<TA> b = b0;
+    int tiles = 0, maxrows = 0, maxmv = 0;
+    for (int i = 0; i < b.njobs; ++i) {
+        HvJobT<TA> &j = b.job[i];
+        if (!j.dblk_ptr || !j.dblk_chunks || j.dblk_n < 1 || j.ld % 32 != 0)
+            return fail(ctx, MO_ED_ERR_STATE, "H*v down-spin block tables missing");
+        j.tile0 = tiles;
+        tiles += j.ntiles;
+        maxrows = std::max(maxrows, j.dblk_max);
+        maxmv = std::max(maxmv, j.dblk_mvmax);
+    }
+    size_t smem = 0;
+    int dbuf = 1;
+    DownLayout L = down_layout(maxrows, maxmv, WB, 2, sizeof(HopEnt<TA>), &smem);
+    if (smem > kDownSmemMax) {
+        dbuf = 0;
+        L = down_layout(maxrows, maxmv, WB, 1, sizeof(HopEnt<TA>), &smem);
+    }
+    if (smem > kDownSmemMax) return fail(ctx, MO_ED_ERR_ARG, "down-spin blocks too large for the split H*v");
+    auto kd = k_hv_down<TX, TA, TY, kDownNT, WB>;
+    MOED_CUDA(ctx, cudaFuncSetAttribute(kd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MOED_CUDA(ctx, cudaFuncSetAttribute(kd, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    int per_sm = 0;
+    MOED_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kd, kDownNT, smem));
+    if (per_sm < 1) return fail(ctx, MO_ED_ERR_ARG, "down-spin blocks too large for the split H*v");
+    const int grid = std::min(tiles, ctx->num_sms * per_sm);
+    kd<<<grid, kDownNT, smem, ctx->stream>>>(b, tiles, L, maxrows, dbuf);
+    MOED_CHECK_LAUNCH(ctx);
+    return launch_batch_async<TX, TA, TY, R, NT, MINB, true>(ctx, b);
+}
+
+// Whether the split kernel fits every down-spin block of the model (any
+// electron count: at most dblk_bound rows and dblk_mv_bound moves).
+static bool split_fits(const mo_ed_ctx *ctx, size_t wb, size_t ent_bytes)
+{
+    size_t smem = 0;
+    down_layout(ctx->dblk_bound, ctx->dblk_mv_bound, wb, 1, ent_bytes, &smem);
+    return smem <= kDownSmemMax;
+}
+
+template <typename TA, int R>
+static int build_desc_r(mo_ed_ctx *ctx, Species *dn, unsigned **out)
+{
+    const DescGeom g = desc_geom<TA, R>(ctx->mdl.ncpl, ctx->mdl);
+    const int n = dn->nitems.at(R);
+    unsigned *p = nullptr;
+    MOED_CUDA(ctx, cudaMalloc(&p, sizeof(unsigned) * (size_t)g.words * std::max(n, 1)));
+    *out = p;
+    const bool f32 = sizeof(TA) == 4;
+    k_item_desc<TA, R><<<(n + 127) / 128, 128, 0, ctx->stream>>>(
+        n, dn->items.at(R), dn->info, f32 ? (const TA *)dn->diag_f : (const TA *)dn->diag_d, dn->hop_tgt,
+        f32 ? (const TA *)dn->hop_val_f : (const TA *)dn->hop_val_d, dn->n, ctx->d_mdl, g, p);
+    MOED_CHECK_LAUNCH(ctx);
+    return MO_ED_OK;
+}
+
+// item descriptors of the down species for R rows per item (k_hv_async)
+static int species_desc(mo_ed_ctx *ctx, Species *dn, int R, bool f32)
+{
+    const int key = R * 2 + (f32 ? 0 : 1);
+    if (dn->desc.count(key)) return MO_ED_OK;
+    unsigned *p = nullptr;
+    int rc;
+    switch (R) {
+    case 2: rc = f32 ? build_desc_r<float, 2>(ctx, dn, &p) : build_desc_r<double, 2>(ctx, dn, &p); break;
+    case 3: rc = f32 ? build_desc_r<float, 3>(ctx, dn, &p) : build_desc_r<double, 3>(ctx, dn, &p); break;
+    case 4: rc = f32 ? build_desc_r<float, 4>(ctx, dn, &p) : build_desc_r<double, 4>(ctx, dn, &p); break;
+    default: return fail(ctx, MO_ED_ERR_ARG, "no item descriptors for this rows-per-item");
+    }
+    if (p) dn->desc[key] = p;
+    return rc;
 }
 
 template <typename TA>
 static int launch_variant(mo_ed_ctx *ctx, int kind, int v, const HvBatch<TA> &b)
 {
-    const StageSizes Z = sizes_of(kind, v);
     if constexpr (sizeof(TA) == 4) {
         (void)kind;
         switch (v) {
-        case 0: return launch_batch<float, float, float, 5, 15, 1>(ctx, Z, b);
-        case 1: return launch_batch<float, float, float, 2, 31, 1>(ctx, Z, b);
-        case 2: return launch_batch<float, float, float, 3, 15, 1>(ctx, Z, b);
-        default: return launch_batch<float, float, float, 3, 23, 1>(ctx, Z, b);
+        case 0: return launch_batch<float, float, float, 3, 512, 2>(ctx, b);
+        case 1: return launch_batch<float, float, float, 4, 256, 2>(ctx, b);
+        case 2: return launch_batch<float, float, float, 6, 512, 1>(ctx, b);
+        case 3: return launch_batch<float, float, float, 3, 256, 3>(ctx, b);
+        case 4: return launch_batch<float, float, float, 8, 512, 1>(ctx, b);
+        case 5: return launch_batch_async<float, float, float, 4, 512>(ctx, b);
+        case 6: return launch_batch_async<float, float, float, 3, 512>(ctx, b);
+        case 7: return launch_batch_async<float, float, float, 2, 512, 2>(ctx, b);
+        case 8: return launch_batch_async<float, float, float, 2, 256, 2>(ctx, b);
+        case 9: return launch_batch_split<float, float, float, 3, 512, 1, 128>(ctx, b);
+        case 10: return launch_batch_split<float, float, float, 4, 512, 1, 128>(ctx, b);
+        default: return launch_batch_split<float, float, float, 3, 512, 1, 64>(ctx, b);
         }
     } else if (kind == HV_F64) {
         switch (v) {
-        case 0: return launch_batch<double, double, double, 3, 15, 1>(ctx, Z, b);
-        case 1: return launch_batch<double, double, double, 5, 15, 1>(ctx, Z, b);
-        default: return launch_batch<double, double, double, 3, 7, 2>(ctx, Z, b);
+        case 0: return launch_batch<double, double, double, 2, 256, 2>(ctx, b);
+        case 1: return launch_batch<double, double, double, 3, 256, 1>(ctx, b);
+        case 2: return launch_batch<double, double, double, 2, 512, 1>(ctx, b);
+        case 3: return launch_batch_async<double, double, double, 2, 512>(ctx, b);
+        case 4: return launch_batch_async<double, double, double, 4, 512>(ctx, b);
+        case 5: return launch_batch_split<double, double, double, 2, 512, 1, 128>(ctx, b);
+        default: return launch_batch_split<double, double, double, 2, 512, 1, 64>(ctx, b);
         }
     } else {
         switch (v) {
-        case 0: return launch_batch<float, double, double, 3, 15, 1>(ctx, Z, b);
-        case 1: return launch_batch<float, double, double, 5, 15, 1>(ctx, Z, b);
-        default: return launch_batch<float, double, double, 3, 7, 2>(ctx, Z, b);
+        case 0: return launch_batch<float, double, double, 2, 256, 2>(ctx, b);
+        case 1: return launch_batch<float, double, double, 3, 256, 1>(ctx, b);
+        case 2: return launch_batch<float, double, double, 2, 512, 1>(ctx, b);
+        case 3: return launch_batch_async<float, double, double, 2, 512>(ctx, b);
+        case 4: return launch_batch_async<float, double, double, 4, 512>(ctx, b);
+        case 5: return launch_batch_split<float, double, double, 2, 512, 1, 128>(ctx, b);
+        default: return launch_batch_split<float, double, double, 2, 512, 1, 64>(ctx, b);
         }
     }
 }
 
-static int nparts_of(const mo_ed_ctx *ctx, int kind, int v) { return ctx->num_sms * variant(kind, v).MINB; }
-
 template <typename TA>
 static int hv_run_jobs(mo_ed_ctx *ctx, int kind, int v, const HvJobT<TA> *jobs, int njobs)
 {
-    if (int rc = ensure_err(ctx)) return rc;
     HvBatch<TA> b;
-    memset(&b, 0, sizeof(b));
-    b.err = (int *)ctx->d_err.p;
+    b.njobs = 0;
+    b.total_items = 0;
     for (int i = 0; i < njobs; ++i) {
-        if (!jobs[i].tiles) return fail(ctx, MO_ED_ERR_STATE, "H*v tile list of a job not built");
         if (b.njobs == kMaxJobs) {
             if (int rc = launch_variant<TA>(ctx, kind, v, b)) return rc;
             b.njobs = 0;
-            b.total = 0;
+            b.total_items = 0;
         }
         b.job[b.njobs] = jobs[i];
-        b.job[b.njobs].tile0 = b.total;
-        b.total += jobs[i].ntiles;
+        b.job[b.njobs].item0 = b.total_items;
+        b.total_items += jobs[i].nitems;
         b.njobs++;
     }
     if (b.njobs == 0) return MO_ED_OK;
@@ -953,27 +1469,42 @@ int hv_launch_f64(mo_ed_ctx *ctx, int kind, int v, const HvJobT<double> *jobs, i
 
 static int launch_one(mo_ed_ctx *ctx, const Sector &s, int kind, int v, const void *x, void *y)
 {
+    const int R = variant(kind, v).R;
     if (kind == HV_F32) {
         HvJobT<float> j;
-        hv_fill_job<float>(ctx, s, kind, v, x, y, j);
+        hv_fill_job<float>(ctx, s, R, x, y, j);
         return hv_launch_f32(ctx, v, &j, 1);
     }
     HvJobT<double> j;
-    hv_fill_job<double>(ctx, s, kind, v, x, y, j);
+    hv_fill_job<double>(ctx, s, R, x, y, j);
     return hv_launch_f64(ctx, kind, v, &j, 1);
 }
 
+// tables variant v of `kind` reads for sector s: the item table of its R,
+// and for the staged kernel the up-spin schedule and the item descriptors
 static int prepare_variant(mo_ed_ctx *ctx, const Sector &s, int kind, int v)
 {
-    const HvTile *t;
+    const HvVariant &h = variant(kind, v);
+    const int *items;
     int n;
-    return hv_tile_list(ctx, s, kind, v, &t, &n);
+    if (int rc = species_items(ctx, s.dn, h.R, &items, &n)) return rc;
+    if (!h.staged) return MO_ED_OK;
+    if (h.staged >= 2) {
+        // the split kernel stages whole down-spin blocks: the largest block of
+        // the model (any electron count) must fit one CTA's shared memory
+        const size_t wb = h.staged == 2 ? 128 : 64;
+        if (!split_fits(ctx, wb, kind == HV_F32 ? sizeof(HopEnt<float>) : sizeof(HopEnt<double>)))
+            return fail(ctx, MO_ED_ERR_ARG, "down-spin blocks too large for the split H*v");
+        if (int rc = species_dblocks(ctx, s.dn, s.ld())) return rc;
+    }
+    if (int rc = species_sched(ctx, s.up, h.R)) return rc;
+    return species_desc(ctx, s.dn, h.R, kind == HV_F32);
 }
 
-// Time every variant on sector s and keep the fastest.
+// Time every variant once on sector s and keep the fastest.
 static int tune(mo_ed_ctx *ctx, const Sector &s, int kind, int *best)
 {
-    const size_t ex = x_size(kind);
+    const size_t ex = kind == HV_F64 ? sizeof(double) : sizeof(float);
     const size_t ey = kind == HV_F32 ? sizeof(float) : sizeof(double);
     DevBuf dx, dy;
     if (int rc = dev_alloc(ctx, dx, ex * (size_t)s.Dpad())) return rc;
@@ -988,10 +1519,10 @@ static int tune(mo_ed_ctx *ctx, const Sector &s, int kind, int *best)
     times.assign(nvariants(kind), -1.0f);
     for (int v = 0; v < nvariants(kind); ++v) {
         if (int rc = prepare_variant(ctx, s, kind, v)) {
-            if (rc == MO_ED_ERR_ARG) continue;   // a block does not fit this variant's stage
+            if (rc == MO_ED_ERR_ARG) continue;   // variant not applicable to this model
             return rc;
         }
-        if (launch_one(ctx, s, kind, v, dx.p, dy.p) != MO_ED_OK) {
+        if (launch_one(ctx, s, kind, v, dx.p, dy.p) != MO_ED_OK) {   // variant does not fit this sector
             cudaGetLastError();
             continue;
         }
@@ -1014,14 +1545,11 @@ static int tune(mo_ed_ctx *ctx, const Sector &s, int kind, int *best)
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (*best < 0) return fail(ctx, MO_ED_ERR_ARG, "no H*v tile shape fits this sector");
-    int herr = 0;
-    MOED_CUDA(ctx, cudaMemcpy(&herr, ctx->d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
-    if (herr) return fail(ctx, MO_ED_ERR_CUDA, "H*v stage wait timed out");
     ctx->err.clear();
     return MO_ED_OK;
 }
 
-int hv_prepare(mo_ed_ctx *ctx, const Sector &s, int kind, int *v_out, int *nparts)
+int hv_prepare(mo_ed_ctx *ctx, const Sector &s, int kind, int *v_out, int *R_out)
 {
     const long long key = shape_key(kind, s);
     auto it = ctx->hv_choice.find(key);
@@ -1036,10 +1564,9 @@ int hv_prepare(mo_ed_ctx *ctx, const Sector &s, int kind, int *v_out, int *npart
         if (int rc = tune(ctx, s, kind, &v)) return rc;
         ctx->hv_choice[key] = v;
     }
-    if (int rc = ensure_err(ctx)) return rc;
     if (int rc = prepare_variant(ctx, s, kind, v)) return rc;
     if (v_out) *v_out = v;
-    if (nparts) *nparts = nparts_of(ctx, kind, v);
+    if (R_out) *R_out = variant(kind, v).R;
     return MO_ED_OK;
 }
 
@@ -1053,27 +1580,35 @@ int hv_tuning(mo_ed_ctx *ctx, const Sector &s, int kind, int cap, int *nvar, int
     for (int i = 0; i < *nvar && i < cap; ++i) {
         const HvVariant &h = variant(kind, i);
         if (shape) {
-            shape[4 * i] = h.RG;
-            shape[4 * i + 1] = 32 * (h.NCW + 1);
+            shape[4 * i] = h.R;
+            shape[4 * i + 1] = h.NT;
             shape[4 * i + 2] = h.MINB;
-            shape[4 * i + 3] = h.TR;
+            shape[4 * i + 3] = h.staged;
         }
         if (ms) ms[i] = i < (int)t.size() ? t[i] : -1.0f;
     }
     return MO_ED_OK;
 }
 
-int hv_prepare_rows(mo_ed_ctx *ctx, const Sector &s, int kind, int v) { return prepare_variant(ctx, s, kind, v); }
+int hv_prepare_rows(mo_ed_ctx *ctx, const Sector &s, int kind, int v)
+{
+    return prepare_variant(ctx, s, kind, v);
+}
 
-int hv_lookup(mo_ed_ctx *ctx, const Sector &s, int kind, int *v_out, int *nparts)
+int hv_lookup(mo_ed_ctx *ctx, const Sector &s, int kind, int *v_out, int *R_out)
 {
     auto it = ctx->hv_choice.find(shape_key(kind, s));
     if (it == ctx->hv_choice.end())
         return fail(ctx, MO_ED_ERR_STATE, "H*v tile shape of this sector not chosen yet");
-    if (!ctx->hv_tiles.count(tile_key(s, kind, it->second)) || !ctx->d_err.p)
-        return fail(ctx, MO_ED_ERR_STATE, "H*v tile list of this sector not built yet");
+    const HvVariant &h = variant(kind, it->second);
+    const int R = h.R;
+    bool ready = s.dn->items.count(R) != 0;
+    if (h.staged)
+        ready = ready && s.up->sched_rf.count(R) && s.dn->desc.count(R * 2 + (kind == HV_F32 ? 0 : 1));
+    if (h.staged >= 2) ready = ready && s.dn->dblk_ptr != nullptr && s.dn->dblk_chunks.count(s.ld());
+    if (!ready) return fail(ctx, MO_ED_ERR_STATE, "H*v item table of this sector not built yet");
     if (v_out) *v_out = it->second;
-    if (nparts) *nparts = nparts_of(ctx, kind, it->second);
+    if (R_out) *R_out = R;
     return MO_ED_OK;
 }
 

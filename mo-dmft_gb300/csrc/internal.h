@@ -2,27 +2,26 @@
 //
 // Data layout in HBM
 //   A sector vector X of dimension D = nup*ndown is stored on the device as
-//   ndown rows (down-spin ranks in the reference's order, ed_basis.F90:120-123)
-//   of row stride ld.  Within a row the up-spin ranks are permuted into
-//   "conserved-block order": hybridisation keeps the electron count of every
-//   conserved subsystem (an impurity orbital with the bath levels coupled to
-//   it), so the up-spin words with equal counts (a block) are closed under
-//   up-spin moves.  Blocks are stored one after the other, each padded to a
-//   multiple of 4 columns (16-byte aligned starts); inside a block the column
-//   index is the mixed-radix number of the subsystems' local states, the last
-//   subsystem fastest.  Species::pos maps an up rank to its column,
-//   Species::rank_at a column back to its rank (-1 on pads, which are zero).
-//   Host entry points convert to and from the reference layout on the device
-//   through a staging buffer.
+//   ndown rows of nup elements, X[idown][iup] -- the reference's row order
+//   (ed_basis.F90:120-123,137-138: row index iup + (idown-1)*nup) -- with the
+//   row stride padded to ld = roundup(nup, 32) so that every row starts on a
+//   128-byte boundary (pad elements are zero).  Host entry points convert to
+//   and from the unpadded reference layout with one 2D copy.  Every H*v term
+//   that moves only up-spin electrons stays inside a row; down-spin moves are
+//   whole-row AXPYs.
 //
-//   Per spin species (nsite sites, N electrons) the device holds the words,
-//   the inverse rank table, the column permutation and the H*v tables of
-//   both roles: as the up spin (columns) the conflict-free gather schedule of
-//   every block, the species diagonal and impurity pattern per column and the
-//   spin-flip / pair-hop partner columns; as the down spin (rows) the "row
-//   sets" -- rows of a block with equal local states in its leading
-//   subsystems -- with their moves split into moves inside the set and moves
-//   to other rows.
+//   Per spin species (nsite sites, N electrons) the device holds
+//     words[n]          ascending state words (colex unrank),
+//     rank[2^nsite]     inverse table (-1 outside the species),
+//     hop_tgt/val[hw][n] up to hw compacted hybridisation moves per word
+//                        (slot-major so a warp reading slot s of 32
+//                        consecutive words is coalesced),
+//     hop_cnt[n]        number of valid moves,
+//     diag[n]           species part of the diagonal.
+//   Because the impurity orbitals are the lowest bits, words sharing their
+//   bath bits are contiguous in rank order ("bath groups"); spin-flip and
+//   pair-hopping only move within a bath group by a rank offset that depends
+//   on the impurity bits alone, kept in a 2^norb-entry table.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -61,85 +60,74 @@ struct ModelDev {
 // ---------------------------------------------------------------------------
 // spin species tables
 // ---------------------------------------------------------------------------
-constexpr int kMaxSub = 8;        // conserved subsystems handled by the block layout
-constexpr int kMaxCoef = 1 + 2 * kMaxHop;   // coupling table: 0, then +-V per coupling
-
-// An up-spin block as the kernel sees it: first column, padded width, first
-// schedule header (4 per 128-column chunk, one per column k = 0..3 of a quad).
-struct UpBlock {
-    int col0, W4, hdr0, W;
-    // the block's gather schedule in 16-bit form (0 bytes when a target or a
-    // coupling index does not fit): offset in 16-byte units into
-    // Species::sched16 and size.  Layout: one word per (64-column chunk, k) =
-    // first entry (in entries from the first entry word) << 8 | slots, then
-    // the entries: target column | coupling index << 10.
-    int s16_off, s16_bytes, pad0, pad1;
+template <typename T>
+struct HopEnt;                    // one up-spin move of a column: target rank and signed coupling
+template <>
+struct alignas(8) HopEnt<float> {
+    int t;
+    float v;
 };
-
-// Row-set geometry of one down-spin block (host): at level j the rows are
-// grouped by the local states of the first j subsystems in the block's row
-// axis order; level nsub is one row per set.
-struct DownBlock {
-    int size;                     // rows in the block
-    int rs0[kMaxSub + 1];         // first row set of each level
-    int rs_rows[kMaxSub + 1];     // rows per set at each level
-    int nset[kMaxSub + 1];        // sets at each level
-    int blob_max[kMaxSub + 1];    // largest metadata blob of a set at each level (bytes)
-    int cnt[kMaxSub];             // electrons per subsystem (block key)
+template <>
+struct alignas(16) HopEnt<double> {
+    int t, pad;
+    double v;
 };
-
-// Metadata blob of one row set (16-byte aligned sections), copied into
-// shared memory with the tile:
-//   int4 header {rows g, byte offset of the moves, byte offset of the
-//                4-operator terms, total bytes}
-//   int4 info[g] {impurity pattern | moves in the set << 8 | moves to other
-//                 rows << 16 | 4-operator terms << 24, first move, first
-//                 4-operator term, row rank}
-//   double diag[g]    species diagonal of the row
-//   unsigned moves[]  row (index within the set for moves inside it, rank
-//                     otherwise) | coupling index << 16; moves inside the set first
-//   unsigned q4[]     4-operator terms: partner rank | pair << 16 | pair hop
-//                     << 21 | negative sign << 22 (spin-flip uses T_{j<-i},
-//                     pair hop T_{i<-j} of the row)
 
 struct Species {
-    int nsite = 0, N = 0, n = 0;
-    int nsub = 0;
-    int ncol = 0;                 // sum of padded block widths
-    int ld = 0;                   // row stride when this species is the up spin (roundup(ncol, 32))
-    int *words = nullptr;         // [n] ascending words (device)
-    int *rank = nullptr;          // [2^nsite] rank of a word, -1 outside the species
-    int *pos = nullptr;           // [n] column of each rank
-    int *rank_at = nullptr;       // [ld] rank at each column, -1 on pads
-    std::vector<int> h_words, h_pos, h_rank_at;
-    // ---- up-spin role (columns) ----
-    std::vector<UpBlock> h_ublk;
-    std::vector<int> h_ublk_cnt;  // [nblk * kMaxSub] electrons per subsystem
-    UpBlock *ublk = nullptr;
-    // gather schedule: header (block, 64-column chunk, k) = {first entry,
-    // slots}; entry (slot s, quad l) at first + 16*s + l = target column
-    // within the block | coupling index << 16 (index 0: no move, coupling 0)
-    // of column 4*l + k of the chunk.  The 16 targets of one slot are
-    // distinct mod 16: with shared-memory row pitches = 16 (mod 32), the two
-    // half-warps reading two rows hit 32 different banks.
+    int nsite = 0, N = 0, n = 0, hw = 0;
+    int n_pad = 0;                // roundup(n, 32): row stride when this species is the up spin
+    int *words = nullptr;
+    int *rank = nullptr;
+    int *hop_cnt = nullptr;
+    int *hop_tgt = nullptr;       // [hw][n]
+    double *hop_val_d = nullptr;  // [hw][n]
+    float *hop_val_f = nullptr;
+    int *info = nullptr;          // [n_pad]: hop count | impurity bits << 8 (pads: 0)
+    double *diag_d = nullptr;     // [n_pad] (pads: 0)
+    float *diag_f = nullptr;
+    // column move tables, chunk-major: entry (chunk c = u/4, slot s, u%4) at
+    // (c*hw + s)*4 + u%4, so one thread reads the slot-s moves of its four
+    // columns as one contiguous 32-byte (FP32) / 64-byte (FP64) block
+    HopEnt<float> *tab_f = nullptr;
+    HopEnt<double> *tab_d = nullptr;
+    // conflict-free gather schedule of the up-spin moves: per 32-column chunk
+    // c, sched_hdr[c] = {first entry, slots}; entry (slot s, lane l) at
+    // first + 32*s + l is 0 (no move) or valid | neg << 22 | coupling << 16 |
+    // target rank.  Within a slot the 32 targets fall in 32 different
+    // shared-memory banks (target mod 32).
     int2 *sched_hdr = nullptr;
     unsigned *sched_ent = nullptr;
+    std::vector<int2> h_sched_hdr;    // host copies (per-R tables derive from them)
+    std::vector<unsigned> h_sched_ent;
     int sched_slots_max = 0;
-    unsigned char *sched16 = nullptr;   // 16-bit schedules of the blocks (UpBlock::s16_off)
-    double *up_diag_d = nullptr;  // [ld] species diagonal per column (pads 0)
-    float *up_diag_f = nullptr;
-    unsigned char *up_imp = nullptr;  // [ld] impurity pattern per column
-    // [npair][ld] up transfer T_{i<-j} of pair p = (i,j) per column: bit 31
-    // valid, bit 30 negative sign, low 16 bits the partner column
-    unsigned *up4 = nullptr;
-    // ---- down-spin role (rows) ----
-    std::vector<DownBlock> h_dblk;
-    int nrs = 0, nrec = 0;
-    int2 *rs = nullptr;           // [nrs] {first row record, rows}
-    int *rs_row = nullptr;        // [nrec] row (rank)
-    int2 *rs_blob = nullptr;      // [nrs] {byte offset / 16, bytes} of the set's metadata blob
-    unsigned char *blob = nullptr;
-    std::vector<int2> h_rs, h_rs_blob;   // host copies (tile descriptors)
+    // per rows-per-item R: the schedule as {shared-memory offset of row 0 in
+    // the [tile][R][32] stage, signed coupling}; empty lanes read a bank that
+    // no other lane of the slot uses, with coupling 0
+    std::map<int, HopEnt<float> *> sched_rf;
+    std::map<int, HopEnt<double> *> sched_rd;
+    int max_cnt = 0;              // largest hop_cnt over words
+    int max_group = 0;            // largest bath group (words sharing their bath bits)
+    // row items for a given rows-per-item R: whole bath groups packed into
+    // items of <= R rows (rank order inside a group), items sorted by the
+    // bath-occupation counts of the conserved subsystems; -1 pads
+    std::map<int, int *> items;   // R -> [nitems][R]
+    // per-item descriptors of the staged H*v kernel, key R*2 + (FP64 ? 1 : 0)
+    std::map<int, unsigned *> desc;
+    std::map<int, int> nitems;
+    // down-spin blocks of the split H*v: rows with equal electron counts in
+    // every conserved subsystem, closed under hybridisation moves.  Positions
+    // p run over the rows block by block (largest block first).
+    int dblk_n = 0, dblk_max = 0, dblk_mvmax = 0;  // blocks, largest block, most moves in a block
+    int *dblk_off = nullptr;      // [dblk_n + 1] first position of each block
+    int *dblk_rows = nullptr;     // [n] row (rank) at position p
+    int *dblk_ptr = nullptr;      // [n + 1] first move of position p
+    // moves of each position: {target index within the block, signed coupling}
+    HopEnt<float> *dblk_mv_f = nullptr;
+    HopEnt<double> *dblk_mv_d = nullptr;
+    // per row stride ld: {first chunk, 32-column units per chunk} of each block
+    std::map<int, int2 *> dblk_chunks;
+    std::map<int, int> dblk_nchunks;
+    std::vector<int> dblk_h_off;  // host copy of dblk_off
     ~Species();
 };
 
@@ -147,40 +135,41 @@ struct Sector {
     int ne_up, ne_down;
     Species *up, *dn;
     long long D() const { return (long long)up->n * dn->n; }     // dimension
-    int ld() const { return up->ld; }                              // device row stride
-    long long Dpad() const { return (long long)up->ld * dn->n; }   // device elements
+    int ld() const { return up->n_pad; }                           // device row stride
+    long long Dpad() const { return (long long)up->n_pad * dn->n; } // device elements
 };
 
 // ---------------------------------------------------------------------------
 // H*v job (one vector of one sector); the kernel walks a list of jobs
 // ---------------------------------------------------------------------------
-// A tile: one row set of the down species times one up block.
-struct HvTile {
-    int rs0, rows, blob16, blob_bytes;   // row set: first row record, rows, metadata blob (16-byte units, bytes)
-    int col0, W4, hdr0, s16_off;         // up block (UpBlock fields)
-    int s16_bytes, ub, pad0, pad1;
-};
-
 template <typename TA>
 struct HvJobT {
     const void *x;            // input vector (TX), device layout
     void *y;                  // output vector (TY), device layout
-    double *dot_partial;      // optional [grid]: per CTA, sum of x*y over its tiles
+    double *dot_partial;      // optional [nitems]: sum over the item of x*y
     const int *active;        // optional device flag: job skipped when *active == 0
-    int ld, ncol, nrow;       // row stride, columns covered by blocks (the rest is pad), rows
-    int tile0, ntiles;        // this job's tiles in the batch (tile0 set at launch)
-    const HvTile *tiles;
-    const UpBlock *ublk;
-    const int2 *sched_hdr;
-    const unsigned *sched_ent;
-    const unsigned char *sched16;
-    const TA *up_diag;
-    const unsigned char *up_imp;
-    const unsigned *up4;
-    const int2 *rs;
-    const int *rs_row;
-    const int2 *rs_blob;
-    const unsigned char *blob;
+    int nu, nd, ld;
+    int item0, nitems;
+    const int *items;         // [nitems][R] rows of each item (-1 pads)
+    const int *up_info;       // [ld]: move count | impurity bits << 8
+    const HopEnt<TA> *up_tab; // chunk-major column moves
+    const TA *up_diag;        // [ld]
+    int up_hw, up_maxcnt;
+    const int *dn_info;       // [nd]
+    const int *dn_tgt;        // [hw][nd]
+    const TA *dn_val;         // [hw][nd]
+    const TA *dn_diag;        // [nd]
+    int dn_maxcnt, pad;
+    const int2 *up_sched_hdr;      // conflict-free gather schedule (Species::sched_*)
+    const unsigned *up_sched_ent;
+    const HopEnt<TA> *up_sched;
+    const unsigned *desc;          // per-item descriptors (staged kernel)
+    // down-spin blocks of the split kernel (Species::dblk_*)
+    const int *dblk_off, *dblk_rows, *dblk_ptr;
+    const HopEnt<TA> *dblk_mv;
+    const int2 *dblk_chunks;
+    int dblk_n, dblk_max, dblk_mvmax;
+    int tile0, ntiles;             // this job's chunks in the batch (split kernel)
 };
 
 // ---------------------------------------------------------------------------
@@ -249,7 +238,8 @@ struct mo_ed_ctx {
     std::vector<int> cpl_orb, cpl_bath;  // nonzero couplings in reference loop order
     std::vector<double> cpl_val;
     std::vector<int> site_subsys;  // conserved subsystem (orbital + coupled bath levels) of each site
-    int nsub = 0;                  // number of conserved subsystems (<= kMaxSub)
+    int dblk_bound = 0;            // largest down-spin block over every electron count
+    int dblk_mv_bound = 0;         // most hybridisation moves in one such block
     std::map<int, std::unique_ptr<moed::Species>> species;  // by N
 
     // statistics of the last eigensolve (mo_ed_diag_stats)
@@ -269,13 +259,8 @@ struct mo_ed_ctx {
     moed::DevBuf d_hk;
     int nq = 0;
 
-    // scratch; stage: the reference-layout copy of a host vector on its way
-    // to or from the device layout
-    moed::DevBuf scratch_a, scratch_b, scratch_part, stage;
-    // H*v tile lists per (sector, stage budget): key -> (tiles, count)
-    std::map<long long, std::pair<moed::DevBuf, int>> hv_tiles;
-    // device word set by a kernel whose bounded wait ran out (0: none)
-    moed::DevBuf d_err;
+    // scratch
+    moed::DevBuf scratch_a, scratch_b, scratch_part;
     // eigensolver workspace reused across sectors (Krylov vectors of sectors
     // up to 64 MB per vector, and the projected-problem arrays)
     std::vector<moed::DevBuf> trl_pool, trl_small, rr_pool;
@@ -305,21 +290,9 @@ int cuda_fail(mo_ed_ctx *ctx, cudaError_t e, const char *what);
 int dev_alloc(mo_ed_ctx *ctx, DevBuf &b, size_t bytes);
 int ensure(mo_ed_ctx *ctx, DevBuf &b, size_t bytes);
 // host vector in the reference layout (D contiguous) <-> device vector in the
-// device layout (ndown rows of stride ld, up ranks at their block columns,
-// zero pads); es = element size.  The copy goes through a device staging
-// area of D elements: `stage` when given (nothing is allocated), else the
-// context's staging buffer.
-int upload_padded(mo_ed_ctx *ctx, const Sector &s, const void *host, void *dev, size_t es,
-                  void *stage = nullptr);
-int download_padded(mo_ed_ctx *ctx, const Sector &s, const void *dev, void *host, size_t es,
-                    void *stage = nullptr);
-// device-side permutations between the reference layout (D contiguous) and
-// the device layout
-int to_device_layout(mo_ed_ctx *ctx, const Sector &s, const void *ref, void *dev, size_t es);
-int to_reference_layout(mo_ed_ctx *ctx, const Sector &s, const void *dev, void *ref, size_t es);
-// FP64 host vector (reference layout) -> FP32 device vector (device layout)
-int upload_f64_to_f32(mo_ed_ctx *ctx, const Sector &s, const double *host, float *dev, void *stage = nullptr);
-int to_device_layout_f64_f32(mo_ed_ctx *ctx, const Sector &s, const double *ref, float *dev);
+// padded layout (ndown rows of stride ld, zero pads); es = element size.
+int upload_padded(mo_ed_ctx *ctx, const Sector &s, const void *host, void *dev, size_t es);
+int download_padded(mo_ed_ctx *ctx, const Sector &s, const void *dev, void *host, size_t es);
 
 // ---- tables (tables.cu) ----------------------------------------------------
 long long binom(int n, int k);
@@ -336,33 +309,37 @@ int basis_idx_dev(mo_ed_ctx *ctx, const Sector &s, long long n, const unsigned *
 
 // ---- H*v (hv.cu) ------------------------------------------------------------
 enum HvKind { HV_F64 = 0, HV_F32 = 1, HV_MIXED = 2 };
-// Fill a job for sector s (x, y device pointers) under tile-shape variant v
-// (its tile list must exist: hv_prepare / hv_prepare_rows).
+// Fill a job for sector s (x, y device pointers) with R rows per item (the
+// item table for R must exist: hv_prepare / hv_prepare_rows).
 template <typename TA>
-void hv_fill_job(const mo_ed_ctx *ctx, const Sector &s, int kind, int v, const void *x, void *y,
-                 HvJobT<TA> &job);
-// Launch H*v over a host list of jobs (tile0 is assigned here); jobs are
+void hv_fill_job(const mo_ed_ctx *ctx, const Sector &s, int R, const void *x, void *y, HvJobT<TA> &job);
+// Launch H*v over a host list of jobs (item0 is assigned here); jobs are
 // passed to the kernel by value, so the call can be captured in a CUDA graph.
+// v = tile-shape variant (hv_prepare); all jobs use its rows per item.
 int hv_launch_f32(mo_ed_ctx *ctx, int v, const HvJobT<float> *jobs, int njobs);
 int hv_launch_f64(mo_ed_ctx *ctx, int kind, int v, const HvJobT<double> *jobs, int njobs);
+int species_items(mo_ed_ctx *ctx, Species *sp, int R, const int **items, int *nitems);
 // Tile-shape variant for sector s (autotuned on the first call per shape;
 // that first call allocates and synchronizes, so make it before any stream
-// capture), its number of dot-product partials (the grid size), and the tile
-// list of the sector.
-int hv_prepare(mo_ed_ctx *ctx, const Sector &s, int kind, int *v, int *nparts);
-// autotuner record of a shape: per variant (RG, threads, MINB, stage rows) and time in ms
+// capture) and its rows per item; builds the item table.
+int hv_prepare(mo_ed_ctx *ctx, const Sector &s, int kind, int *v, int *R);
+// autotuner record of a shape: per variant (R, NT, MINB) and time in ms
 int hv_tuning(mo_ed_ctx *ctx, const Sector &s, int kind, int cap, int *nvar, int *shape, float *ms, int *chosen);
-// tile list of variant v for a sector batched with the one v was tuned on
+// tables of variant v (item table, schedule, descriptors) for a sector
+// batched with the one v was tuned on
 int hv_prepare_rows(mo_ed_ctx *ctx, const Sector &s, int kind, int v);
-// Lookup only: the variant and tile list that hv_prepare left for this sector
-// and kind, or MO_ED_ERR_STATE if it never ran (never tunes or allocates).
-int hv_lookup(mo_ed_ctx *ctx, const Sector &s, int kind, int *v, int *nparts);
+// Per-R stage offsets of the up-spin gather schedule (built once per R).
+int species_sched(mo_ed_ctx *ctx, Species *sp, int R);
+// Down-spin block tables of a species (split H*v), built once; chunk table
+// for row stride ld.
+int species_dblocks(mo_ed_ctx *ctx, Species *sp, int ld);
+// Lookup only: the tile shape and item table that hv_prepare left for this
+// sector and kind, or MO_ED_ERR_STATE if it never ran (never tunes or allocates).
+int hv_lookup(mo_ed_ctx *ctx, const Sector &s, int kind, int *v, int *R);
 // Pin the tile-shape variant of a sector and kind (instead of the autotuner's choice).
 int hv_set_variant(mo_ed_ctx *ctx, const Sector &s, int kind, int v);
-// Convenience: one vector.
+// Convenience: one vector, jobs staged through scratch.
 int hv_single(mo_ed_ctx *ctx, const Sector &s, int kind, const void *x, void *y);
-// Tile list of a sector for tile-shape variant v of `kind` (built once).
-int hv_tile_list(mo_ed_ctx *ctx, const Sector &s, int kind, int v, const HvTile **tiles, int *ntiles);
 
 // ---- Krylov (krylov.cu) -----------------------------------------------------
 int lanczos_reference(mo_ed_ctx *ctx, const Sector &s, const double *h_vec, int nstep,
@@ -370,7 +347,7 @@ int lanczos_reference(mo_ed_ctx *ctx, const Sector &s, const double *h_vec, int 
 // The same recurrence with every device buffer carved from the caller's
 // region [scratch, scratch + cap) (256-byte aligned).  Needs hv_lookup to
 // succeed for the sector; allocates no device memory.  Bytes needed:
-size_t lanczos_region_bytes(const Sector &s, int prec, int nstep, int hv_parts);
+size_t lanczos_region_bytes(const Sector &s, int prec, int nstep, int hv_rows);
 // Look up (and so commit) the no-allocation region on the context's device.
 int noalloc_prepare(mo_ed_ctx *ctx);
 int lanczos_region_preload(mo_ed_ctx *ctx);

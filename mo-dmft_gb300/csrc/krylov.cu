@@ -298,14 +298,14 @@ int lz_setup(mo_ed_ctx *ctx, LzBatch &b, const std::vector<Sector> &secs, int pr
     int big = 0;
     for (int r = 1; r < nrun; ++r)
         if (secs[r].D() > secs[big].D()) big = r;
-    if (int rc = hv_prepare(ctx, secs[big], kind, &b.hv_variant, &b.hv_parts)) return rc;
+    if (int rc = hv_prepare(ctx, secs[big], kind, &b.hv_variant, &b.hv_rows)) return rc;
     for (int r = 0; r < nrun; ++r) {
         if (int rc = hv_prepare_rows(ctx, secs[r], kind, b.hv_variant)) return rc;
         b.upd_item0[r] = b.upd_total;
         b.upd_nitems[r] = (int)((secs[r].Dpad() + kVecChunk - 1) / kVecChunk);
         b.upd_total += b.upd_nitems[r];
         b.hv_item0[r] = b.hv_total;
-        b.hv_nitems[r] = b.hv_parts;
+        b.hv_nitems[r] = secs[r].dn->nitems.at(b.hv_rows);
         b.hv_total += b.hv_nitems[r];
     }
     if (int rc = dev_alloc(ctx, b.upd_part, sizeof(double) * std::max(1, b.upd_total))) return rc;
@@ -348,7 +348,7 @@ static int lz_enqueue(mo_ed_ctx *ctx, LzBatch &b, LzBatchDev &d)
     for (int k = 0; k < 3; ++k) {
         jobs[k].resize(nrun);
         for (int r = 0; r < nrun; ++r) {
-            hv_fill_job<T>(ctx, b.sec[r], kind, b.hv_variant, d.run[r].u[k], d.run[r].w, jobs[k][r]);
+            hv_fill_job<T>(ctx, b.sec[r], b.hv_rows, d.run[r].u[k], d.run[r].w, jobs[k][r]);
             jobs[k][r].dot_partial = d.run[r].hv_part;
             jobs[k][r].active = d.run[r].active;
         }
@@ -438,9 +438,12 @@ int lanczos_reference(mo_ed_ctx *ctx, const Sector &s, const double *h_vec, int 
     const int prec = ctx->opt.precision;
     if (int rc = lz_setup(ctx, lb, {s}, prec, nstep)) return rc;
     const long long Dp = s.Dpad();
-    (void)Dp;
     if (prec == MO_ED_FP32) {
-        if (int rc = upload_f64_to_f32(ctx, s, h_vec, (float *)lz_start_vector(lb, 0))) return rc;
+        if (int rc = ensure(ctx, ctx->scratch_a, sizeof(double) * Dp)) return rc;
+        if (int rc = upload_padded(ctx, s, h_vec, ctx->scratch_a.p, sizeof(double))) return rc;
+        if (int rc = convert_f64_to_f32(ctx, (const double *)ctx->scratch_a.p,
+                                        (float *)lz_start_vector(lb, 0), Dp))
+            return rc;
     } else {
         if (int rc = upload_padded(ctx, s, h_vec, lz_start_vector(lb, 0), sizeof(double))) return rc;
     }
@@ -457,8 +460,8 @@ int lanczos_reference(mo_ed_ctx *ctx, const Sector &s, const double *h_vec, int 
 
 // The same recurrence inside a caller-provided device region.  Layout, each
 // part starting on a 256-byte boundary: a and nrm [nstep+1] each, the two
-// flags, the update and H*v partial sums, u_0, u_1 u_2 (adjacent; they first
-// stage the FP64 start vector in the reference layout on its way to u_0) and w.
+// flags, the update and H*v partial sums, u_0, u_1 u_2 (adjacent; for FP32
+// runs they first hold the FP64 start vector before its conversion) and w.
 namespace {
 struct LzRegion {
     size_t coef, flags, upd, hv, u0, u12, w, end;
@@ -466,12 +469,12 @@ struct LzRegion {
 
 size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-LzRegion lz_region(const Sector &s, int prec, int nstep, int hv_parts)
+LzRegion lz_region(const Sector &s, int prec, int nstep, int hv_rows)
 {
     const size_t es = prec == MO_ED_FP32 ? sizeof(float) : sizeof(double);
     const size_t Dp = (size_t)s.Dpad();
     const size_t upd_n = (Dp + kVecChunk - 1) / kVecChunk;
-    const size_t hv_n = (size_t)std::max(1, hv_parts);
+    const size_t hv_n = (size_t)std::max(1, s.dn->nitems.at(hv_rows));
     LzRegion r;
     r.coef = 0;
     r.flags = up256(r.coef + sizeof(double) * 2 * (size_t)(nstep + 1));
@@ -508,9 +511,9 @@ int lanczos_region_preload(mo_ed_ctx *ctx)
     return MO_ED_OK;
 }
 
-size_t lanczos_region_bytes(const Sector &s, int prec, int nstep, int hv_parts)
+size_t lanczos_region_bytes(const Sector &s, int prec, int nstep, int hv_rows)
 {
-    return lz_region(s, prec, nstep, hv_parts).end;
+    return lz_region(s, prec, nstep, hv_rows).end;
 }
 
 int lanczos_reference_in(mo_ed_ctx *ctx, const Sector &s, const double *h_vec, int nstep,
@@ -522,8 +525,8 @@ int lanczos_reference_in(mo_ed_ctx *ctx, const Sector &s, const double *h_vec, i
     lb.prec = prec;
     lb.nstep = nstep;
     lb.sec = {s};
-    if (int rc = hv_lookup(ctx, s, kind, &lb.hv_variant, &lb.hv_parts)) return rc;
-    const LzRegion g = lz_region(s, prec, nstep, lb.hv_parts);
+    if (int rc = hv_lookup(ctx, s, kind, &lb.hv_variant, &lb.hv_rows)) return rc;
+    const LzRegion g = lz_region(s, prec, nstep, lb.hv_rows);
     if (g.end > cap || ((size_t)scratch & 255)) return fail(ctx, MO_ED_ERR_CAPACITY, "Lanczos region too small");
     char *base = (char *)scratch;
     const size_t es = prec == MO_ED_FP32 ? sizeof(float) : sizeof(double);
@@ -541,7 +544,7 @@ int lanczos_reference_in(mo_ed_ctx *ctx, const Sector &s, const double *h_vec, i
     R.upd_item0 = 0;
     R.upd_nitems = (int)((Dp + kVecChunk - 1) / kVecChunk);
     R.hv_item0 = 0;
-    R.hv_nitems = lb.hv_parts;
+    R.hv_nitems = s.dn->nitems.at(lb.hv_rows);
     R.a = (double *)(base + g.coef);
     R.nrm = R.a + (nstep + 1);
     R.active = (int *)(base + g.flags);
@@ -552,12 +555,13 @@ int lanczos_reference_in(mo_ed_ctx *ctx, const Sector &s, const double *h_vec, i
 
     k_lz_reset<<<1, kVecThreads, 0, ctx->stream>>>(d, nstep);
     MOED_CHECK_LAUNCH(ctx);
-    void *stage = base + g.u12;
     if (prec == MO_ED_FP32) {
-        if (int rc = upload_f64_to_f32(ctx, s, h_vec, (float *)R.u[0], stage)) return rc;
+        double *stage = (double *)(base + g.u12);
+        if (int rc = upload_padded(ctx, s, h_vec, stage, sizeof(double))) return rc;
+        if (int rc = convert_f64_to_f32(ctx, stage, (float *)R.u[0], Dp)) return rc;
         if (int rc = lz_steps<float>(ctx, lb, d, false)) return rc;
     } else {
-        if (int rc = upload_padded(ctx, s, h_vec, R.u[0], sizeof(double), stage)) return rc;
+        if (int rc = upload_padded(ctx, s, h_vec, R.u[0], sizeof(double))) return rc;
         if (int rc = lz_steps<double>(ctx, lb, d, false)) return rc;
     }
     MOED_CUDA(ctx, cudaMemcpyAsync(a, R.a, sizeof(double) * (nstep + 1), cudaMemcpyDeviceToHost, ctx->stream));
@@ -778,21 +782,17 @@ __global__ void k_resid_part(const T *__restrict__ x, const double *__restrict__
     if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
-// deterministic pseudo-random start vector in [-1, 1), a function of the
-// reference index (down rank * nup + up rank); zero in the pads
+// deterministic pseudo-random start vector in [-1, 1) (zero in the row pads)
 template <typename T>
-__global__ void k_random(T *x, long long n, int ld, int nu, const int *__restrict__ rank_at,
-                         unsigned long long seed)
+__global__ void k_random(T *x, long long n, int ld, int nu, unsigned long long seed)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
-        const long long d = i / ld;
-        const int r = rank_at[i - d * ld];
-        if (r < 0) {
+        if ((int)(i % ld) >= nu) {
             x[i] = T(0);
             continue;
         }
-        unsigned long long z = (unsigned long long)(d * nu + r) + seed * 0x9E3779B97F4A7C15ull;
+        unsigned long long z = (unsigned long long)i + seed * 0x9E3779B97F4A7C15ull;
         z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
         z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
         z ^= z >> 31;
@@ -1124,7 +1124,7 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
 
     // start vector
     unsigned long long seed = 0x5eedULL + 977ULL * (unsigned)s.ne_up + 131ULL * (unsigned)s.ne_down;
-    k_random<T><<<G, kVecThreads, 0, ctx->stream>>>((T *)W->p, Dp, s.ld(), s.up->n, s.up->rank_at, seed);
+    k_random<T><<<G, kVecThreads, 0, ctx->stream>>>((T *)W->p, Dp, s.ld(), s.up->n, seed);
     MOED_CHECK_LAUNCH(ctx);
     if (int rc = normalize_into((T *)W->p, V[0])) return rc;
 
@@ -1222,7 +1222,7 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
         for (int i = 0; i < kk; ++i) std::swap(V[i], spare[i]);
         if (broke) {
             // invariant subspace: continue from a fresh random direction
-            k_random<T><<<G, kVecThreads, 0, ctx->stream>>>((T *)W->p, Dp, s.ld(), s.up->n, s.up->rank_at,
+            k_random<T><<<G, kVecThreads, 0, ctx->stream>>>((T *)W->p, Dp, s.ld(), s.up->n,
                                                             seed + 7919ULL * (cycle + 1) * kMaxNcv);
             MOED_CHECK_LAUNCH(ctx);
             if (int rc = orthogonalize<T>(ctx, V, kk, (T *)W->p, Dp, (double *)dh1.p, (double *)dh2.p,

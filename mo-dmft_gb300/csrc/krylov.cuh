@@ -39,7 +39,7 @@ struct LzBatch {
     DevBuf upd_part, hv_part;
     std::vector<int> upd_item0, upd_nitems, hv_item0, hv_nitems;
     int upd_total = 0, hv_total = 0;
-    int hv_variant = 0, hv_parts = 0;  // H*v tile shape shared by all runs, its dot partials per run
+    int hv_variant = 0, hv_rows = 0;   // H*v tile shape shared by all runs
 };
 
 // Allocate a batch for the given target sectors; start vectors are written

@@ -87,10 +87,10 @@ int mo_ed_lanczos_iteration_noalloc(mo_ed_ctx *ctx, int ne_up, int ne_down, cons
     Sector s;
     if (int rc = find_sector(ctx, ne_up, ne_down, &s)) return rc;
     const int prec = ctx->opt.precision;
-    int v = 0, nparts = 0;
-    if (int rc = hv_lookup(ctx, s, prec == MO_ED_FP32 ? HV_F32 : HV_F64, &v, &nparts)) return rc;
+    int v = 0, R = 0;
+    if (int rc = hv_lookup(ctx, s, prec == MO_ED_FP32 ? HV_F32 : HV_F64, &v, &R)) return rc;
     const int nstep = ctx->opt.nstep;
-    const size_t need = lanczos_region_bytes(s, prec, nstep, nparts);
+    const size_t need = lanczos_region_bytes(s, prec, nstep, R);
     if (need > kNoAllocBytes)
         return fail(ctx, MO_ED_ERR_CAPACITY,
                     "sector needs " + std::to_string(need) + " bytes, the no-allocation region holds " +

@@ -10,7 +10,6 @@
 // (combinatorial number system) and a rank is unranked greedily from the top
 // bit.  Both directions are one thread per element here.
 #include <algorithm>
-#include <array>
 #include <cstring>
 
 #include "internal.h"
@@ -42,20 +41,27 @@ Species::~Species()
 {
     cudaFree(words);
     cudaFree(rank);
-    cudaFree(pos);
-    cudaFree(rank_at);
-    cudaFree(ublk);
+    cudaFree(hop_cnt);
+    cudaFree(hop_tgt);
+    cudaFree(hop_val_d);
+    cudaFree(hop_val_f);
+    cudaFree(info);
+    cudaFree(diag_d);
+    cudaFree(diag_f);
+    cudaFree(tab_f);
+    cudaFree(tab_d);
     cudaFree(sched_hdr);
     cudaFree(sched_ent);
-    cudaFree(sched16);
-    cudaFree(up_diag_d);
-    cudaFree(up_diag_f);
-    cudaFree(up_imp);
-    cudaFree(up4);
-    cudaFree(rs);
-    cudaFree(rs_row);
-    cudaFree(rs_blob);
-    cudaFree(blob);
+    for (auto &kv : sched_rf) cudaFree(kv.second);
+    for (auto &kv : sched_rd) cudaFree(kv.second);
+    for (auto &kv : items) cudaFree(kv.second);
+    for (auto &kv : desc) cudaFree(kv.second);
+    cudaFree(dblk_off);
+    cudaFree(dblk_rows);
+    cudaFree(dblk_ptr);
+    cudaFree(dblk_mv_f);
+    cudaFree(dblk_mv_d);
+    for (auto &kv : dblk_chunks) cudaFree(kv.second);
 }
 
 // ---------------------------------------------------------------------------
@@ -97,6 +103,111 @@ __global__ void k_rank(int nsite, int N, int *rank)
     for (int p = 0; p < nsite; ++p)
         if ((w >> p) & 1) r += c_binom[p][i++];
     rank[w] = r;
+}
+
+struct CplList {
+    int n;
+    int orb[kMaxHop];   // impurity bit (0-based orbital)
+    int bath[kMaxHop];  // bath bit (norb + ibath - 1)
+    double val[kMaxHop];
+};
+
+// Hybridisation moves of one species word, compacted, in the reference's loop
+// order (iorb outer, ibath inner; hybridization1 then hybridization2,
+// ed_hamiltonian.F90:146-161).  Signs: product of the destruction / creation
+// signs (parity of occupied bits below the target bit), ed_operators.F90:292-348.
+// For the down species the reference also counts all up-spin bits below; that
+// parity appears once in each of the two operators and cancels.
+__global__ void k_hops(int n, int n_pad, int impmask, CplList cpl, const int *words, const int *rank,
+                       int *cnt, int *tgt, double *vd, float *vf, int *info, int *max_cnt)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_pad) return;
+    if (r >= n) {             // pad columns: no moves, impurity bits 0
+        info[r] = 0;
+        return;
+    }
+    unsigned w = (unsigned)words[r];
+    int c = 0;
+    for (int i = 0; i < cpl.n; ++i) {
+        int o = cpl.orb[i], k = cpl.bath[i];
+        int ob = (w >> o) & 1, kb = (w >> k) & 1;
+        int src, dst;
+        if (kb && !ob) {          // hybridization1: c_k then c+_o
+            src = k;
+            dst = o;
+        } else if (ob && !kb) {   // hybridization2: c_o then c+_k
+            src = o;
+            dst = k;
+        } else {
+            continue;
+        }
+        int s1 = parity_below(w, src);
+        unsigned w1 = w & ~(1u << src);
+        int s2 = parity_below(w1, dst);
+        unsigned w2 = w1 | (1u << dst);
+        const int neg = (s1 ^ s2) & 1;
+        double v = cpl.val[i] * (neg ? -1.0 : 1.0);
+        const int t = rank[w2];
+        tgt[(size_t)c * n + r] = t;
+        vd[(size_t)c * n + r] = v;
+        vf[(size_t)c * n + r] = (float)v;
+        ++c;
+    }
+    for (int i = c; i < cpl.n; ++i) {
+        tgt[(size_t)i * n + r] = r;   // padding: harmless in-range target
+        vd[(size_t)i * n + r] = 0.0;
+        vf[(size_t)i * n + r] = 0.0f;
+    }
+    cnt[r] = c;
+    info[r] = c | ((int)(w & (unsigned)impmask) << 8);
+    atomicMax(max_cnt, c);
+}
+
+// Chunk-major column move tables: entry (c, s, k) = move s of column 4c+k.
+// Slots beyond a column's count (and pad columns) hold (own rank, 0).
+__global__ void k_chunk_tables(int n, int n_pad, int hw, const int *cnt, const int *tgt, const double *vd,
+                               HopEnt<float> *tf, HopEnt<double> *td)
+{
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= (long long)n_pad * hw) return;
+    const int u = (int)(i % n_pad), s = (int)(i / n_pad);
+    const size_t o = ((size_t)(u >> 2) * hw + s) * 4 + (u & 3);
+    int t = u < n ? u : 0;
+    double v = 0.0;
+    if (u < n && s < cnt[u]) {
+        t = tgt[(size_t)s * n + u];
+        v = vd[(size_t)s * n + u];
+    }
+    tf[o].t = t;
+    tf[o].v = (float)v;
+    td[o].t = t;
+    td[o].pad = 0;
+    td[o].v = v;
+}
+
+// Species part of the diagonal: sum_site ek(site) n_site (onsite,
+// ed_operators.F90:68-84) + (U-3J) sum_{i<j} n_i n_j over impurity orbitals
+// (same-spin dens_dens, ed_operators.F90:157-159).
+__global__ void k_species_diag(int n, int n_pad, int nsite, int norb, const int *words, const double *ek,
+                               double Usame, double *dd, float *df)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_pad) return;
+    if (r >= n) {
+        dd[r] = 0.0;
+        df[r] = 0.0f;
+        return;
+    }
+    unsigned w = (unsigned)words[r];
+    double s = 0.0;
+    for (int i = 0; i < nsite; ++i)
+        if ((w >> i) & 1) s += ek[i];
+    for (int i = 0; i < norb; ++i)
+        for (int j = i + 1; j < norb; ++j)
+            if (((w >> i) & 1) && ((w >> j) & 1)) s += Usame;
+    dd[r] = s;
+    df[r] = (float)s;
 }
 
 __global__ void k_basis_get(long long n, const long long *idx, unsigned *state, const int *up,
@@ -226,52 +337,227 @@ int build_model(mo_ed_ctx *ctx)
             if (id[r] < 0) id[r] = nsub++;
             ctx->site_subsys[i] = id[r];
         }
-        // Sites without couplings have no moves: they share one subsystem.
-        // Beyond kMaxSub subsystems the two smallest are merged (a merged
-        // count is still conserved, the blocks are only coarser).
-        std::vector<int> size(nsub, 0), coupled(nsub, 0);
-        for (int i = 0; i < m.nsite; ++i) size[ctx->site_subsys[i]]++;
-        for (int i = 0; i < m.ncpl; ++i) coupled[ctx->site_subsys[ctx->cpl_orb[i]]] = 1;
-        std::vector<int> remap(nsub, -1);
-        int nnew = 0, inert = -1;
-        for (int k = 0; k < nsub; ++k) {
-            if (coupled[k]) {
-                remap[k] = nnew++;
-            } else {
-                if (inert < 0) inert = nnew++;
-                remap[k] = inert;
+        // largest down-spin block and most hybridisation moves in one block,
+        // over every electron count (all 2^nsite words, nsite <= 15)
+        std::map<unsigned long long, std::pair<long long, long long>> blk;
+        for (unsigned w = 0; w < (1u << m.nsite); ++w) {
+            unsigned long long key = (unsigned long long)__builtin_popcount(w);
+            for (int sub = 0; sub < nsub; ++sub) {
+                int c = 0;
+                for (int i = 0; i < m.nsite; ++i)
+                    if (((w >> i) & 1) && ctx->site_subsys[i] == sub) ++c;
+                key = key * 32 + (unsigned)c;
             }
+            int mv = 0;
+            for (int i = 0; i < m.ncpl; ++i)
+                mv += (int)(((w >> ctx->cpl_orb[i]) & 1) != ((w >> ctx->cpl_bath[i]) & 1));
+            auto &e = blk[key];
+            e.first += 1;
+            e.second += mv;
         }
-        for (int i = 0; i < m.nsite; ++i) ctx->site_subsys[i] = remap[ctx->site_subsys[i]];
-        nsub = nnew;
-        while (nsub > kMaxSub) {
-            std::vector<int> sz(nsub, 0);
-            for (int i = 0; i < m.nsite; ++i) sz[ctx->site_subsys[i]]++;
-            int a1 = 0;
-            for (int k = 1; k < nsub; ++k)
-                if (sz[k] < sz[a1]) a1 = k;
-            int a2 = a1 == 0 ? 1 : 0;
-            for (int k = 0; k < nsub; ++k)
-                if (k != a1 && sz[k] < sz[a2]) a2 = k;
-            const int lo = std::min(a1, a2), hi = std::max(a1, a2);
-            for (int i = 0; i < m.nsite; ++i) {
-                int &v = ctx->site_subsys[i];
-                if (v == hi) v = lo;
-                else if (v > hi) --v;
-            }
-            --nsub;
+        ctx->dblk_bound = 0;
+        ctx->dblk_mv_bound = 0;
+        for (const auto &kv : blk) {
+            ctx->dblk_bound = (int)std::max<long long>(ctx->dblk_bound, kv.second.first);
+            ctx->dblk_mv_bound = (int)std::max<long long>(ctx->dblk_mv_bound, kv.second.second);
         }
-        ctx->nsub = nsub;
     }
     if (!ctx->d_mdl) MOED_CUDA(ctx, cudaMalloc(&ctx->d_mdl, sizeof(ModelDev)));
     MOED_CUDA(ctx, cudaMemcpyAsync(ctx->d_mdl, &m, sizeof(m), cudaMemcpyHostToDevice, ctx->stream));
     MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    // species tables, H*v tile lists and tile-shape choices belong to the model
-    ctx->hv_tiles.clear();
+    // species tables and tile-shape choices belong to the model
     ctx->hv_choice.clear();
     ctx->hv_times.clear();
     ctx->species.clear();
     return upload_binom(ctx);
+}
+
+// Row items of a species for R rows per item.  Words sharing their bath bits
+// (a bath group) are consecutive ranks; spin-flip / pair hopping map a row
+// into its own group, so whole groups are kept in one item when they fit.
+// Groups are ordered by the bath-electron counts of the conserved subsystems
+// (down-spin moves change those counts by one), then packed greedily.
+int species_items(mo_ed_ctx *ctx, Species *sp, int R, const int **items, int *nitems)
+{
+    auto it = sp->items.find(R);
+    if (it != sp->items.end()) {
+        *items = it->second;
+        *nitems = sp->nitems[R];
+        return MO_ED_OK;
+    }
+    const int nsite = sp->nsite, N = sp->N, norb = ctx->norb;
+    int nsub = 0;
+    for (int v : ctx->site_subsys) nsub = std::max(nsub, v + 1);
+    struct Group {
+        unsigned long long key;
+        int first, size;
+    };
+    std::vector<Group> groups;
+    int r = 0;
+    unsigned prev = ~0u;
+    for (unsigned w = 0; w < (1u << nsite); ++w) {
+        if (__builtin_popcount(w) != N) continue;
+        const unsigned bath = w >> norb;
+        if (groups.empty() || bath != prev) {
+            unsigned long long k = 0;
+            for (int sub = 0; sub < nsub; ++sub) {
+                int c = 0;
+                for (int i = norb; i < nsite; ++i)
+                    if (((w >> i) & 1) && ctx->site_subsys[i] == sub) ++c;
+                k = k * 16 + (unsigned)c;
+            }
+            groups.push_back({k, r, 0});
+            prev = bath;
+        }
+        groups.back().size++;
+        ++r;
+    }
+    std::stable_sort(groups.begin(), groups.end(),
+                     [](const Group &a, const Group &b) { return a.key < b.key; });
+    std::vector<int> tab;
+    int fill = R;
+    for (const Group &g : groups) {
+        for (int off = 0; off < g.size; off += R) {       // a group larger than R is split
+            const int len = std::min(R, g.size - off);
+            if (fill + len > R) {
+                tab.insert(tab.end(), R, -1);
+                fill = 0;
+            }
+            for (int i = 0; i < len; ++i) tab[tab.size() - R + fill + i] = g.first + off + i;
+            fill += len;
+        }
+    }
+    const int n_items = (int)(tab.size() / R);
+    int *d = nullptr;
+    MOED_CUDA(ctx, cudaMalloc(&d, sizeof(int) * std::max<size_t>(1, tab.size())));
+    MOED_CUDA(ctx, cudaMemcpyAsync(d, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice, ctx->stream));
+    MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    sp->items[R] = d;
+    sp->nitems[R] = n_items;
+    *items = d;
+    *nitems = n_items;
+    return MO_ED_OK;
+}
+
+// Down-spin blocks of a species for the split H*v.  Rows (words, rank order)
+// are keyed by their electron count in every conserved subsystem; a
+// hybridisation move stays inside its subsystem, so every block is closed
+// under the moves and a block times a column range is an independent chunk.
+// Moves are copied from the species' move tables with their targets rewritten
+// as indices within the block.  Chunks: a block's columns are cut into ranges of about
+// kChunkElems elements (whole 32-column units), so the chunks of a sector do
+// similar work whatever the block sizes.
+int species_dblocks(mo_ed_ctx *ctx, Species *sp, int ld)
+{
+    constexpr long long kChunkElems = 1 << 16;
+    if (!sp->dblk_ptr) {
+        // a build that failed part way left some tables: start over
+        cudaFree(sp->dblk_off);
+        cudaFree(sp->dblk_rows);
+        cudaFree(sp->dblk_mv_f);
+        cudaFree(sp->dblk_mv_d);
+        sp->dblk_off = sp->dblk_rows = nullptr;
+        sp->dblk_mv_f = nullptr;
+        sp->dblk_mv_d = nullptr;
+        const int n = sp->n, hw = sp->hw, nsite = sp->nsite, N = sp->N;
+        int nsub = 0;
+        for (int v : ctx->site_subsys) nsub = std::max(nsub, v + 1);
+        std::vector<int> cnt(n), tgt((size_t)hw * n);
+        std::vector<double> val((size_t)hw * n);
+        MOED_CUDA(ctx, cudaMemcpyAsync(cnt.data(), sp->hop_cnt, sizeof(int) * n, cudaMemcpyDeviceToHost, ctx->stream));
+        MOED_CUDA(ctx, cudaMemcpyAsync(tgt.data(), sp->hop_tgt, sizeof(int) * tgt.size(), cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+        MOED_CUDA(ctx, cudaMemcpyAsync(val.data(), sp->hop_val_d, sizeof(double) * val.size(),
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+        MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        // block key of every rank (words in increasing numeric order = rank order)
+        std::map<unsigned long long, std::vector<int>> blocks;
+        int r = 0;
+        for (unsigned w = 0; w < (1u << nsite); ++w) {
+            if (__builtin_popcount(w) != N) continue;
+            unsigned long long k = 0;
+            for (int sub = 0; sub < nsub; ++sub) {
+                int c = 0;
+                for (int i = 0; i < nsite; ++i)
+                    if (((w >> i) & 1) && ctx->site_subsys[i] == sub) ++c;
+                k = k * 32 + (unsigned)c;
+            }
+            blocks[k].push_back(r++);
+        }
+        std::vector<const std::vector<int> *> order;
+        for (auto &kv : blocks) order.push_back(&kv.second);
+        std::stable_sort(order.begin(), order.end(),
+                         [](const std::vector<int> *a, const std::vector<int> *b) { return a->size() > b->size(); });
+        std::vector<int> local(n, -1), blk(n, -1);
+        for (size_t b = 0; b < order.size(); ++b)
+            for (size_t i = 0; i < order[b]->size(); ++i) {
+                local[(*order[b])[i]] = (int)i;
+                blk[(*order[b])[i]] = (int)b;
+            }
+        std::vector<int> off(1, 0), rows, ptr(1, 0);
+        std::vector<HopEnt<float>> mvf;
+        std::vector<HopEnt<double>> mvd;
+        int maxrows = 0, mvmax = 0;
+        for (size_t b = 0; b < order.size(); ++b) {
+            const size_t m0 = mvf.size();
+            for (int row : *order[b]) {
+                rows.push_back(row);
+                for (int s = 0; s < cnt[row]; ++s) {
+                    const int tr = tgt[(size_t)s * n + row];
+                    if (tr < 0 || tr >= n || blk[tr] != (int)b)
+                        return fail(ctx, MO_ED_ERR_STATE, "down-spin move leaves its conserved block");
+                    const double v = val[(size_t)s * n + row];
+                    HopEnt<float> ef;
+                    ef.t = local[tr];
+                    ef.v = (float)v;
+                    HopEnt<double> ed;
+                    ed.t = local[tr];
+                    ed.pad = 0;
+                    ed.v = v;
+                    mvf.push_back(ef);
+                    mvd.push_back(ed);
+                }
+                ptr.push_back((int)mvf.size());
+            }
+            off.push_back((int)rows.size());
+            maxrows = std::max(maxrows, (int)order[b]->size());
+            mvmax = std::max(mvmax, (int)(mvf.size() - m0));
+        }
+        auto up = [&](auto **dst, const auto &v) -> int {
+            using E = std::remove_const_t<std::remove_reference_t<decltype(v[0])>>;
+            MOED_CUDA(ctx, cudaMalloc((void **)dst, sizeof(E) * std::max<size_t>(1, v.size())));
+            MOED_CUDA(ctx, cudaMemcpyAsync((void *)*dst, v.data(), sizeof(E) * v.size(), cudaMemcpyHostToDevice,
+                                           ctx->stream));
+            return MO_ED_OK;
+        };
+        if (int rc = up(&sp->dblk_off, off)) return rc;
+        if (int rc = up(&sp->dblk_rows, rows)) return rc;
+        if (int rc = up(&sp->dblk_mv_f, mvf)) return rc;
+        if (int rc = up(&sp->dblk_mv_d, mvd)) return rc;
+        if (int rc = up(&sp->dblk_ptr, ptr)) return rc;   // last: marks the tables complete
+        MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        sp->dblk_n = (int)order.size();
+        sp->dblk_max = maxrows;
+        sp->dblk_mvmax = mvmax;
+        sp->dblk_h_off = off;
+    }
+    if (sp->dblk_chunks.count(ld)) return MO_ED_OK;
+    const int units = ld / 32;
+    std::vector<int2> ch(sp->dblk_n);
+    int total = 0;
+    for (int b = 0; b < sp->dblk_n; ++b) {
+        const long long nr = sp->dblk_h_off[b + 1] - sp->dblk_h_off[b];
+        const int per = (int)std::max(1LL, std::min<long long>(units, kChunkElems / (32 * nr)));
+        ch[b] = make_int2(total, per);
+        total += (units + per - 1) / per;
+    }
+    int2 *d = nullptr;
+    MOED_CUDA(ctx, cudaMalloc(&d, sizeof(int2) * std::max<size_t>(1, ch.size())));
+    MOED_CUDA(ctx, cudaMemcpyAsync(d, ch.data(), sizeof(int2) * ch.size(), cudaMemcpyHostToDevice, ctx->stream));
+    MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    sp->dblk_chunks[ld] = d;
+    sp->dblk_nchunks[ld] = total;
+    return MO_ED_OK;
 }
 
 // Up-spin gather schedule.  The moves of the 32 columns of a chunk are the
@@ -338,76 +624,136 @@ static void colour_chunk(const std::vector<int> &lane, const std::vector<int> &b
     colour = g.col;
 }
 
-// ---------------------------------------------------------------------------
-// Species tables of the conserved-block layout, built on the host (nsite <=
-// 15: at most 6435 words per species) and uploaded once.
-// ---------------------------------------------------------------------------
-namespace {
-
-inline int par_below(unsigned w, int bit) { return __builtin_popcount(w & ((1u << bit) - 1u)) & 1; }
-
-struct Hop {
-    int tgt;    // target rank
-    int cidx;   // coupling index: 1 + 2*coupling + negative sign
-    int sub;    // subsystem the move stays in
-};
-
-// Hybridisation moves of a word in the reference's loop order (iorb outer,
-// ibath inner; hybridization1 then hybridization2, ed_hamiltonian.F90:146-161).
-// Signs: product of the destruction and creation signs (parity of occupied
-// bits below the operated bit, ed_operators.F90:292-348).  For the down
-// species the reference also counts every up-spin bit below; that parity
-// appears in both operators and cancels.
-void word_hops(const mo_ed_ctx *ctx, const std::vector<int> &rank, unsigned w, std::vector<Hop> &out)
+static int build_up_schedule(mo_ed_ctx *ctx, Species *s)
 {
-    out.clear();
-    for (size_t i = 0; i < ctx->cpl_val.size(); ++i) {
-        const int o = ctx->cpl_orb[i], k = ctx->cpl_bath[i];
-        const int ob = (w >> o) & 1, kb = (w >> k) & 1;
-        int src, dst;
-        if (kb && !ob) {          // hybridization1: c_k then c+_o
-            src = k;
-            dst = o;
-        } else if (ob && !kb) {   // hybridization2: c_o then c+_k
-            src = o;
-            dst = k;
-        } else {
-            continue;
+    const int nsite = ctx->nsite, N = s->N, n = s->n, nch = s->n_pad / 32;
+    std::vector<int> words;
+    std::vector<int> rank((size_t)1 << nsite, -1);
+    for (unsigned w = 0; w < (1u << nsite); ++w)
+        if (__builtin_popcount(w) == N) {
+            rank[w] = (int)words.size();
+            words.push_back((int)w);
         }
-        const int s1 = par_below(w, src);
-        const unsigned w1 = w & ~(1u << src);
-        const int s2 = par_below(w1, dst);
-        const unsigned w2 = w1 | (1u << dst);
-        out.push_back({rank[w2], 1 + 2 * (int)i + ((s1 ^ s2) & 1), ctx->site_subsys[o]});
+    auto parity_below_h = [](unsigned w, int bit) { return __builtin_popcount(w & ((1u << bit) - 1u)) & 1; };
+    const int ncpl = ctx->mdl.ncpl;
+    std::vector<int2> hdr(nch);
+    std::vector<unsigned> ent;
+    std::vector<int> el, eb, colour;
+    std::vector<unsigned> ecode;
+    int smax = 0;
+    for (int c = 0; c < nch; ++c) {
+        el.clear();
+        eb.clear();
+        ecode.clear();
+        int deg_l[32] = {0}, deg_b[32] = {0};
+        for (int l = 0; l < 32; ++l) {
+            const int u = 32 * c + l;
+            if (u >= n) continue;
+            const unsigned w = (unsigned)words[u];
+            for (int i = 0; i < ncpl; ++i) {   // the move rule of k_hops
+                const int o = ctx->cpl_orb[i], k = ctx->cpl_bath[i];
+                const int ob = (w >> o) & 1, kb = (w >> k) & 1;
+                int src, dst;
+                if (kb && !ob) {
+                    src = k;
+                    dst = o;
+                } else if (ob && !kb) {
+                    src = o;
+                    dst = k;
+                } else {
+                    continue;
+                }
+                const int s1 = parity_below_h(w, src);
+                const unsigned w1 = w & ~(1u << src);
+                const int s2 = parity_below_h(w1, dst);
+                const int t = rank[w1 | (1u << dst)];
+                el.push_back(l);
+                eb.push_back(t & 31);
+                ecode.push_back(0x80000000u | ((unsigned)((s1 ^ s2) & 1) << 22) | ((unsigned)i << 16) |
+                                (unsigned)t);
+                deg_l[l]++;
+                deg_b[t & 31]++;
+            }
+        }
+        int delta = 0;
+        for (int q = 0; q < 32; ++q) delta = std::max(delta, std::max(deg_l[q], deg_b[q]));
+        hdr[c] = make_int2((int)ent.size(), delta);
+        if (delta == 0) continue;
+        colour_chunk(el, eb, delta, colour);
+        const size_t base = ent.size();
+        ent.resize(base + (size_t)32 * delta, 0u);
+        for (size_t e = 0; e < el.size(); ++e) {
+            unsigned &slot = ent[base + (size_t)32 * colour[e] + el[e]];
+            if (colour[e] < 0 || colour[e] >= delta || slot != 0u)
+                return fail(ctx, MO_ED_ERR_STATE, "gather schedule colouring failed");
+            slot = ecode[e];
+        }
+        smax = std::max(smax, delta);
     }
-}
-
-// Impurity transfer T_{i<-j} (c+_i c_j on one species): valid when j is
-// occupied and i empty; sign from the two operators' parities.
-bool transfer(unsigned w, int i, int j, unsigned *w2, int *neg)
-{
-    if (!((w >> j) & 1) || ((w >> i) & 1)) return false;
-    const int s1 = par_below(w, j);
-    const unsigned w1 = w & ~(1u << j);
-    const int s2 = par_below(w1, i);
-    *w2 = w1 | (1u << i);
-    *neg = (s1 ^ s2) & 1;
-    return true;
-}
-
-template <typename T>
-int upload_vec(mo_ed_ctx *ctx, T **dst, const std::vector<T> &src)
-{
-    cudaFree(*dst);
-    *dst = nullptr;
-    MOED_CUDA(ctx, cudaMalloc(dst, sizeof(T) * std::max<size_t>(1, src.size())));
-    if (!src.empty())
-        MOED_CUDA(ctx, cudaMemcpyAsync(*dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice,
+    s->sched_slots_max = smax;
+    if (ent.empty()) ent.push_back(0u);
+    MOED_CUDA(ctx, cudaMalloc(&s->sched_hdr, sizeof(int2) * std::max(nch, 1)));
+    MOED_CUDA(ctx, cudaMalloc(&s->sched_ent, sizeof(unsigned) * ent.size()));
+    if (nch > 0)
+        MOED_CUDA(ctx, cudaMemcpyAsync(s->sched_hdr, hdr.data(), sizeof(int2) * nch, cudaMemcpyHostToDevice,
                                        ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpyAsync(s->sched_ent, ent.data(), sizeof(unsigned) * ent.size(),
+                                   cudaMemcpyHostToDevice, ctx->stream));
+    MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));   // before the host vectors move
+    s->h_sched_hdr = std::move(hdr);
+    s->h_sched_ent = std::move(ent);
     return MO_ED_OK;
 }
 
-}  // namespace
+int species_sched(mo_ed_ctx *ctx, Species *sp, int R)
+{
+    if (sp->sched_rf.count(R)) return MO_ED_OK;
+    const std::vector<int2> &hdr = sp->h_sched_hdr;
+    const std::vector<unsigned> &ent = sp->h_sched_ent;
+    std::vector<HopEnt<float>> ef(ent.size());
+    std::vector<HopEnt<double>> ed(ent.size());
+    auto offset = [R](int t) { return ((t >> 5) * R) * 32 + (t & 31); };
+    for (size_t c = 0; c < hdr.size(); ++c) {
+        const int first = hdr[c].x, nslot = hdr[c].y;
+        for (int sl = 0; sl < nslot; ++sl) {
+            const unsigned *e = &ent[(size_t)first + (size_t)32 * sl];
+            unsigned used = 0u;
+            for (int l = 0; l < 32; ++l)
+                if (e[l] & 0x80000000u) used |= 1u << (e[l] & 31u);
+            for (int l = 0; l < 32; ++l) {
+                const size_t o = (size_t)first + (size_t)32 * sl + l;
+                int t;
+                double v;
+                if (e[l] & 0x80000000u) {
+                    t = (int)(e[l] & 0xffffu);
+                    v = ctx->cpl_val[(e[l] >> 16) & 63u];
+                    if (e[l] & (1u << 22)) v = -v;
+                } else {
+                    t = __builtin_ctz(~used);   // a bank no lane of this slot reads (column t of tile 0)
+                    used |= 1u << t;
+                    v = 0.0;
+                }
+                ef[o].t = offset(t);
+                ef[o].v = (float)v;
+                ed[o].t = offset(t);
+                ed[o].pad = 0;
+                ed[o].v = v;
+            }
+        }
+    }
+    HopEnt<float> *df = nullptr;
+    HopEnt<double> *dd = nullptr;
+    MOED_CUDA(ctx, cudaMalloc(&df, sizeof(HopEnt<float>) * ef.size()));
+    sp->sched_rf[R] = df;
+    MOED_CUDA(ctx, cudaMalloc(&dd, sizeof(HopEnt<double>) * ed.size()));
+    sp->sched_rd[R] = dd;
+    MOED_CUDA(ctx, cudaMemcpyAsync(df, ef.data(), sizeof(HopEnt<float>) * ef.size(), cudaMemcpyHostToDevice,
+                                   ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpyAsync(dd, ed.data(), sizeof(HopEnt<double>) * ed.size(), cudaMemcpyHostToDevice,
+                                   ctx->stream));
+    MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return MO_ED_OK;
+}
 
 int get_species(mo_ed_ctx *ctx, int N, Species **out)
 {
@@ -416,374 +762,76 @@ int get_species(mo_ed_ctx *ctx, int N, Species **out)
         *out = it->second.get();
         return MO_ED_OK;
     }
-    const int nsite = ctx->nsite, nsub = ctx->nsub, norb = ctx->norb;
-    const ModelDev &m = ctx->mdl;
+    const int nsite = ctx->nsite;
     std::unique_ptr<Species> s(new Species);
     s->nsite = nsite;
     s->N = N;
     s->n = (int)binom(nsite, N);
-    s->nsub = nsub;
-    const int n = s->n;
-
-    // words in ascending order (the reference's basis order) and their ranks
-    std::vector<int> rank(1u << nsite, -1);
-    s->h_words.reserve(n);
-    for (unsigned w = 0; w < (1u << nsite); ++w)
-        if (__builtin_popcount(w) == N) {
-            rank[w] = (int)s->h_words.size();
-            s->h_words.push_back((int)w);
-        }
-
-    // subsystem masks; local state index of every sub-pattern (ascending
-    // within each subsystem and electron count)
-    unsigned smask[kMaxSub] = {0};
-    for (int i = 0; i < nsite; ++i) smask[ctx->site_subsys[i]] |= 1u << i;
-    std::vector<int> lidx(1u << nsite, 0);
-    for (int k = 0; k < nsub; ++k) {
-        int cnt[kMaxSite + 2] = {0};
-        unsigned sub = 0;
-        while (true) {   // submasks of smask[k] in ascending order
-            lidx[sub] = cnt[__builtin_popcount(sub)]++;
-            if (sub == smask[k]) break;
-            sub = (sub - smask[k]) & smask[k];
-        }
-    }
-    auto counts_of = [&](unsigned w, int *c) {
-        for (int k = 0; k < nsub; ++k) c[k] = __builtin_popcount(w & smask[k]);
-    };
-
-    // blocks: distinct count tuples, lexicographic
-    std::map<std::vector<int>, int> bkey;
-    for (int r = 0; r < n; ++r) {
-        int c[kMaxSub];
-        counts_of((unsigned)s->h_words[r], c);
-        bkey.emplace(std::vector<int>(c, c + nsub), 0);
-    }
-    const int nblk = (int)bkey.size();
-    std::vector<std::vector<int>> bcnt;
-    std::vector<std::array<int, kMaxSub>> bL(nblk), bstride(nblk);
-    {
-        int b = 0;
-        for (auto &kv : bkey) {
-            kv.second = b++;
-            bcnt.push_back(kv.first);
-        }
-    }
-    s->h_ublk.resize(nblk);
-    s->h_ublk_cnt.assign((size_t)nblk * kMaxSub, 0);
-    int col = 0;
-    for (int b = 0; b < nblk; ++b) {
-        int W = 1;
-        for (int k = nsub - 1; k >= 0; --k) {
-            bL[b][k] = (int)binom(__builtin_popcount(smask[k]), bcnt[b][k]);
-            bstride[b][k] = W;
-            W *= bL[b][k];
-            s->h_ublk_cnt[(size_t)b * kMaxSub + k] = bcnt[b][k];
-        }
-        UpBlock &u = s->h_ublk[b];
-        u.col0 = col;
-        u.W = W;
-        u.W4 = (W + 3) & ~3;
-        u.hdr0 = 0;
-        u.s16_off = u.s16_bytes = u.pad0 = u.pad1 = 0;
-        col += u.W4;
-    }
-    s->ncol = col;
-    s->ld = std::max(32, (col + 31) & ~31);
-    if (s->ld > 65535) return fail(ctx, MO_ED_ERR_ARG, "species too wide for the 16-bit column tables");
-    const int ld = s->ld;
-    std::vector<int> blk_of(n), idx_of(n);
-    s->h_pos.assign(n, 0);
-    s->h_rank_at.assign(ld, -1);
-    for (int r = 0; r < n; ++r) {
-        const unsigned w = (unsigned)s->h_words[r];
-        int c[kMaxSub];
-        counts_of(w, c);
-        const int b = bkey.at(std::vector<int>(c, c + nsub));
-        int idx = 0;
-        for (int k = 0; k < nsub; ++k) idx += lidx[w & smask[k]] * bstride[b][k];
-        blk_of[r] = b;
-        idx_of[r] = idx;
-        s->h_pos[r] = s->h_ublk[b].col0 + idx;
-        s->h_rank_at[s->h_pos[r]] = r;
-    }
-
-    // per word: moves, diagonal, impurity pattern
-    std::vector<std::vector<Hop>> hops(n);
-    std::vector<double> diag(n);
-    for (int r = 0; r < n; ++r) {
-        const unsigned w = (unsigned)s->h_words[r];
-        word_hops(ctx, rank, w, hops[r]);
-        // onsite (ed_operators.F90:68-84) + same-spin (U-3J) n_i n_j over
-        // impurity orbitals (dens_dens, ed_operators.F90:157-159)
-        double d = 0.0;
-        for (int i = 0; i < nsite; ++i)
-            if ((w >> i) & 1) d += ctx->ek[i];
-        for (int i = 0; i < norb; ++i)
-            for (int j = i + 1; j < norb; ++j)
-                if (((w >> i) & 1) && ((w >> j) & 1)) d += ctx->U - 3 * ctx->J;
-        diag[r] = d;
-    }
-    const bool four = ctx->J != 0.0 && m.npair > 0;
-    int pidx[kMaxOrb][kMaxOrb] = {{0}};
-    {
-        int p = 0;
-        for (int i = 0; i < norb; ++i)
-            for (int j = 0; j < norb; ++j)
-                if (i != j) pidx[i][j] = p++;
-    }
-
-    // ---- up-spin role: per-column tables and gather schedules ----
-    std::vector<double> updd(ld, 0.0);
-    std::vector<float> updf(ld, 0.0f);
-    std::vector<unsigned char> upimp(ld, 0);
-    std::vector<unsigned> up4((size_t)std::max(1, m.npair) * ld, 0u);
-    for (int r = 0; r < n; ++r) {
-        const int c = s->h_pos[r];
-        const unsigned w = (unsigned)s->h_words[r];
-        updd[c] = diag[r];
-        updf[c] = (float)diag[r];
-        upimp[c] = (unsigned char)(w & (unsigned)(m.nimp - 1));
-        if (!four) continue;
-        for (int i = 0; i < norb; ++i)
-            for (int j = 0; j < norb; ++j) {
-                if (i == j) continue;
-                unsigned w2;
-                int neg;
-                if (transfer(w, i, j, &w2, &neg))
-                    up4[(size_t)pidx[i][j] * ld + c] =
-                        0x80000000u | ((unsigned)neg << 30) | (unsigned)s->h_pos[rank[w2]];
-            }
-    }
-    std::vector<int2> hdr;
-    std::vector<unsigned> ent;
-    for (int b = 0; b < nblk; ++b) {
-        UpBlock &u = s->h_ublk[b];
-        const int nq = u.W4 / 4, nch = (nq + 15) / 16;
-        u.hdr0 = (int)hdr.size();
-        for (int ch = 0; ch < nch; ++ch)
-            for (int k = 0; k < 4; ++k) {
-                // lanes: the 16 columns 4*l + k of the chunk; banks: target mod 32 (the
-                // two half-warps read two rows, which may then meet in a bank)
-                std::vector<int> el, eb, et, ec;
-                int ldeg[16] = {0}, bdeg[32] = {0};
-                for (int l = 0; l < 16; ++l) {
-                    const int c = 4 * (16 * ch + l) + k;
-                    if (c >= u.W) continue;
-                    const int r = s->h_rank_at[u.col0 + c];
-                    for (const Hop &h : hops[r]) {
-                        const int tc = s->h_pos[h.tgt] - u.col0;
-                        if (tc < 0 || tc >= u.W) return fail(ctx, MO_ED_ERR_ARG, "up-spin move leaves its block");
-                        el.push_back(l);
-                        eb.push_back(tc & 31);
-                        et.push_back(tc);
-                        ec.push_back(h.cidx);
-                        ldeg[l]++;
-                        bdeg[tc & 31]++;
-                    }
-                }
-                int delta = 0;
-                for (int t = 0; t < 16; ++t) delta = std::max(delta, ldeg[t]);
-                for (int t = 0; t < 32; ++t) delta = std::max(delta, bdeg[t]);
-                std::vector<int> colour;
-                if (!el.empty()) colour_chunk(el, eb, delta, colour);
-                const int first = (int)ent.size();
-                ent.resize(ent.size() + (size_t)16 * delta, 0xffffffffu);
-                std::vector<unsigned> used((size_t)delta, 0u);
-                for (size_t e = 0; e < el.size(); ++e) {
-                    ent[first + 16 * colour[e] + el[e]] = (unsigned)et[e] | ((unsigned)ec[e] << 16);
-                    used[colour[e]] |= 1u << eb[e];
-                }
-                for (int sl = 0; sl < delta; ++sl)
-                    for (int l = 0; l < 16; ++l) {
-                        unsigned &x = ent[first + 16 * sl + l];
-                        if (x != 0xffffffffu) continue;
-                        // no move: read a bank no other lane of the slot uses
-                        int t = -1;
-                        for (int bb = 0; bb < 32 && bb < u.W4; ++bb)
-                            if (!((used[sl] >> bb) & 1u)) {
-                                t = bb;
-                                used[sl] |= 1u << bb;
-                                break;
-                            }
-                        if (t < 0) t = std::min(4 * (16 * ch + l) + k, u.W4 - 1);
-                        x = (unsigned)t;
-                    }
-                hdr.push_back(make_int2(first, delta));
-                s->sched_slots_max = std::max(s->sched_slots_max, delta);
-            }
-    }
-
-    // 16-bit copies of the block schedules (staged into shared memory by the
-    // H*v kernel) where every target and coupling index fits
-    std::vector<unsigned char> s16;
-    for (int b = 0; b < nblk; ++b) {
-        UpBlock &u = s->h_ublk[b];
-        const int nh = (u.W4 / 4 + 15) / 16 * 4;
-        if (u.W4 > 1024 || 2 * m.ncpl + 1 > 64) continue;
-        const int e0 = hdr[u.hdr0].x;
-        const int e1 = hdr[u.hdr0 + nh - 1].x + 16 * hdr[u.hdr0 + nh - 1].y;
-        const size_t bytes = ((size_t)4 * nh + 2 * (size_t)(e1 - e0) + 15) & ~(size_t)15;
-        std::vector<unsigned char> bl(bytes, 0);
-        for (int h = 0; h < nh; ++h) {
-            const unsigned w = ((unsigned)(hdr[u.hdr0 + h].x - e0) << 8) | (unsigned)hdr[u.hdr0 + h].y;
-            memcpy(&bl[4 * h], &w, 4);
-        }
-        for (int e = e0; e < e1; ++e) {
-            const unsigned x = ent[e];
-            const unsigned short v = (unsigned short)((x & 0xffffu) | ((x >> 16) << 10));
-            memcpy(&bl[4 * nh + 2 * (size_t)(e - e0)], &v, 2);
-        }
-        u.s16_off = (int)(s16.size() / 16);
-        u.s16_bytes = (int)bytes;
-        s16.insert(s16.end(), bl.begin(), bl.end());
-    }
-
-    // ---- down-spin role: row sets at every level, with their metadata blobs ----
-    s->h_dblk.assign(nblk, DownBlock());
-    std::vector<std::vector<int>> members(nblk);
-    for (int r = 0; r < n; ++r) members[blk_of[r]].push_back(r);
-    std::vector<int2> rsv, rblob;
-    std::vector<int> rrow;
-    std::vector<unsigned char> blob;
-    auto a16 = [](size_t v) { return (v + 15) & ~(size_t)15; };
-    for (int b = 0; b < nblk; ++b) {
-        DownBlock &db = s->h_dblk[b];
-        db.size = (int)members[b].size();
-        for (int k = 0; k < nsub; ++k) db.cnt[k] = bcnt[b][k];
-        // row axis order: subsystems with fewer moves first, so that the
-        // trailing (closed) axes carry the most moves
-        std::vector<double> mv(nsub, 0.0);
-        for (int r : members[b])
-            for (const Hop &h : hops[r]) mv[h.sub] += 1.0;
-        std::vector<int> ax(nsub);
-        for (int k = 0; k < nsub; ++k) ax[k] = k;
-        std::stable_sort(ax.begin(), ax.end(), [&](int x, int y) { return mv[x] < mv[y]; });
-        std::vector<int> inpos(nsub);
-        for (int t = 0; t < nsub; ++t) inpos[ax[t]] = t;
-        for (int j = 0; j <= nsub; ++j) {
-            int nset = 1, rows = 1;
-            for (int t = 0; t < nsub; ++t) (t < j ? nset : rows) *= bL[b][ax[t]];
-            db.rs0[j] = (int)rsv.size();
-            db.nset[j] = nset;
-            db.rs_rows[j] = rows;
-            db.blob_max[j] = 0;
-            // set index / index in the set of a word of this block
-            auto place = [&](unsigned w, int *set, int *row) {
-                int sv = 0, rv = 0;
-                for (int t = 0; t < nsub; ++t) {
-                    const int li = lidx[w & smask[ax[t]]];
-                    if (t < j) sv = sv * bL[b][ax[t]] + li;
-                    else rv = rv * bL[b][ax[t]] + li;
-                }
-                *set = sv;
-                *row = rv;
-            };
-            std::vector<int> at((size_t)nset * rows, -1);
-            for (int r : members[b]) {
-                int sv, rv;
-                place((unsigned)s->h_words[r], &sv, &rv);
-                at[(size_t)sv * rows + rv] = r;
-            }
-            for (int q = 0; q < nset; ++q) {
-                const int rec0 = (int)rrow.size();
-                rsv.push_back(make_int2(rec0, rows));
-                std::vector<int4> info(rows);
-                std::vector<double> dg(rows);
-                std::vector<unsigned> mvs, q4s;
-                for (int rv = 0; rv < rows; ++rv) {
-                    const int r = at[(size_t)q * rows + rv];
-                    if (r < 0) return fail(ctx, MO_ED_ERR_ARG, "row set with a missing row");
-                    rrow.push_back(r);
-                    const unsigned w = (unsigned)s->h_words[r];
-                    dg[rv] = diag[r];
-                    const int mv0 = (int)mvs.size();
-                    int nin = 0, nopen = 0;
-                    for (const Hop &h : hops[r])
-                        if (inpos[h.sub] >= j) {
-                            int s2, r2;
-                            place((unsigned)s->h_words[h.tgt], &s2, &r2);
-                            mvs.push_back((unsigned)r2 | ((unsigned)h.cidx << 16));
-                            ++nin;
-                        }
-                    for (const Hop &h : hops[r])
-                        if (inpos[h.sub] < j) {
-                            mvs.push_back((unsigned)h.tgt | ((unsigned)h.cidx << 16));
-                            ++nopen;
-                        }
-                    const int q0 = (int)q4s.size();
-                    int n4 = 0;
-                    if (four)
-                        for (int i = 0; i < norb; ++i)
-                            for (int jj = 0; jj < norb; ++jj) {
-                                if (i == jj) continue;
-                                const int p = pidx[i][jj];
-                                unsigned w2;
-                                int neg;
-                                // spin-flip: the down spin moves i -> j (T_{j<-i})
-                                if (transfer(w, jj, i, &w2, &neg)) {
-                                    q4s.push_back((unsigned)rank[w2] | ((unsigned)p << 16) | ((unsigned)neg << 22));
-                                    ++n4;
-                                }
-                                // pair hopping: the down spin moves j -> i (T_{i<-j})
-                                if (transfer(w, i, jj, &w2, &neg)) {
-                                    q4s.push_back((unsigned)rank[w2] | ((unsigned)p << 16) | (1u << 21) |
-                                                  ((unsigned)neg << 22));
-                                    ++n4;
-                                }
-                            }
-                    info[rv] = make_int4((int)(w & (unsigned)(m.nimp - 1)) | (nin << 8) | (nopen << 16) | (n4 << 24),
-                                         mv0, q0, r);
-                }
-                const size_t off_info = 16, off_diag = off_info + 16 * (size_t)rows;
-                const size_t off_mv = a16(off_diag + 8 * (size_t)rows);
-                const size_t off_q4 = a16(off_mv + 4 * mvs.size());
-                const size_t total = a16(off_q4 + 4 * q4s.size());
-                const size_t base = blob.size();
-                blob.resize(base + total, 0);
-                const int4 head = make_int4(rows, (int)off_mv, (int)off_q4, (int)total);
-                memcpy(&blob[base], &head, 16);
-                memcpy(&blob[base + off_info], info.data(), 16 * (size_t)rows);
-                memcpy(&blob[base + off_diag], dg.data(), 8 * (size_t)rows);
-                if (!mvs.empty()) memcpy(&blob[base + off_mv], mvs.data(), 4 * mvs.size());
-                if (!q4s.empty()) memcpy(&blob[base + off_q4], q4s.data(), 4 * q4s.size());
-                rblob.push_back(make_int2((int)(base / 16), (int)total));
-                db.blob_max[j] = std::max(db.blob_max[j], (int)total);
-            }
-        }
-    }
-    s->nrs = (int)rsv.size();
-    s->nrec = (int)rrow.size();
-
-    // the device basis: combinadic unrank / rank kernels (the host lists
-    // above give the same words; they only drive the table construction)
-    MOED_CUDA(ctx, cudaMalloc(&s->words, sizeof(int) * std::max(1, n)));
+    s->n_pad = (s->n + 31) / 32 * 32;
+    s->hw = std::max(ctx->mdl.ncpl, 1);
+    const int n = s->n, np = s->n_pad;
+    const size_t nh = (size_t)n * s->hw;
+    MOED_CUDA(ctx, cudaMalloc(&s->words, sizeof(int) * n));
     MOED_CUDA(ctx, cudaMalloc(&s->rank, sizeof(int) << nsite));
+    MOED_CUDA(ctx, cudaMalloc(&s->hop_cnt, sizeof(int) * n));
+    MOED_CUDA(ctx, cudaMalloc(&s->hop_tgt, sizeof(int) * nh));
+    MOED_CUDA(ctx, cudaMalloc(&s->hop_val_d, sizeof(double) * nh));
+    MOED_CUDA(ctx, cudaMalloc(&s->hop_val_f, sizeof(float) * nh));
+    MOED_CUDA(ctx, cudaMalloc(&s->tab_f, sizeof(HopEnt<float>) * (size_t)np * s->hw));
+    MOED_CUDA(ctx, cudaMalloc(&s->tab_d, sizeof(HopEnt<double>) * (size_t)np * s->hw));
+    MOED_CUDA(ctx, cudaMalloc(&s->info, sizeof(int) * np));
+    MOED_CUDA(ctx, cudaMalloc(&s->diag_d, sizeof(double) * np));
+    MOED_CUDA(ctx, cudaMalloc(&s->diag_f, sizeof(float) * np));
+
+    const int T = 256;
+    k_unrank<<<(n + T - 1) / T, T, 0, ctx->stream>>>(nsite, N, n, s->words);
+    MOED_CHECK_LAUNCH(ctx);
+    k_rank<<<((1 << nsite) + T - 1) / T, T, 0, ctx->stream>>>(nsite, N, s->rank);
+    MOED_CHECK_LAUNCH(ctx);
+
+    CplList cl;
+    memset(&cl, 0, sizeof(cl));
+    cl.n = ctx->mdl.ncpl;
+    for (int i = 0; i < cl.n; ++i) {
+        cl.orb[i] = ctx->cpl_orb[i];
+        cl.bath[i] = ctx->cpl_bath[i];
+        cl.val[i] = ctx->cpl_val[i];
+    }
+    DevBuf dmax, dek;
+    if (int rc = dev_alloc(ctx, dmax, sizeof(int))) return rc;
+    if (int rc = dev_alloc(ctx, dek, sizeof(double) * nsite)) return rc;
+    MOED_CUDA(ctx, cudaMemsetAsync(dmax.p, 0, sizeof(int), ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpyAsync(dek.p, ctx->ek.data(), sizeof(double) * nsite,
+                                   cudaMemcpyHostToDevice, ctx->stream));
+    if (cl.n == 0) {
+        MOED_CUDA(ctx, cudaMemsetAsync(s->hop_cnt, 0, sizeof(int) * n, ctx->stream));
+        MOED_CUDA(ctx, cudaMemsetAsync(s->hop_tgt, 0, sizeof(int) * nh, ctx->stream));
+        MOED_CUDA(ctx, cudaMemsetAsync(s->hop_val_d, 0, sizeof(double) * nh, ctx->stream));
+        MOED_CUDA(ctx, cudaMemsetAsync(s->hop_val_f, 0, sizeof(float) * nh, ctx->stream));
+    }
+    k_hops<<<(np + T - 1) / T, T, 0, ctx->stream>>>(n, np, ctx->mdl.nimp - 1, cl, s->words, s->rank,
+                                                    s->hop_cnt, s->hop_tgt, s->hop_val_d, s->hop_val_f,
+                                                    s->info, (int *)dmax.p);
+    MOED_CHECK_LAUNCH(ctx);
     {
-        const int T = 256;
-        k_unrank<<<(n + T - 1) / T, T, 0, ctx->stream>>>(nsite, N, n, s->words);
-        MOED_CHECK_LAUNCH(ctx);
-        k_rank<<<((1 << nsite) + T - 1) / T, T, 0, ctx->stream>>>(nsite, N, s->rank);
+        const long long tot = (long long)np * s->hw;
+        k_chunk_tables<<<(unsigned)((tot + T - 1) / T), T, 0, ctx->stream>>>(n, np, s->hw, s->hop_cnt, s->hop_tgt,
+                                                                             s->hop_val_d, s->tab_f, s->tab_d);
         MOED_CHECK_LAUNCH(ctx);
     }
-    if (int rc = upload_vec(ctx, &s->pos, s->h_pos)) return rc;
-    if (int rc = upload_vec(ctx, &s->rank_at, s->h_rank_at)) return rc;
-    if (int rc = upload_vec(ctx, &s->ublk, s->h_ublk)) return rc;
-    if (int rc = upload_vec(ctx, &s->sched_hdr, hdr)) return rc;
-    if (int rc = upload_vec(ctx, &s->sched_ent, ent)) return rc;
-    if (int rc = upload_vec(ctx, &s->up_diag_d, updd)) return rc;
-    if (int rc = upload_vec(ctx, &s->up_diag_f, updf)) return rc;
-    if (int rc = upload_vec(ctx, &s->up_imp, upimp)) return rc;
-    if (int rc = upload_vec(ctx, &s->up4, up4)) return rc;
-    if (blob.size() / 16 > (size_t)0x7fffffff) return fail(ctx, MO_ED_ERR_ARG, "row-set metadata too large");
-    s->h_rs = rsv;
-    s->h_rs_blob = rblob;
-    if (int rc = upload_vec(ctx, &s->sched16, s16)) return rc;
-    if (int rc = upload_vec(ctx, &s->rs, rsv)) return rc;
-    if (int rc = upload_vec(ctx, &s->rs_row, rrow)) return rc;
-    if (int rc = upload_vec(ctx, &s->rs_blob, rblob)) return rc;
-    if (int rc = upload_vec(ctx, &s->blob, blob)) return rc;
+    k_species_diag<<<(np + T - 1) / T, T, 0, ctx->stream>>>(n, np, nsite, ctx->norb, s->words,
+                                                            (const double *)dek.p, ctx->U - 3 * ctx->J,
+                                                            s->diag_d, s->diag_f);
+    MOED_CHECK_LAUNCH(ctx);
+    {   // largest bath group (words sharing their bath bits)
+        std::map<unsigned, int> gs;
+        for (unsigned w = 0; w < (1u << nsite); ++w)
+            if (__builtin_popcount(w) == N) s->max_group = std::max(s->max_group, ++gs[w >> ctx->norb]);
+    }
+    MOED_CUDA(ctx, cudaMemcpyAsync(&s->max_cnt, dmax.p, sizeof(int), cudaMemcpyDeviceToHost,
+                                   ctx->stream));
     MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (int rc = build_up_schedule(ctx, s.get())) return rc;
     *out = s.get();
     ctx->species[N] = std::move(s);
     return MO_ED_OK;

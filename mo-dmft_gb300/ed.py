@@ -75,7 +75,6 @@ SIGNATURES = [
     ("mo_ed_icom", C.c_longlong, [C.c_int, C.c_int]),
     ("mo_ed_sector_dims", C.c_int, [C.c_void_p, C.c_int, C.c_int, _ip, _ip, _llp]),
     ("mo_ed_vector_layout", C.c_int, [C.c_void_p, C.c_int, C.c_int, _ip, _llp]),
-    ("mo_ed_vector_columns", C.c_int, [C.c_void_p, C.c_int, C.c_int, _ip, C.c_int]),
     ("mo_ed_generate_basis", C.c_int, [C.c_void_p, C.c_int, C.c_int, _ip, _ip, _ip, _ip]),
     ("mo_ed_basis_get", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_longlong, _llp, _up]),
     ("mo_ed_basis_idx", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_longlong, _up, _llp]),
@@ -254,28 +253,6 @@ class EDSolver:
         ld, n = C.c_int(), C.c_longlong()
         self._chk(lib().mo_ed_vector_layout(self._ctx, ne_up, ne_down, C.byref(ld), C.byref(n)))
         return ld.value, n.value
-
-    def vector_columns(self, ne_up, ne_down):
-        """Device column of every up rank (0-based) in the device layout."""
-        nu = self.sector_dims(ne_up, ne_down)[0]
-        col = np.zeros(nu, dtype=np.int32)
-        self._chk(lib().mo_ed_vector_columns(self._ctx, ne_up, ne_down,
-                                             col.ctypes.data_as(_ip), nu))
-        return col
-
-    def to_device_layout(self, ne_up, ne_down, x):
-        """Reference-layout vector (ntot,) -> (ndown, ld) array in the device layout (numpy)."""
-        ld, _ = self.vector_layout(ne_up, ne_down)
-        nu, nd, _ = self.sector_dims(ne_up, ne_down)
-        out = np.zeros((nd, ld), dtype=np.asarray(x).dtype)
-        out[:, self.vector_columns(ne_up, ne_down)] = np.asarray(x).reshape(nd, nu)
-        return out
-
-    def from_device_layout(self, ne_up, ne_down, xd):
-        """(ndown, ld) device-layout array -> reference-layout vector (ntot,)."""
-        ld, _ = self.vector_layout(ne_up, ne_down)
-        nd = self.sector_dims(ne_up, ne_down)[1]
-        return np.asarray(xd).reshape(nd, ld)[:, self.vector_columns(ne_up, ne_down)].ravel()
 
     def generate_basis(self, ne_up, ne_down):
         nup, ndn, _ = self.sector_dims(ne_up, ne_down)

@@ -122,9 +122,11 @@ def test_multiply_h_fp32(setup, oracle, name):
 @pytest.mark.parametrize("name", ["3x6_block", "4x4_mixed", "5x2_dense"])
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-13), ("fp32", 2e-6)])
 def test_multiply_h_every_variant(setup, oracle, pkg, name, precision, tol):
-    """Each tile-shape variant of the block-tiled H*v (rows per thread, threads,
-    CTAs per SM, stage size), pinned in turn, against the oracle on every
-    sector, dense-V (one block per sector) included."""
+    """Each tile-shape variant (k_hv, the double-buffered staged k_hv_async and the
+    split k_hv_down + k_hv_async), pinned in turn, against the oracle on several
+    sectors.  The split variants need every down-spin block of the model in one
+    CTA's shared memory: the dense-V model has one block per sector and rejects
+    them with MO_ED_ERR_ARG."""
     s, m = setup(name, precision=precision)
     dt = pkg.FP32 if precision == "fp32" else pkg.FP64
     ns = m.nsite
@@ -136,18 +138,24 @@ def test_multiply_h_every_variant(setup, oracle, pkg, name, precision, tol):
             x = x.astype(np.float32)
         ref = oracle.multiply_H(m, b, x.astype(np.float64))
         variants, _ = s.hv_tuning(nu, nd, dt)
-        ran = 0
+        ran, staged, split = 0, 0, 0
         for v, (shape, ms) in enumerate(variants):
-            s.hv_set_variant(nu, nd, v, dt)
-            y = s.multiply_H(nu, nd, x)
+            try:
+                s.hv_set_variant(nu, nd, v, dt)
+                y = s.multiply_H(nu, nd, x)
+            except pkg.EDError as e:
+                assert e.code == 1, e       # MO_ED_ERR_ARG: the shape does not fit this sector
+                continue
             ran += 1
+            staged += shape[3] == 1
+            split += shape[3] >= 2
             assert rel(y, ref) < tol, (name, nu, nd, v, shape)
-        assert ran == len(variants) >= 3
+        assert ran >= 2 and staged >= 1
+        if name == "3x6_block":
+            assert split >= 2
 
 
 def test_multiply_h_mixed(setup, oracle):
-    """FP32 input, FP64-accumulated FP64 output, on device vectors placed with
-    the layout's column map (pads zero in and out)."""
     import torch
     s, m = setup("3x6_block")
     nu, nd = 4, 5
@@ -155,18 +163,15 @@ def test_multiply_h_mixed(setup, oracle):
     x = np.random.default_rng(3).standard_normal(b.ntot).astype(np.float32)
     ld, nelem = s.vector_layout(nu, nd)
     assert ld % 32 == 0 and nelem == ld * b.ndown
-    cols = s.vector_columns(nu, nd)
-    assert len(set(cols.tolist())) == b.nup and cols.max() < ld
-    xp = s.to_device_layout(nu, nd, x)
+    xp = np.zeros((b.ndown, ld), np.float32)
+    xp[:, :b.nup] = x.reshape(b.ndown, b.nup)
     dx = torch.from_numpy(xp.ravel()).cuda()
     dy = torch.empty(nelem, dtype=torch.float64, device="cuda")
     s.multiply_H_mixed_dev(nu, nd, dx.data_ptr(), dy.data_ptr())
     torch.cuda.synchronize()
     yp = dy.cpu().numpy().reshape(b.ndown, ld)
-    pad = np.ones(ld, bool)
-    pad[cols] = False
-    assert np.all(yp[:, pad] == 0)
-    assert rel(s.from_device_layout(nu, nd, yp), oracle.multiply_H(m, b, x.astype(np.float64))) < 1e-13
+    assert np.all(yp[:, b.nup:] == 0)
+    assert rel(yp[:, :b.nup].ravel(), oracle.multiply_H(m, b, x.astype(np.float64))) < 1e-13
 
 
 def test_multiply_h_symmetric_c3(setup, oracle):
@@ -208,14 +213,23 @@ def test_multiply_h_c4_full_size(solver, pkg):
     x32 = x.astype(np.float32)
     h64 = solver.multiply_H(nu, nd, x32.astype(np.float64))
     variants, chosen = solver.hv_tuning(nu, nd, pkg.FP32)
-    assert all(ms > 0 for _, ms in variants)
+    kinds = set()
     for v, (shape, ms) in enumerate(variants):
+        if ms < 0:
+            continue
         solver.hv_set_variant(nu, nd, v, pkg.FP32)
         assert rel(solver.multiply_H(nu, nd, x32), h64) < 2e-6, (v, shape)
+        kinds.add(shape[3])
+    assert kinds == {0, 1, 2, 3}
     variants, chosen = solver.hv_tuning(nu, nd, pkg.FP64)
     for v, (shape, ms) in enumerate(variants):
-        solver.hv_set_variant(nu, nd, v, pkg.FP64)
-        assert rel(solver.multiply_H(nu, nd, x), hx) < 1e-13, (v, shape)
+        if shape[3] >= 2:
+            try:   # FP64 move lists and slices may not fit one CTA for C4's blocks
+                solver.hv_set_variant(nu, nd, v, pkg.FP64)
+            except pkg.EDError as e:
+                assert e.code == 1, e
+                continue
+            assert rel(solver.multiply_H(nu, nd, x), hx) < 1e-13, (v, shape)
 
 
 # ---------------------------------------------------------------- apply_c
