@@ -40,96 +40,179 @@ __device__ __forceinline__ double2 zdiv(double2 a, double2 b)   // Smith (1962)
     return make_double2((a.x * r + a.y) / den, (a.y * r - a.x) / den);
 }
 
-// chi^2 of one parameter set xb by the whole CTA (blockDim.x threads, one
-// thread per frequency stripe): per-parameter partials in sm [nrow][blockDim.x]
-// summed in a fixed order; thread i < nrow writes row i (f, then g) to out[i].
+// 1/d for d > 0 from an FP32 seed y0 = rcp.approx(d) refined by one
+// third-order step of the Newton-Raphson family for the reciprocal,
+//   y1 = y0 + y0 (e + e^2),  e = 1 - d y0,
+// the truncated series y0 / (1 - e) = y0 (1 + e + e^2 + ...).  The seed's
+// relative error |e| is below 2^-22, so the truncation error |e|^3 < 2^-66 and
+// y1 is within one ulp of 1/d.  Outside the FP32 range of the seed (and for
+// d <= 0 or non-finite d) it falls back to the IEEE division.
+__device__ __forceinline__ double rcp_pos(double d)
+{
+    const float df = __double2float_rn(d);
+    if (!(df >= 1e-37f && df <= 1e37f)) return 1.0 / d;
+    float yf;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(df));
+    const double y0 = (double)yf;
+    const double e = fma(-d, y0, 1.0);
+    return fma(y0, fma(e, e, e), y0);
+}
+
+// fixed-order sum over the CTA of one value per thread (blockDim.x a multiple
+// of 32, at most 32 warps): a butterfly within each warp, then the warps' sums
+// in order by thread 0.  red: blockDim.x / 32 doubles of shared memory.
+__device__ __forceinline__ double cta_sum(double v, double *red)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+    return s;
+}
+
+// Shared memory of one chi2_block evaluation: per-parameter partials
+// [nx][nt] (rows eps_k, V_ak, ef_a), the thread's 1/z_k for its current w_n
+// [nbath][2][nt], V^2 [norb * nbath], and kRedSlots doubles for the sums.
+constexpr int kRedSlots = 4 * (kMaxX + 1);
+__host__ __device__ inline size_t chi2_smem_doubles(int nx, int nbath, int norb, int nt)
+{
+    return (size_t)nx * nt + 2 * (size_t)nbath * nt + (size_t)norb * nbath + kRedSlots;
+}
+
+// chi^2 of one parameter set xb (shared or global memory) by the whole CTA
+// (blockDim.x threads, a multiple of 32; thread t takes w_n, n = t mod
+// blockDim.x).  Per (w_n, bath level) one reciprocal 1/|z_k|^2 serves the
+// forward sum of every orbital and, kept in shared memory, the gradient
+// terms; couplings V_ak = 0 (with a finite eps_k) contribute exactly zero to
+// every sum and are skipped.  The 2 and 4 of the gradient formulas and the
+// 1/w_n weight of the residual are applied once per term group.  Per-thread
+// partials are summed in a fixed order.  Thread 0 writes out_f; the
+// gradient (grad) goes to out_g[0..nx).  Every thread returns after a final
+// barrier, so out_f / out_g may be shared memory read by all threads next.
 __device__ void chi2_block(const double *__restrict__ xb, int nx, bool grad, int nw, int norb, int nbath,
                            const double *__restrict__ omega, const double *__restrict__ dev, int fcmplx,
                            double *sm, double *out_f, double *out_g)
 {
     const int tid = threadIdx.x, nt = blockDim.x;
-    const int nrow = grad ? nx + 1 : 1;
-    for (int i = 0; i < nrow; ++i) sm[i * nt + tid] = 0.0;
-    // parameters (x_to_ev)
-    const double *eps = xb;                       // eps_k
-    const double *V = xb + nbath;                 // V[a*nbath + k]
-    const double *ef = xb + nx - norb;            // ef_a
+    double *sz = sm + (size_t)nx * nt;                 // [nbath][2][nt]
+    double *sv2 = sz + 2 * (size_t)nbath * nt;         // [norb][nbath]
+    double *red = sv2 + (size_t)norb * nbath;          // [kRedSlots]
+    const double *eps = xb;                            // eps_k
+    const double *V = xb + nbath;                      // V[a*nbath + k]
+    const double *ef = xb + nx - norb;                 // ef_a
+    for (int i = tid; i < norb * nbath; i += nt) sv2[i] = V[i] * V[i];
+    if (grad)
+        for (int i = 0; i < nx - norb; ++i) sm[(size_t)i * nt + tid] = 0.0;
+    __syncthreads();
+    double fsum = 0.0, gef[kMaxOrb];
+#pragma unroll
+    for (int a = 0; a < kMaxOrb; ++a) gef[a] = 0.0;
     for (int n = tid; n < nw; n += nt) {
         const double w = omega[n];
         const double wz = fcmplx ? (double)(float)w : w;
-        const double inv_w = 1.0 / w;
-        // 1 / z_k with z_k = i wz - eps_k: one real reciprocal per bath level,
-        // shared by every orbital of this frequency; the orbitals' sums stay
-        // in registers (norb <= kMaxOrb)
+        const double wz2 = wz * wz;
+        const double inv_w = rcp_pos(w);
+        // Delta(a, n) - ef_a = sum_k V_ak^2 / z_k, z_k = i wz - eps_k
         double dre[kMaxOrb], dim[kMaxOrb];
 #pragma unroll
         for (int a = 0; a < kMaxOrb; ++a) dre[a] = dim[a] = 0.0;
         for (int k = 0; k < nbath; ++k) {
-            const double inv = 1.0 / (eps[k] * eps[k] + wz * wz);
-            const double izr = -eps[k] * inv, izi = -wz * inv;
+            const double e = eps[k];
+            const double y = rcp_pos(fma(e, e, wz2));
+            const double izr = -e * y, izi = -wz * y;
+            const bool all = !isfinite(e);
+            if (grad) {
+                sz[(size_t)(2 * k) * nt + tid] = izr;
+                sz[(size_t)(2 * k + 1) * nt + tid] = izi;
+            }
 #pragma unroll
             for (int a = 0; a < kMaxOrb; ++a) {
                 if (a < norb) {
-                    const double v = V[a * nbath + k];
-                    dre[a] += v * v * izr;
-                    dim[a] += v * v * izi;
+                    const double v2 = sv2[a * nbath + k];
+                    if (v2 != 0.0 || all) {
+                        dre[a] = fma(v2, izr, dre[a]);
+                        dim[a] = fma(v2, izi, dim[a]);
+                    }
                 }
             }
         }
-        double rr[kMaxOrb], ri[kMaxOrb];
+        // r = Delta - D_ev; chi2 terms |r|^2 / w_n; weighted residuals for the gradient
+        double Rr[kMaxOrb], Ri[kMaxOrb];
 #pragma unroll
         for (int a = 0; a < kMaxOrb; ++a) {
-            rr[a] = ri[a] = 0.0;
+            Rr[a] = Ri[a] = 0.0;
             if (a < norb) {
                 const size_t di = 2 * ((size_t)n * norb + a);
-                rr[a] = (dre[a] + ef[a]) - dev[di];
-                ri[a] = dim[a] - dev[di + 1];
-                const double ar = hypot(rr[a], ri[a]);
-                sm[0 * nt + tid] += ar * ar / w;
+                const double rr = (dre[a] + ef[a]) - dev[di], ri = dim[a] - dev[di + 1];
+                fsum = fma(fma(rr, rr, ri * ri), inv_w, fsum);
+                Rr[a] = rr * inv_w;
+                Ri[a] = ri * inv_w;
+                gef[a] += Rr[a];
             }
         }
         if (grad) {
             for (int k = 0; k < nbath; ++k) {
-                const double inv = 1.0 / (eps[k] * eps[k] + wz * wz);
-                const double izr = -eps[k] * inv, izi = -wz * inv;
-                const double sr = izr * izr - izi * izi, si = 2.0 * izr * izi;   // 1 / z^2
+                const double izr = sz[(size_t)(2 * k) * nt + tid], izi = sz[(size_t)(2 * k + 1) * nt + tid];
+                const double sr = fma(izr, izr, -izi * izi), si = 2.0 * izr * izi;   // 1 / z^2
+                const bool all = !isfinite(eps[k]);
+                double ge = 0.0;
 #pragma unroll
                 for (int a = 0; a < kMaxOrb; ++a) {
                     if (a < norb) {
-                        const double v = V[a * nbath + k];
-                        // conjg(r) v v / z / z, with conjg(r) = (rr, -ri)
-                        const double cr = rr[a] * v * v, ci = -ri[a] * v * v;
-                        sm[(1 + k) * nt + tid] += 2.0 * (cr * sr - ci * si) * inv_w;
-                        // conjg(r) v / z + conjg(r) v / z
-                        const double t2 = rr[a] * v * izr + ri[a] * v * izi;
-                        sm[(1 + nbath + a * nbath + k) * nt + tid] += 2.0 * (t2 + t2) * inv_w;
+                        const double v2 = sv2[a * nbath + k];
+                        if (v2 != 0.0 || all) {
+                            // Re[conj(r) V^2 / z^2] and Re[conj(r) V / z], weighted by 1 / w_n
+                            ge = fma(v2, fma(Rr[a], sr, Ri[a] * si), ge);
+                            double &gv = sm[(size_t)(nbath + a * nbath + k) * nt + tid];
+                            gv = fma(V[a * nbath + k], fma(Rr[a], izr, Ri[a] * izi), gv);
+                        }
                     }
                 }
+                sm[(size_t)k * nt + tid] += ge;
             }
+        }
+    }
+    if (grad) {
 #pragma unroll
-            for (int a = 0; a < kMaxOrb; ++a)
-                if (a < norb) sm[(1 + nx - norb + a) * nt + tid] += 2.0 * rr[a] * inv_w;
+        for (int a = 0; a < kMaxOrb; ++a)
+            if (a < norb) sm[(size_t)(nx - norb + a) * nt + tid] = gef[a];
+    }
+    const double f = cta_sum(fsum, red);
+    const double fn = (double)(float)(norb * norb * nw);
+    if (tid == 0) *out_f = f / fn;
+    if (grad) {
+        // rows in four fixed column segments, then the segments in order
+        __syncthreads();
+        const int seg = nt / 4;
+        for (int i = tid; i < 4 * nx; i += nt) {
+            const int r = i >> 2, q = i & 3;
+            const double *row = sm + (size_t)r * nt + q * seg;
+            double s = 0.0;
+            for (int t = 0; t < seg; ++t) s += row[t];
+            red[i] = s;
+        }
+        __syncthreads();
+        const double gn1 = (double)(float)(norb * norb), gn2 = (double)(float)nw;
+        for (int i = tid; i < nx; i += nt) {
+            const double s = ((red[4 * i] + red[4 * i + 1]) + red[4 * i + 2]) + red[4 * i + 3];
+            const double c = (i >= nbath && i < nx - norb) ? 4.0 : 2.0;   // d/dV_ak carries 2 * 2
+            out_g[i] = c * s / gn1 / gn2;
         }
     }
     __syncthreads();
-    const double fn = (double)(float)(norb * norb * nw);
-    const double gn1 = (double)(float)(norb * norb), gn2 = (double)(float)nw;
-    for (int i = tid; i < nrow; i += nt) {
-        double s = 0.0;
-        for (int t = 0; t < nt; ++t) s += sm[i * nt + t];
-        if (i == 0) *out_f = s / fn;
-        else out_g[i - 1] = s / gn1 / gn2;
-    }
 }
 
 // x: [nreq][nx]; dev: Fortran (norb, nw) interleaved complex; f: [nreq];
 // g: [nreq][nx] (written only where want_grad[b] != 0, or all if want_grad null)
-__global__ void __launch_bounds__(kFitThreads)
+__global__ void __launch_bounds__(kFitThreads, 1)
 k_chi2(const double *__restrict__ x, int nx, const int *__restrict__ want_grad, int nw, int norb,
        int nbath, const double *__restrict__ omega, const double *__restrict__ dev, int fcmplx,
        double *__restrict__ f, double *__restrict__ g)
 {
-    extern __shared__ double sm[];          // [nx + 1][kFitThreads]
+    extern __shared__ double sm[];          // chi2_smem_doubles(nx, nbath, norb, kFitThreads)
     const int b = blockIdx.x;
     const bool grad = g != nullptr && (want_grad ? want_grad[b] != 0 : true);
     chi2_block(x + (size_t)b * nx, nx, grad, nw, norb, nbath, omega, dev, fcmplx, sm, f + b,
@@ -155,10 +238,11 @@ __global__ void k_calc_dev(int norb, int nbath, int nw, const double *omega, con
     dev[2 * (size_t)t + 1] = d.y;
 }
 
-static int chi2_smem_attr(mo_ed_ctx *ctx)
+// dynamic shared memory of k_chi2 / k_fit for these dimensions (128 threads)
+static int chi2_smem(mo_ed_ctx *ctx, const void *kernel, int nx, int nbath, int norb, size_t *bytes)
 {
-    MOED_CUDA(ctx, cudaFuncSetAttribute(k_chi2, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)(sizeof(double) * (kMaxX + 1) * kFitThreads)));
+    *bytes = sizeof(double) * chi2_smem_doubles(nx, nbath, norb, kFitThreads);
+    MOED_CUDA(ctx, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*bytes));
     return MO_ED_OK;
 }
 
@@ -168,8 +252,8 @@ int chi2_grad_dev(mo_ed_ctx *ctx, int nbatch, const double *x, int nwloc, int ns
 {
     (void)ns;
     if (nbatch <= 0) return MO_ED_OK;
-    const size_t smem = sizeof(double) * (size_t)(nxsize + 1) * kFitThreads;
-    if (int rc = chi2_smem_attr(ctx)) return rc;
+    size_t smem;
+    if (int rc = chi2_smem(ctx, (const void *)k_chi2, nxsize, nbath, norb, &smem)) return rc;
     k_chi2<<<nbatch, kFitThreads, smem, ctx->stream>>>(x, nxsize, nullptr, nwloc, norb, nbath, omega, dev,
                                                        ctx->opt.fortran_cmplx, f, want_grad ? g : nullptr);
     MOED_CHECK_LAUNCH(ctx);
@@ -188,7 +272,7 @@ static int fit_problem(mo_ed_ctx *ctx, FitProblem &P, const double *omega, const
                        int ns, int nxsize, int nbath, int norb)
 {
     if (!omega || !D_ev || nwloc < 1 || nbath < 0 || norb < 1 || ns != norb + nbath ||
-        nxsize != nbath + nbath * norb + norb || nxsize > kMaxX)
+        nxsize != nbath + nbath * norb + norb || nxsize > kMaxX || norb > kMaxOrb)
         return fail(ctx, MO_ED_ERR_ARG, "invalid fit dimensions");
     P.nwloc = nwloc;
     P.ns = ns;
@@ -200,7 +284,7 @@ static int fit_problem(mo_ed_ctx *ctx, FitProblem &P, const double *omega, const
     MOED_CUDA(ctx, cudaMemcpyAsync(P.omega.p, omega, sizeof(double) * nwloc, cudaMemcpyHostToDevice, ctx->stream));
     MOED_CUDA(ctx, cudaMemcpyAsync(P.dev.p, D_ev, sizeof(double) * 2 * (size_t)norb * nwloc,
                                    cudaMemcpyHostToDevice, ctx->stream));
-    return chi2_smem_attr(ctx);
+    return MO_ED_OK;
 }
 
 // Evaluate nreq requests (x host [nreq][nx], want_grad host [nreq]).
@@ -221,7 +305,8 @@ struct Evaluator {
         }
         MOED_CUDA(ctx, cudaMemcpyAsync(dx.p, x, sizeof(double) * nreq * nx, cudaMemcpyHostToDevice, ctx->stream));
         MOED_CUDA(ctx, cudaMemcpyAsync(dw.p, want, sizeof(int) * nreq, cudaMemcpyHostToDevice, ctx->stream));
-        const size_t smem = sizeof(double) * (size_t)(nx + 1) * kFitThreads;
+        size_t smem;
+        if (int rc = chi2_smem(ctx, (const void *)k_chi2, nx, P->nbath, P->norb, &smem)) return rc;
         k_chi2<<<nreq, kFitThreads, smem, ctx->stream>>>((const double *)dx.p, nx, (const int *)dw.p, P->nwloc,
                                                          P->norb, P->nbath, (const double *)P->omega.p,
                                                          (const double *)P->dev.p, ctx->opt.fortran_cmplx,
@@ -244,15 +329,11 @@ struct Frprmn {
     DF dfunc;
     int n;
     const double *pcom = nullptr, *xicom = nullptr;
-    double xt[kMaxX];
 
     __host__ __device__ static double fsign(double a, double b) { return b >= 0.0 ? fabs(a) : -fabs(a); }
 
-    __host__ __device__ double f1dim(double x)   // frprmn.f90:212-234
-    {
-        for (int j = 0; j < n; ++j) xt[j] = pcom[j] + x * xicom[j];
-        return func(xt);
-    }
+    // frprmn.f90:212-234: func at pcom + x xicom (formed by the functor)
+    __host__ __device__ double f1dim(double x) { return func.line(pcom, xicom, x); }
 
     __host__ __device__ void mnbrak(double &ax, double &bx, double &cx, double &fa, double &fb, double &fc)
     {
@@ -425,39 +506,50 @@ struct Frprmn {
 // (chi2_block) and broadcast through shared memory, so all threads follow the
 // same path.  No host round trip per evaluation.
 // ---------------------------------------------------------------------------
-constexpr int kFitCta = 128;   // threads per fit: all four SM sub-partitions' FP64 units
+constexpr int kFitCta = kFitThreads;   // threads per fit: all four SM sub-partitions' FP64 units
 
 struct DevChi2 {
     int nx, nw, norb, nbath, fcmplx;
     const double *omega, *dev;
     double *sm, *sx, *sres;
-    __device__ double eval(const double *x, double *g)
+    // chi^2 (and the gradient into g) at the point sx, already in shared memory
+    __device__ double eval_sx(double *g)
     {
-        for (int j = threadIdx.x; j < nx; j += blockDim.x) sx[j] = x[j];
         __syncthreads();
         chi2_block(sx, nx, g != nullptr, nw, norb, nbath, omega, dev, fcmplx, sm, sres, sres + 1);
-        __syncthreads();
         if (g)
             for (int j = 0; j < nx; ++j) g[j] = sres[1 + j];
         const double f = sres[0];
         __syncthreads();   // sx / sres are reused by the next evaluation
         return f;
     }
+    __device__ double eval(const double *x, double *g)
+    {
+        for (int j = threadIdx.x; j < nx; j += blockDim.x) sx[j] = x[j];
+        return eval_sx(g);
+    }
+    // f1dim's point p + t xi, each element formed once, by one thread
+    __device__ double line(const double *p, const double *xi, double t)
+    {
+        for (int j = threadIdx.x; j < nx; j += blockDim.x) sx[j] = p[j] + t * xi[j];
+        return eval_sx(nullptr);
+    }
 };
 struct DevFunc {
     DevChi2 *c;
     __device__ double operator()(const double *x) const { return c->eval(x, nullptr); }
+    __device__ double line(const double *p, const double *xi, double t) const { return c->line(p, xi, t); }
 };
 struct DevDFunc {
     DevChi2 *c;
     __device__ void operator()(const double *x, double *g) const { c->eval(x, g); }
 };
 
-__global__ void __launch_bounds__(kFitCta)
+__global__ void __launch_bounds__(kFitCta, 1)
 k_fit(double *__restrict__ X, int nx, int nw, int norb, int nbath, const double *__restrict__ omega,
       const double *__restrict__ dev, int fcmplx, double ftol, double *fret, int *iter, int *status)
 {
-    extern __shared__ double sm[];   // [nx + 1][kFitCta] partial sums
+    extern __shared__ double sm[];   // chi2_smem_doubles(nx, nbath, norb, kFitCta)
     __shared__ double sx[kMaxX], sres[kMaxX + 1];
     const int b = blockIdx.x;
     DevChi2 c{nx, nw, norb, nbath, fcmplx, omega, dev, sm, sx, sres};
@@ -486,9 +578,8 @@ static int fit_on_device(mo_ed_ctx *ctx, FitProblem &P, int nbatch, double *x, d
     if (int rc = dev_alloc(ctx, di, sizeof(int) * nbatch)) return rc;
     if (int rc = dev_alloc(ctx, ds, sizeof(int) * nbatch)) return rc;
     MOED_CUDA(ctx, cudaMemcpyAsync(dx.p, x, sizeof(double) * (size_t)nbatch * nx, cudaMemcpyHostToDevice, ctx->stream));
-    const size_t smem = sizeof(double) * (size_t)(nx + 1) * kFitCta;
-    MOED_CUDA(ctx, cudaFuncSetAttribute(k_fit, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)(sizeof(double) * (kMaxX + 1) * kFitCta)));
+    size_t smem;
+    if (int rc = chi2_smem(ctx, (const void *)k_fit, nx, P.nbath, P.norb, &smem)) return rc;
     k_fit<<<nbatch, kFitCta, smem, ctx->stream>>>((double *)dx.p, nx, P.nwloc, P.norb, P.nbath,
                                                 (const double *)P.omega.p, (const double *)P.dev.p,
                                                 ctx->opt.fortran_cmplx, ftol, (double *)df.p, (int *)di.p,
@@ -541,7 +632,7 @@ int mo_ed_chi2_grad_dev(mo_ed_ctx *ctx, int nbatch, const double *x, int nwloc, 
 {
     if (!ctx) return MO_ED_ERR_ARG;
     cudaSetDevice(ctx->device);
-    if (!x || !f || !omega || !D_ev || nbatch < 0 || nxsize > kMaxX ||
+    if (!x || !f || !omega || !D_ev || nbatch < 0 || nxsize > kMaxX || norb < 1 || norb > kMaxOrb ||
         nxsize != nbath + nbath * norb + norb || ns != norb + nbath)
         return fail(ctx, MO_ED_ERR_ARG, "bad arguments");
     return chi2_grad_dev(ctx, nbatch, x, nwloc, ns, nxsize, omega, D_ev, nbath, norb, f, g, g != nullptr);

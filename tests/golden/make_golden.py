@@ -1,8 +1,8 @@
 """Generate the committed golden fixtures under tests/golden/.
 
-Run in a container that has the reference sources mounted (it reads
-$MO_DMFT_REFERENCE, default /root/reference); the GPU-side tests only read
-the JSON files written here.
+Run where the reference sources are available, giving their root as the
+first argument or in $MO_DMFT_REFERENCE (there is no default); the tests
+only read the JSON files written here.
 
 notebook_hmat.json
     The reference's only known-answer test: the 9x9 Hamiltonian matrix that
@@ -16,7 +16,7 @@ import json
 import os
 import re
 
-REF = os.environ.get("MO_DMFT_REFERENCE", "/root/reference")
+REF = None   # the reference's root: first argument or $MO_DMFT_REFERENCE
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -71,4 +71,8 @@ def main():
 
 
 if __name__ == "__main__":
+    import sys
+    REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MO_DMFT_REFERENCE")
+    if not REF:
+        sys.exit("usage: make_golden.py REFERENCE_ROOT  (or set MO_DMFT_REFERENCE)")
     main()
