@@ -14,19 +14,24 @@ the reference are identities here.
 """
 from __future__ import annotations
 
+import time
+
 import numpy as np
 
 from .ed import EDSolver, ev_to_x, matsubara, x_to_ev
 
 
 def dmft_loop(solver: EDSolver, inp: dict, nloop: int | None = None, precision: str = "fp32",
-              green_fp64: bool = False, callback=None) -> dict:
+              green_fp64: bool = False, callback=None, trace: list | None = None) -> dict:
     """Run the DMFT loop of main.f90 with the parameters of an FDF input.
 
     solver: an open EDSolver (its options, model, sectors and omega are set here).
     inp: configs.read_fdf output.  nloop overrides DMFT.MaxIterations.
     callback(iteration, record) is called after every iteration with its record
-    (scf_diff, chi^2, CG iterations, occupations, nev_calc).
+    (scf_diff, chi^2, CG iterations, occupations, nev_calc, seconds).
+    trace: a list that receives, per iteration, the iteration's starting bath
+    (ek, vk, ef), the D_ev it starts from, Gr, Gksum, the new D_ev of
+    delta_new and the fitted parameters x (copies).
 
     Returns dict(converged, iterations, history, Gr, D_ev, Gksum, Sigma, ek, vk, ef, nocc, omega)."""
     norb, nbath = inp["DMFT.Norbs"], inp["DMFT.Nbaths"]
@@ -55,6 +60,9 @@ def dmft_loop(solver: EDSolver, inp: dict, nloop: int | None = None, precision: 
     history, converged, iloop = [], False, 0
     Gr = Gksum = nocc = None
     while not converged and iloop < nloop:
+        t0 = time.perf_counter()
+        if trace is not None:
+            step = dict(ek=ek.copy(), vk=vk.copy(), ef=np.array(ef, dtype=np.float64), D_ev_in=D_ev.copy())
         solver.set_model(norb, nbath, U, J, ek, vk)
         states = solver.ed_solve()
         Gr = solver.ed_calc_green_ftn()
@@ -62,6 +70,9 @@ def dmft_loop(solver: EDSolver, inp: dict, nloop: int | None = None, precision: 
         nocc = solver.n_from_gksum(Gksum, beta)
         x = ev_to_x(ek, vk, ef, nsite, nbath)
         x, fret, it = solver.minimization(x, nw, nsite, nx, omega, D_ev, nbath, norb)
+        if trace is not None:
+            step.update(Gr=Gr.copy(), Gksum=np.array(Gksum), D_ev=D_ev.copy(), x=np.array(x))
+            trace.append(step)
         ef, ek, vk = x_to_ev(x, nsite, nbath, norb)
         # scf_diff (main.f90:95-101): mean over orbitals of sum_w |Gr_prev - Gr| / float(Nw)
         tol = float(np.sum(np.abs(Gr_prev - Gr).sum(axis=1) / float(np.float32(nw))) / norb)
@@ -69,7 +80,7 @@ def dmft_loop(solver: EDSolver, inp: dict, nloop: int | None = None, precision: 
         D_ev = solver.calc_dev(norb, nsite, omega, ek, vk, ef)
         converged = tol < scf_tol
         rec = dict(iteration=iloop, scf_diff=tol, chi2=fret, cg_iterations=it, nocc=nocc.tolist(),
-                   nev_calc=len(states))
+                   nev_calc=len(states), seconds=time.perf_counter() - t0)
         history.append(rec)
         if callback is not None:
             callback(iloop, rec)

@@ -507,36 +507,48 @@ def test_eigvec_and_apbpanbn_files(pkg, oracle, tmp_path, precision):
     s3.close()
 
 
-def test_dmft_loop_first_iteration(pkg, oracle, tmp_path):
-    """main.f90's DMFT loop through the C-ABI (dmft_loop) on C1 written as
-    an FDF input: the first iteration's G(i w_n), Gksum and occupations
-    against the oracle's chain (ed_solve, ed_calc_green_ftn, ed_delta_new,
-    n_from_gksum) from the same start, and a fitted bath whose chi^2 is no
-    worse than the oracle's frprmn from the same start."""
+def test_dmft_loop_two_iterations(pkg, oracle, tmp_path):
+    """main.f90's DMFT loop through the C-ABI (dmft_loop) on C1 written as an
+    FDF input, two iterations, each against the oracle's chain from the same
+    starting bath: G(i w_n), Gksum, the new D_ev and the occupations
+    (ed_solve, ed_calc_green_ftn, ed_delta_new, n_from_gksum) to 1e-8, the
+    fitted chi^2 no worse than the oracle's frprmn from the same start, and
+    scf_diff.  The second iteration starts from the first's fitted bath
+    (x_to_ev of its x, impurity levels included) bit for bit."""
     cfg = pkg.configs.config("C1")
     p = tmp_path / "input.fdf"
     pkg.configs.write_fdf(cfg, p, nev=8, nq=400)
     inp = pkg.configs.read_fdf(str(p))
     s = pkg.EDSolver(0)
-    out = pkg.dmft_loop(s, inp, nloop=1, precision="fp64")
+    trace = []
+    out = pkg.dmft_loop(s, inp, nloop=2, precision="fp64", trace=trace)
     s.close()
-    assert out["iterations"] == 1 and np.all(np.isfinite(out["Sigma"]))
+    assert out["iterations"] == 2 and len(trace) == 2 and np.all(np.isfinite(out["Sigma"]))
     norb, nbath, ns = cfg.norb, cfg.nbath, cfg.nsite
-    hk, ef = oracle.set_band_structure(norb, 400)
-    ek = np.concatenate([ef, inp["eps_bath"]])
-    vk = inp["vk"]
+    hk, ef_band = oracle.set_band_structure(norb, 400)
     om = oracle.matsubara(cfg.nw, cfg.beta)
-    dev0 = oracle.calc_dev(norb, ns, om, ek, vk, ef)
-    m = oracle.Model(norb, nbath, cfg.U, cfg.J, ek, vk)
-    st_o, vecs = oracle.ed_solve(m, inp["sectors"], 8, cfg.beta)
-    Gr_o = oracle.ed_calc_green_ftn(m, inp["sectors"], st_o, vecs, cfg.nstep, om)
-    assert rel(out["Gr"], Gr_o) < 1e-8
-    dn_o, gk_o = oracle.delta_new(hk, inp["DMFT.Mu"], Gr_o, dev0)
-    assert rel(out["Gksum"], gk_o) < 1e-8
-    assert np.abs(out["nocc"] - oracle.n_from_gksum(gk_o, cfg.beta)).max() < 1e-8
-    x0 = oracle.ev_to_x(ek, vk, ef, ns, nbath)
-    _, f_o, _, _ = oracle.frprmn(x0, ns, om, dn_o, nbath, norb)
-    assert out["history"][0]["chi2"] <= 1.1 * f_o + 1e-10
+    assert np.abs(trace[0]["ef"] - ef_band).max() < 1e-14
+    Gr_prev = np.zeros_like(trace[0]["Gr"])
+    for i, t in enumerate(trace):
+        if i:
+            ef1, ek1, vk1 = oracle.x_to_ev(trace[i - 1]["x"], ns, nbath, norb)
+            assert np.array_equal(t["ek"], ek1) and np.array_equal(t["vk"], vk1) and np.array_equal(t["ef"], ef1)
+        assert rel(t["D_ev_in"], oracle.calc_dev(norb, ns, om, t["ek"], t["vk"], t["ef"])) < 1e-13
+        m = oracle.Model(norb, nbath, cfg.U, cfg.J, t["ek"], t["vk"])
+        st_o, vecs = oracle.ed_solve(m, inp["sectors"], 8, cfg.beta)
+        Gr_o = oracle.ed_calc_green_ftn(m, inp["sectors"], st_o, vecs, cfg.nstep, om)
+        assert rel(t["Gr"], Gr_o) < 1e-8
+        dn_o, gk_o = oracle.delta_new(hk, inp["DMFT.Mu"], Gr_o, t["D_ev_in"])
+        assert rel(t["Gksum"], gk_o) < 1e-8
+        assert rel(t["D_ev"], dn_o) < 1e-8
+        rec = out["history"][i]
+        assert np.abs(np.array(rec["nocc"]) - oracle.n_from_gksum(gk_o, cfg.beta)).max() < 1e-8
+        x0 = oracle.ev_to_x(t["ek"], t["vk"], t["ef"], ns, nbath)
+        _, f_o, _, _ = oracle.frprmn(x0, ns, om, t["D_ev"], nbath, norb)
+        assert rec["chi2"] <= 1.1 * f_o + 1e-10
+        scf = np.sum(np.abs(Gr_prev - Gr_o).sum(axis=1) / float(np.float32(cfg.nw))) / norb
+        assert abs(rec["scf_diff"] - scf) < 1e-8 * max(1.0, scf)
+        Gr_prev = t["Gr"]
 
 
 # ---------------------------------------------------------------- bath fit
