@@ -147,15 +147,62 @@ def cpu_baseline_sample(cfg, nup, ndn, seconds=3.0):
                 sample=f"{done} of {b.ntot} rows of one FP64 H*v (oracle C port, OpenMP over rows), {dt:.2f} s")
 
 
+def lanczos_g_cpu(pkg, name, nev, states, matvecs, full=False, seconds=3.0):
+    """The oracle's ed_solve + ed_calc_green_ftn on the host cores (scipy
+    ARPACK on the C restatement of multiply_H, OpenMP over rows; the
+    reference's continued-fraction Lanczos), for comparison with the device's
+    Lanczos+G of the same configuration.
+
+    full: the whole oracle path is timed.  Otherwise the time is extrapolated
+    from the oracle's H*v rate on a row sample of the first sector (about
+    `seconds` of work): (eigensolver matvecs of the device's FP64 run) x
+    t(H*v, ground sector) + nstep x sum over the excitations of the kept
+    states of t(H*v, target sector) -- H*v alone, so a lower bound."""
+    import math
+    import __graft_entry__ as g
+    O = g.load_oracle()
+    cfg = pkg.configs.config(name)
+    ek, vk = cfg.model()
+    m = O.Model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
+    cores = os.cpu_count()
+    if full:
+        om = cfg.omega()
+        t0 = time.perf_counter()
+        st, vecs = O.ed_solve(m, cfg.sectors, nev, cfg.beta)
+        t1 = time.perf_counter()
+        O.ed_calc_green_ftn(m, cfg.sectors, st, vecs, cfg.nstep, om)
+        t2 = time.perf_counter()
+        return {"kind": "port", "mode": "full", "solve_s": round(t1 - t0, 3), "green_s": round(t2 - t1, 3),
+                "total_s": round(t2 - t0, 3), "cores": cores,
+                "sample": "oracle ed_solve (scipy ARPACK on the C multiply_H, OpenMP) + ed_calc_green_ftn, whole run"}
+    nelec, nup = cfg.sectors[0]
+    smp = cpu_baseline_sample(cfg, nup, nelec - nup, seconds)
+    t_elem = 2.0 * 8 / (smp["value"] * 1e9)           # seconds per row of H*v
+    dim = lambda nu, nd: math.comb(cfg.nsite, nu) * math.comb(cfg.nsite, nd)
+    rows = matvecs * dim(nup, nelec - nup)
+    for s in states:
+        nu_, nd_ = s["nup"], s["ndown"]
+        for ispin in ((1,) if nu_ == nd_ else (1, 2)):
+            for d in (1, -1):
+                tu, td = nu_ + (d if ispin == 1 else 0), nd_ + (d if ispin == 2 else 0)
+                if 0 <= tu <= cfg.nsite and 0 <= td <= cfg.nsite:
+                    rows += cfg.norb * cfg.nstep * dim(tu, td)
+    return {"kind": "port", "mode": "extrapolated (H*v only: a lower bound)", "total_s": round(rows * t_elem, 1),
+            "cores": cores, "hv_rows": int(rows), "rows_per_s": round(1.0 / t_elem),
+            "sample": smp["sample"] + f"; {matvecs} eigensolver matvecs (device FP64 run) + "
+                      f"{cfg.nstep} steps per excitation of {len(states)} kept state(s)"}
+
+
 # H*v kernel of each tile-shape variant kind (hv_tuning's fourth field)
 KERNEL_NAMES = {0: "k_hv", 1: "k_hv_async", 2: "k_hv_down (128-byte slices) + k_hv_async<split>",
                 3: "k_hv_down (64-byte slices) + k_hv_async<split>"}
 
 
-def lanczos_g(pkg, name, nev, precisions=("fp32", "fp32+g64", "fp64")):
+def lanczos_g(pkg, name, nev, precisions=("fp32", "fp32+g64", "fp64"), cpu=None):
     """Eigensolve + Green's function in FP32-mixed, FP32-mixed with an FP64
     Green's-function recurrence ("fp32+g64") and FP64; times and errors
-    against the FP64 run."""
+    against the FP64 run.  cpu: None, "auto" (the oracle's whole path for C1
+    and C2, an extrapolation for larger sectors) or "full"."""
     import torch
     cfg = pkg.configs.config(name)
     ek, vk = cfg.model()
@@ -192,6 +239,16 @@ def lanczos_g(pkg, name, nev, precisions=("fp32", "fp32+g64", "fp64")):
         o["dE_kept_max"] = max(abs(a["val"] - b["val"]) for a, b in zip(s32, s64)) if len(s32) == len(s64) else None
         o["dG_rel"] = float(np.abs(g32 - g64).max() / np.abs(g64).max())
         o["speedup_vs_fp64"] = round(out["fp64"]["total_s"] / o["total_s"], 3)
+    if cpu:
+        states = []
+        for st in s64:
+            nelec, nup = cfg.sectors[st["sector"] - 1]
+            states.append(dict(nup=nup, ndown=nelec - nup))
+        full = cpu == "full" or name in ("C1", "C2")
+        c = lanczos_g_cpu(pkg, name, nev, states, out["fp64"]["eigensolver"]["matvecs"], full=full)
+        for prec in res:
+            c[f"speedup_{prec}"] = round(c["total_s"] / out[prec]["total_s"], 1)
+        out["cpu"] = c
     return out
 
 
@@ -260,6 +317,38 @@ def fit_bench(pkg, cpu_fits=2):
         out["cpu_s_per_fit"] = round(t_cpu, 4)
         out["cpu_sample"] = f"oracle frprmn (C port, 1 core) on the first {cpu_fits} starts"
     return out
+
+
+def dmft_loop_bench(pkg, name, nloop, precision="fp32", scf_tol=1e-4, fit_starts=1, nev=6):
+    """main.f90's DMFT loop (dmft_loop, every step through the C-ABI) on an
+    impurity configuration written as an FDF input, at the reference's Nq =
+    10,000: wall time per iteration (ed_solve + Green's function + delta_new
+    + occupations + one device frprmn fit + calc_dev) and the scf_diff, chi^2
+    and CG-iteration history."""
+    import tempfile
+    cfg = pkg.configs.config(name)
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "input.fdf")
+        pkg.configs.write_fdf(cfg, path, nev=nev, nq=10000, nloop=nloop, scf_tol=scf_tol)
+        inp = pkg.configs.read_fdf(path)
+    s = pkg.EDSolver(0)
+    h, stopped, converged = [], None, False
+    t0 = time.perf_counter()
+    try:
+        out = pkg.dmft_loop(s, inp, precision=precision, callback=lambda i, r: h.append(r), fit_starts=fit_starts)
+        converged = bool(out["converged"])
+    except pkg.EDError as e:
+        if e.code != 6:        # MO_ED_ERR_FIT: frprmn's own limits, where the reference STOPs
+            raise
+        stopped = f"frprmn stopped by its iteration limit in DMFT iteration {len(h) + 1} ({e})"
+    total = time.perf_counter() - t0
+    s.close()
+    return {"config": name, "precision": precision, "nev": nev, "nq": 10000, "nw": cfg.nw, "scf_tol": scf_tol,
+            "fit_starts": fit_starts,
+            "iterations": len(h), "converged": converged, "stopped": stopped, "total_s": round(total, 3),
+            "seconds_per_iteration": [round(r["seconds"], 4) for r in h],
+            "scf_diff": [float(r["scf_diff"]) for r in h], "chi2": [float(r["chi2"]) for r in h],
+            "cg_iterations": [int(r["cg_iterations"]) for r in h], "nocc_last": h[-1]["nocc"] if h else None}
 
 
 def run_ours(args):
@@ -357,11 +446,15 @@ def run_ours(args):
     lg = None
     fit = None
     if rank == 0 and not args.no_lanczos_g:
-        lg = {c: guarded(lanczos_g, pkg, c, args.lg_nev, tuple(args.lg_precisions.split(",")))
+        lg = {c: guarded(lanczos_g, pkg, c, args.lg_nev, tuple(args.lg_precisions.split(",")),
+                         None if args.no_cpu else args.lg_cpu)
               for c in args.lg_config.split(",") if c}
     if rank == 0 and not args.no_fit:
         fit = guarded(fit_bench, pkg, 0 if args.no_cpu else 2)
     dmft = guarded(dmft_bench, pkg, not args.no_cpu) if rank == 0 and not args.no_fit else None
+    loops = None
+    if rank == 0 and args.dmft_loop:
+        loops = [guarded(dmft_loop_bench, pkg, *parse_loop(spec)) for spec in args.dmft_loop.split(",") if spec]
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         cpu = guarded(cpu_baseline_sample, cfg, nup, ndn)
@@ -388,6 +481,7 @@ def run_ours(args):
             "lanczos_g": lg,
             "fit": fit,
             "dmft_delta_new": dmft,
+            "dmft_loop": loops,
         }
         print(json.dumps(line), flush=True)
     s.close()
@@ -437,6 +531,14 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def parse_loop(spec):
+    """CONFIG:ITERATIONS[:PRECISION[:SCF_TOLERANCE[:FIT_STARTS]]] -> (name, nloop, precision, scf_tol,
+    fit_starts)."""
+    f = spec.split(":")
+    return (f[0], int(f[1]), (f[2] if len(f) > 2 else "fp32"), (float(f[3]) if len(f) > 3 else 1e-4),
+            (int(f[4]) if len(f) > 4 else 1))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -454,6 +556,14 @@ def main():
                     help="only the Lanczos+G pipeline (one JSON object per configuration; for profiling)")
     ap.add_argument("--lg-precisions", default="fp32,fp32+g64,fp64",
                     help="modes of Lanczos+G: fp32, fp32+g64 (FP64 Green's-function recurrence), fp64")
+    ap.add_argument("--lg-cpu", default="auto", choices=["auto", "full"],
+                    help="CPU leg of Lanczos+G: the oracle's whole path for C1/C2 and an extrapolation from an "
+                         "H*v sample for larger sectors (auto), or the whole path everywhere (full: minutes)")
+    ap.add_argument("--dmft-loop", default="C1:20:fp64",
+                    help="DMFT-loop runs CONFIG:ITERATIONS[:PRECISION[:SCF_TOLERANCE[:FIT_STARTS]]], "
+                         "comma-separated ('' for none)")
+    ap.add_argument("--dmft-loop-only", action="store_true",
+                    help="only the DMFT-loop runs (one JSON object per run)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -463,7 +573,15 @@ def main():
         torch.cuda.set_stream(torch.cuda.Stream())
         pkg = g.load_package()
         for c in args.lg_config.split(","):
-            print(json.dumps(lanczos_g(pkg, c, args.lg_nev, tuple(args.lg_precisions.split(",")))), flush=True)
+            print(json.dumps(lanczos_g(pkg, c, args.lg_nev, tuple(args.lg_precisions.split(",")),
+                                       None if args.no_cpu else args.lg_cpu)), flush=True)
+        return
+    if args.dmft_loop_only:
+        import __graft_entry__ as g
+        pkg = g.load_package()
+        for spec in args.dmft_loop.split(","):
+            if spec:
+                print(json.dumps(dmft_loop_bench(pkg, *parse_loop(spec))), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)

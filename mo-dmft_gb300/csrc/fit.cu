@@ -23,6 +23,8 @@
 #include <cmath>
 #include <cstring>
 
+#include <cooperative_groups.h>
+
 #include "internal.h"
 
 namespace moed {
@@ -43,17 +45,23 @@ __device__ __forceinline__ double2 zdiv(double2 a, double2 b)   // Smith (1962)
 // 1/d for d > 0 from an FP32 seed y0 = rcp.approx(d) refined by one
 // third-order step of the Newton-Raphson family for the reciprocal,
 //   y1 = y0 + y0 (e + e^2),  e = 1 - d y0,
-// the truncated series y0 / (1 - e) = y0 (1 + e + e^2 + ...).  The seed's
-// relative error |e| is below 2^-22, so the truncation error |e|^3 < 2^-66 and
-// y1 is within one ulp of 1/d.  Outside the FP32 range of the seed (and for
-// d <= 0 or non-finite d) it falls back to the IEEE division.
+// the truncated series y0 / (1 - e) = y0 (1 + e + e^2 + ...).  d is narrowed
+// to FP32 by truncating its significand (relative error < 2^-23) and the seed
+// widened back exactly, both with integer operations, so the FP64 pipe sees
+// only the three FMAs.  The seed's relative error |e| is below 2^-21, the
+// truncation error |e|^3 < 2^-63, and y1 is within one ulp of 1/d.  Outside
+// [2^-125, 2^126) (and for d <= 0, non-finite d) it is the IEEE division.
 __device__ __forceinline__ double rcp_pos(double d)
 {
-    const float df = __double2float_rn(d);
-    if (!(df >= 1e-37f && df <= 1e37f)) return 1.0 / d;
+    const long long b = __double_as_longlong(d);
+    const int ex = (int)(b >> 52);                          // biased exponent (sign bit 0)
+    if ((unsigned)(ex - 898) > 250u) return 1.0 / d;        // FP32 exponent ex - 896 outside [2, 252]
+    const float df = __int_as_float(((ex - 896) << 23) | (int)((b >> 29) & 0x7fffff));
     float yf;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(df));
-    const double y0 = (double)yf;
+    const int fb = __float_as_int(yf);                      // a normal float: 1/df in (2^-126, 2^125]
+    const double y0 = __longlong_as_double(((long long)(((fb >> 23) & 0xff) + 896) << 52) |
+                                           ((long long)(fb & 0x7fffff) << 29));
     const double e = fma(-d, y0, 1.0);
     return fma(y0, fma(e, e, e), y0);
 }
@@ -73,105 +81,129 @@ __device__ __forceinline__ double cta_sum(double v, double *red)
     return s;
 }
 
-// Shared memory of one chi2_block evaluation: per-parameter partials
-// [nx][nt] (rows eps_k, V_ak, ef_a), the thread's 1/z_k for its current w_n
-// [nbath][2][nt], V^2 [norb * nbath], and kRedSlots doubles for the sums.
+// Shared memory of one chi2_block evaluation (doubles, then ints):
+//   per-parameter partials [nx][nt] (rows eps_k, V_ak, ef_a);
+//   1/z_k of the thread's current w_n, [nbath][2][nt];
+//   kRedSlots doubles for the sums;
+//   per orbital a the couplings that enter its sums: V_ak^2 and V_ak
+//   [kMaxOrb][kListMax] each, bath level k [kMaxOrb][kListMax] and the count.
+// nx <= kMaxX = 60 with norb >= 1 bounds nbath by 29 < kListMax.
 constexpr int kRedSlots = 4 * (kMaxX + 1);
-__host__ __device__ inline size_t chi2_smem_doubles(int nx, int nbath, int norb, int nt)
+constexpr int kListMax = 32;
+__host__ __device__ inline size_t chi2_smem_bytes(int nx, int nbath, int nt)
 {
-    return (size_t)nx * nt + 2 * (size_t)nbath * nt + (size_t)norb * nbath + kRedSlots;
+    return sizeof(double) * ((size_t)nx * nt + 2 * (size_t)nbath * nt + kRedSlots + 2 * kMaxOrb * kListMax) +
+           sizeof(int) * (kMaxOrb * kListMax + kMaxOrb);
 }
 
-// chi^2 of one parameter set xb (shared or global memory) by the whole CTA
-// (blockDim.x threads, a multiple of 32; thread t takes w_n, n = t mod
-// blockDim.x).  Per (w_n, bath level) one reciprocal 1/|z_k|^2 serves the
-// forward sum of every orbital and, kept in shared memory, the gradient
-// terms; couplings V_ak = 0 (with a finite eps_k) contribute exactly zero to
-// every sum and are skipped.  The 2 and 4 of the gradient formulas and the
-// 1/w_n weight of the residual are applied once per term group.  Per-thread
-// partials are summed in a fixed order.  Thread 0 writes out_f; the
-// gradient (grad) goes to out_g[0..nx).  Every thread returns after a final
-// barrier, so out_f / out_g may be shared memory read by all threads next.
-__device__ void chi2_block(const double *__restrict__ xb, int nx, bool grad, int nw, int norb, int nbath,
-                           const double *__restrict__ omega, const double *__restrict__ dev, int fcmplx,
-                           double *sm, double *out_f, double *out_g)
+__device__ __forceinline__ bool finite_bits(double x)
+{
+    return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
+}
+
+// Sums of the chi^2 terms of one parameter set xb (shared or global memory)
+// by the whole CTA (blockDim.x threads, a multiple of 32) over the w_n with
+// n = n_first + t + k n_step (thread t; n_step = blockDim.x when one CTA
+// takes every w_n).
+//  * Per (w_n, bath level) one reciprocal 1/|z_k|^2 gives 1/z_k, kept in
+//    shared memory for every orbital's sum and the gradient terms.
+//  * Orbital a sums over the bath levels it couples to, listed once per
+//    evaluation: a coupling V_ak = 0 with a finite eps_k contributes exactly
+//    zero to every sum (a non-finite eps_k is kept for every orbital, so it
+//    propagates as in the reference).  The lists keep ascending k, the
+//    reference's order of the sum over k.
+//  * The 2 and 4 of the gradient formulas and the 1/w_n weight of the
+//    residual are applied once per term group.
+// Per-thread partials are summed in a fixed order.  out[0] = sum_n,a
+// |r|^2 / w_n (thread 0); with grad out[1 + i] = the unscaled sum of
+// gradient row i (chi2_scale turns the sums into FUNC / dfunc).  Every
+// thread returns after a final barrier, so out may be shared memory read by
+// all next.
+__device__ void chi2_sums(const double *__restrict__ xb, int nx, bool grad, int nw, int n_first, int n_step,
+                          int norb, int nbath, const double *__restrict__ omega, const double *__restrict__ dev,
+                          int fcmplx, double *sm, double *out)
 {
     const int tid = threadIdx.x, nt = blockDim.x;
     double *sz = sm + (size_t)nx * nt;                 // [nbath][2][nt]
-    double *sv2 = sz + 2 * (size_t)nbath * nt;         // [norb][nbath]
-    double *red = sv2 + (size_t)norb * nbath;          // [kRedSlots]
+    double *red = sz + 2 * (size_t)nbath * nt;         // [kRedSlots]
+    double *lv2 = red + kRedSlots;                     // [kMaxOrb][kListMax]
+    double *lv = lv2 + kMaxOrb * kListMax;             // [kMaxOrb][kListMax]
+    int *lk = (int *)(lv + kMaxOrb * kListMax);        // [kMaxOrb][kListMax]
+    int *lcnt = lk + kMaxOrb * kListMax;               // [kMaxOrb]
     const double *eps = xb;                            // eps_k
     const double *V = xb + nbath;                      // V[a*nbath + k]
     const double *ef = xb + nx - norb;                 // ef_a
-    for (int i = tid; i < norb * nbath; i += nt) sv2[i] = V[i] * V[i];
+    if (tid < norb) {
+        int c = 0;
+        for (int k = 0; k < nbath; ++k) {
+            const double v = V[tid * nbath + k];
+            if ((__double_as_longlong(v) << 1) != 0 || !finite_bits(eps[k])) {
+                lk[tid * kListMax + c] = k;
+                lv[tid * kListMax + c] = v;
+                lv2[tid * kListMax + c] = v * v;
+                ++c;
+            }
+        }
+        lcnt[tid] = c;
+    }
     if (grad)
         for (int i = 0; i < nx - norb; ++i) sm[(size_t)i * nt + tid] = 0.0;
     __syncthreads();
     double fsum = 0.0, gef[kMaxOrb];
 #pragma unroll
     for (int a = 0; a < kMaxOrb; ++a) gef[a] = 0.0;
-    for (int n = tid; n < nw; n += nt) {
+    for (int n = n_first + tid; n < nw; n += n_step) {
         const double w = omega[n];
         const double wz = fcmplx ? (double)(float)w : w;
         const double wz2 = wz * wz;
         const double inv_w = rcp_pos(w);
-        // Delta(a, n) - ef_a = sum_k V_ak^2 / z_k, z_k = i wz - eps_k
-        double dre[kMaxOrb], dim[kMaxOrb];
-#pragma unroll
-        for (int a = 0; a < kMaxOrb; ++a) dre[a] = dim[a] = 0.0;
+        // 1/z_k, z_k = i wz - eps_k
         for (int k = 0; k < nbath; ++k) {
             const double e = eps[k];
             const double y = rcp_pos(fma(e, e, wz2));
-            const double izr = -e * y, izi = -wz * y;
-            const bool all = !isfinite(e);
-            if (grad) {
-                sz[(size_t)(2 * k) * nt + tid] = izr;
-                sz[(size_t)(2 * k + 1) * nt + tid] = izi;
-            }
-#pragma unroll
-            for (int a = 0; a < kMaxOrb; ++a) {
-                if (a < norb) {
-                    const double v2 = sv2[a * nbath + k];
-                    if (v2 != 0.0 || all) {
-                        dre[a] = fma(v2, izr, dre[a]);
-                        dim[a] = fma(v2, izi, dim[a]);
-                    }
-                }
-            }
+            sz[(size_t)(2 * k) * nt + tid] = -e * y;
+            sz[(size_t)(2 * k + 1) * nt + tid] = -wz * y;
         }
-        // r = Delta - D_ev; chi2 terms |r|^2 / w_n; weighted residuals for the gradient
+        // r(a, n) = sum_k V_ak^2 / z_k + ef_a - D_ev(a, n); chi2 terms |r|^2 / w_n
         double Rr[kMaxOrb], Ri[kMaxOrb];
 #pragma unroll
         for (int a = 0; a < kMaxOrb; ++a) {
             Rr[a] = Ri[a] = 0.0;
             if (a < norb) {
+                double dre = 0.0, dim = 0.0;
+                for (int j = 0; j < lcnt[a]; ++j) {
+                    const int k = lk[a * kListMax + j];
+                    const double v2 = lv2[a * kListMax + j];
+                    dre = fma(v2, sz[(size_t)(2 * k) * nt + tid], dre);
+                    dim = fma(v2, sz[(size_t)(2 * k + 1) * nt + tid], dim);
+                }
                 const size_t di = 2 * ((size_t)n * norb + a);
-                const double rr = (dre[a] + ef[a]) - dev[di], ri = dim[a] - dev[di + 1];
+                const double rr = (dre + ef[a]) - dev[di], ri = dim - dev[di + 1];
                 fsum = fma(fma(rr, rr, ri * ri), inv_w, fsum);
-                Rr[a] = rr * inv_w;
-                Ri[a] = ri * inv_w;
-                gef[a] += Rr[a];
+                if (grad) {
+                    Rr[a] = rr * inv_w;
+                    Ri[a] = ri * inv_w;
+                    gef[a] += Rr[a];
+                }
             }
         }
         if (grad) {
-            for (int k = 0; k < nbath; ++k) {
-                const double izr = sz[(size_t)(2 * k) * nt + tid], izi = sz[(size_t)(2 * k + 1) * nt + tid];
-                const double sr = fma(izr, izr, -izi * izi), si = 2.0 * izr * izi;   // 1 / z^2
-                const bool all = !isfinite(eps[k]);
-                double ge = 0.0;
+            // Re[conj(r) V^2 / z^2] into the eps_k rows, Re[conj(r) V / z] into
+            // the V_ak rows, both weighted by 1 / w_n
 #pragma unroll
-                for (int a = 0; a < kMaxOrb; ++a) {
-                    if (a < norb) {
-                        const double v2 = sv2[a * nbath + k];
-                        if (v2 != 0.0 || all) {
-                            // Re[conj(r) V^2 / z^2] and Re[conj(r) V / z], weighted by 1 / w_n
-                            ge = fma(v2, fma(Rr[a], sr, Ri[a] * si), ge);
-                            double &gv = sm[(size_t)(nbath + a * nbath + k) * nt + tid];
-                            gv = fma(V[a * nbath + k], fma(Rr[a], izr, Ri[a] * izi), gv);
-                        }
+            for (int a = 0; a < kMaxOrb; ++a) {
+                if (a < norb) {
+                    const double Ri2 = Ri[a] + Ri[a];
+                    for (int j = 0; j < lcnt[a]; ++j) {
+                        const int k = lk[a * kListMax + j];
+                        const double izr = sz[(size_t)(2 * k) * nt + tid], izi = sz[(size_t)(2 * k + 1) * nt + tid];
+                        const double sr = fma(izr, izr, -(izi * izi)), si = izr * izi;   // 1/z^2 = sr + 2i si
+                        double &ge = sm[(size_t)k * nt + tid];
+                        ge = fma(lv2[a * kListMax + j], fma(Rr[a], sr, Ri2 * si), ge);
+                        double &gv = sm[(size_t)(nbath + a * nbath + k) * nt + tid];
+                        gv = fma(lv[a * kListMax + j], fma(Rr[a], izr, Ri[a] * izi), gv);
                     }
                 }
-                sm[(size_t)k * nt + tid] += ge;
             }
         }
     }
@@ -181,8 +213,7 @@ __device__ void chi2_block(const double *__restrict__ xb, int nx, bool grad, int
             if (a < norb) sm[(size_t)(nx - norb + a) * nt + tid] = gef[a];
     }
     const double f = cta_sum(fsum, red);
-    const double fn = (double)(float)(norb * norb * nw);
-    if (tid == 0) *out_f = f / fn;
+    if (tid == 0) out[0] = f;
     if (grad) {
         // rows in four fixed column segments, then the segments in order
         __syncthreads();
@@ -195,14 +226,23 @@ __device__ void chi2_block(const double *__restrict__ xb, int nx, bool grad, int
             red[i] = s;
         }
         __syncthreads();
-        const double gn1 = (double)(float)(norb * norb), gn2 = (double)(float)nw;
-        for (int i = tid; i < nx; i += nt) {
-            const double s = ((red[4 * i] + red[4 * i + 1]) + red[4 * i + 2]) + red[4 * i + 3];
-            const double c = (i >= nbath && i < nx - norb) ? 4.0 : 2.0;   // d/dV_ak carries 2 * 2
-            out_g[i] = c * s / gn1 / gn2;
-        }
+        for (int i = tid; i < nx; i += nt)
+            out[1 + i] = ((red[4 * i] + red[4 * i + 1]) + red[4 * i + 2]) + red[4 * i + 3];
     }
     __syncthreads();
+}
+
+// FUNC = sum / (norb^2 nw) (func.f90:40-43) from out[0] of chi2_sums over
+// every w_n; dfunc_i from out[1 + i]: 2 sum / norb^2 / nw, and 4 sum /
+// norb^2 / nw for the V_ak (func.f90:128-140)
+__device__ __forceinline__ double chi2_scale_f(double s, int norb, int nw)
+{
+    return s / (double)(float)(norb * norb * nw);
+}
+__device__ __forceinline__ double chi2_scale_g(double s, int i, int nx, int norb, int nbath, int nw)
+{
+    const double c = (i >= nbath && i < nx - norb) ? 4.0 : 2.0;
+    return c * s / (double)(float)(norb * norb) / (double)(float)nw;
 }
 
 // x: [nreq][nx]; dev: Fortran (norb, nw) interleaved complex; f: [nreq];
@@ -212,11 +252,15 @@ k_chi2(const double *__restrict__ x, int nx, const int *__restrict__ want_grad, 
        int nbath, const double *__restrict__ omega, const double *__restrict__ dev, int fcmplx,
        double *__restrict__ f, double *__restrict__ g)
 {
-    extern __shared__ double sm[];          // chi2_smem_doubles(nx, nbath, norb, kFitThreads)
+    extern __shared__ double sm[];          // chi2_smem_bytes(nx, nbath, kFitThreads)
+    __shared__ double sums[kMaxX + 1];
     const int b = blockIdx.x;
     const bool grad = g != nullptr && (want_grad ? want_grad[b] != 0 : true);
-    chi2_block(x + (size_t)b * nx, nx, grad, nw, norb, nbath, omega, dev, fcmplx, sm, f + b,
-               grad ? g + (size_t)b * nx : nullptr);
+    chi2_sums(x + (size_t)b * nx, nx, grad, nw, 0, blockDim.x, norb, nbath, omega, dev, fcmplx, sm, sums);
+    if (threadIdx.x == 0) f[b] = chi2_scale_f(sums[0], norb, nw);
+    if (grad)
+        for (int i = threadIdx.x; i < nx; i += blockDim.x)
+            g[(size_t)b * nx + i] = chi2_scale_g(sums[1 + i], i, nx, norb, nbath, nw);
 }
 
 // calc_dev (ed_green.F90:260-273)
@@ -238,10 +282,10 @@ __global__ void k_calc_dev(int norb, int nbath, int nw, const double *omega, con
     dev[2 * (size_t)t + 1] = d.y;
 }
 
-// dynamic shared memory of k_chi2 / k_fit for these dimensions (128 threads)
-static int chi2_smem(mo_ed_ctx *ctx, const void *kernel, int nx, int nbath, int norb, size_t *bytes)
+// dynamic shared memory of k_chi2 / k_fit for these dimensions and nt threads
+static int chi2_smem(mo_ed_ctx *ctx, const void *kernel, int nx, int nbath, int nt, size_t *bytes)
 {
-    *bytes = sizeof(double) * chi2_smem_doubles(nx, nbath, norb, kFitThreads);
+    *bytes = chi2_smem_bytes(nx, nbath, nt);
     MOED_CUDA(ctx, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*bytes));
     return MO_ED_OK;
 }
@@ -253,7 +297,7 @@ int chi2_grad_dev(mo_ed_ctx *ctx, int nbatch, const double *x, int nwloc, int ns
     (void)ns;
     if (nbatch <= 0) return MO_ED_OK;
     size_t smem;
-    if (int rc = chi2_smem(ctx, (const void *)k_chi2, nxsize, nbath, norb, &smem)) return rc;
+    if (int rc = chi2_smem(ctx, (const void *)k_chi2, nxsize, nbath, kFitThreads, &smem)) return rc;
     k_chi2<<<nbatch, kFitThreads, smem, ctx->stream>>>(x, nxsize, nullptr, nwloc, norb, nbath, omega, dev,
                                                        ctx->opt.fortran_cmplx, f, want_grad ? g : nullptr);
     MOED_CHECK_LAUNCH(ctx);
@@ -306,7 +350,7 @@ struct Evaluator {
         MOED_CUDA(ctx, cudaMemcpyAsync(dx.p, x, sizeof(double) * nreq * nx, cudaMemcpyHostToDevice, ctx->stream));
         MOED_CUDA(ctx, cudaMemcpyAsync(dw.p, want, sizeof(int) * nreq, cudaMemcpyHostToDevice, ctx->stream));
         size_t smem;
-        if (int rc = chi2_smem(ctx, (const void *)k_chi2, nx, P->nbath, P->norb, &smem)) return rc;
+        if (int rc = chi2_smem(ctx, (const void *)k_chi2, nx, P->nbath, kFitThreads, &smem)) return rc;
         k_chi2<<<nreq, kFitThreads, smem, ctx->stream>>>((const double *)dx.p, nx, (const int *)dw.p, P->nwloc,
                                                          P->norb, P->nbath, (const double *)P->omega.p,
                                                          (const double *)P->dev.p, ctx->opt.fortran_cmplx,
@@ -500,23 +544,57 @@ struct Frprmn {
 };
 
 // ---------------------------------------------------------------------------
-// fits on the device: one CTA of kFitCta threads per fit runs frprmn to the
-// end.  Every thread executes the same frprmn steps on its own copy of the
-// scalars and vectors; each FUNC / dfunc is evaluated by the whole CTA
-// (chi2_block) and broadcast through shared memory, so all threads follow the
-// same path.  No host round trip per evaluation.
+// fits on the device: a cluster of C CTAs (C = 1 .. 8) runs one fit to the
+// end.  Every thread of every CTA executes the same frprmn steps on its own
+// copy of the scalars and vectors.  Each FUNC / dfunc is split over the
+// cluster by w_n: CTA r of the cluster sums the terms of the w_n with
+// n = r nt + t + k C nt (chi2_sums), writes its sums into its slot, and after
+// one cluster barrier every CTA adds the C slots (read through distributed
+// shared memory) in rank order.  All CTAs so see bit-identical values and
+// take the same path, one cluster barrier per evaluation.  The slots are
+// double-buffered: a CTA rewrites a slot two evaluations later, after the
+// next barrier, which no CTA passes before every CTA has read it.  No host
+// round trip per evaluation.
 // ---------------------------------------------------------------------------
-constexpr int kFitCta = kFitThreads;   // threads per fit: all four SM sub-partitions' FP64 units
+// One fit on one SM is bound by the latency of its FP64 dependency chains
+// (GB300 has about 2 FP64 lanes per SM and clock), so a fit over nw >= 256
+// w_n is spread over a cluster of up to kFitMaxCluster SMs of kFitThreads
+// threads, about one w_n per thread.  Smaller grids run on one CTA of
+// kFitCta threads where the partial sums fit in shared memory.
+constexpr int kFitCta = 256;
+constexpr int kFitMaxCluster = 8;
+constexpr size_t kFitSmemMax = 220 * 1024;
+
+namespace cg = cooperative_groups;
 
 struct DevChi2 {
     int nx, nw, norb, nbath, fcmplx;
     const double *omega, *dev;
-    double *sm, *sx, *sres;
+    double *sm, *sx, *sres, *slots;   // slots: [2][kMaxX + 1] of this CTA
+    int rank, ncta, par;
     // chi^2 (and the gradient into g) at the point sx, already in shared memory
     __device__ double eval_sx(double *g)
     {
         __syncthreads();
-        chi2_block(sx, nx, g != nullptr, nw, norb, nbath, omega, dev, fcmplx, sm, sres, sres + 1);
+        const int nt = blockDim.x;
+        const bool grad = g != nullptr;
+        double *mine = slots + par * (kMaxX + 1);
+        chi2_sums(sx, nx, grad, nw, rank * nt, ncta * nt, norb, nbath, omega, dev, fcmplx, sm, mine);
+        const int nout = grad ? nx + 1 : 1;
+        if (ncta == 1) {
+            for (int i = threadIdx.x; i < nout; i += nt)
+                sres[i] = i ? chi2_scale_g(mine[i], i - 1, nx, norb, nbath, nw) : chi2_scale_f(mine[0], norb, nw);
+        } else {
+            cg::cluster_group cl = cg::this_cluster();
+            cl.sync();
+            for (int i = threadIdx.x; i < nout; i += nt) {
+                double s = 0.0;
+                for (int r = 0; r < ncta; ++r) s += cl.map_shared_rank(mine, r)[i];
+                sres[i] = i ? chi2_scale_g(s, i - 1, nx, norb, nbath, nw) : chi2_scale_f(s, norb, nw);
+            }
+        }
+        par ^= 1;
+        __syncthreads();
         if (g)
             for (int j = 0; j < nx; ++j) g[j] = sres[1 + j];
         const double f = sres[0];
@@ -545,26 +623,30 @@ struct DevDFunc {
     __device__ void operator()(const double *x, double *g) const { c->eval(x, g); }
 };
 
+// grid: nbatch clusters of ncta CTAs (ncta = 1: a plain launch); fit b is
+// cluster b, and CTA rank 0 writes its results
 __global__ void __launch_bounds__(kFitCta, 1)
 k_fit(double *__restrict__ X, int nx, int nw, int norb, int nbath, const double *__restrict__ omega,
-      const double *__restrict__ dev, int fcmplx, double ftol, double *fret, int *iter, int *status)
+      const double *__restrict__ dev, int fcmplx, double ftol, int ncta, double *fret, int *iter, int *status)
 {
-    extern __shared__ double sm[];   // chi2_smem_doubles(nx, nbath, norb, kFitCta)
-    __shared__ double sx[kMaxX], sres[kMaxX + 1];
-    const int b = blockIdx.x;
-    DevChi2 c{nx, nw, norb, nbath, fcmplx, omega, dev, sm, sx, sres};
+    extern __shared__ double sm[];   // chi2_smem_bytes(nx, nbath, blockDim.x)
+    __shared__ double sx[kMaxX], sres[kMaxX + 1], slots[2 * (kMaxX + 1)];
+    const int b = blockIdx.x / ncta, rank = blockIdx.x % ncta;
+    DevChi2 c{nx, nw, norb, nbath, fcmplx, omega, dev, sm, sx, sres, slots, rank, ncta, 0};
     Frprmn<DevFunc, DevDFunc> fr{DevFunc{&c}, DevDFunc{&c}, nx};
     double p[kMaxX];
     for (int j = 0; j < nx; ++j) p[j] = X[(size_t)b * nx + j];
     int it = 0;
     double f = 0.0;
     const int rc = fr.run(p, ftol, it, f);
-    if (threadIdx.x == 0) {
+    if (rank == 0 && threadIdx.x == 0) {
         for (int j = 0; j < nx; ++j) X[(size_t)b * nx + j] = p[j];
         fret[b] = f;
         iter[b] = it;
         status[b] = rc;
     }
+    // no CTA leaves while another may still read its slots
+    if (ncta > 1) cg::this_cluster().sync();
 }
 
 // nbatch fits of host parameter sets x[nbatch][nxsize], in place
@@ -578,12 +660,29 @@ static int fit_on_device(mo_ed_ctx *ctx, FitProblem &P, int nbatch, double *x, d
     if (int rc = dev_alloc(ctx, di, sizeof(int) * nbatch)) return rc;
     if (int rc = dev_alloc(ctx, ds, sizeof(int) * nbatch)) return rc;
     MOED_CUDA(ctx, cudaMemcpyAsync(dx.p, x, sizeof(double) * (size_t)nbatch * nx, cudaMemcpyHostToDevice, ctx->stream));
+    // a cluster of ncta CTAs of kFitThreads per fit for nw >= 256 (about one
+    // w_n per thread); else one CTA of kFitCta threads where the partial sums
+    // fit in shared memory, or of kFitThreads
+    int ncta = 1, nt = kFitThreads;
+    while (ncta < kFitMaxCluster && P.nwloc >= 2 * ncta * kFitThreads) ncta *= 2;
+    if (P.nwloc < 2 * kFitThreads && chi2_smem_bytes(nx, P.nbath, kFitCta) <= kFitSmemMax) nt = kFitCta;
     size_t smem;
-    if (int rc = chi2_smem(ctx, (const void *)k_fit, nx, P.nbath, P.norb, &smem)) return rc;
-    k_fit<<<nbatch, kFitCta, smem, ctx->stream>>>((double *)dx.p, nx, P.nwloc, P.norb, P.nbath,
-                                                (const double *)P.omega.p, (const double *)P.dev.p,
-                                                ctx->opt.fortran_cmplx, ftol, (double *)df.p, (int *)di.p,
-                                                (int *)ds.p);
+    if (int rc = chi2_smem(ctx, (const void *)k_fit, nx, P.nbath, nt, &smem)) return rc;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    cfg.gridDim = dim3((unsigned)(nbatch * ncta));
+    cfg.blockDim = dim3((unsigned)nt);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = ctx->stream;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)ncta;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    MOED_CUDA(ctx, cudaLaunchKernelEx(&cfg, k_fit, (double *)dx.p, nx, P.nwloc, P.norb, P.nbath,
+                                      (const double *)P.omega.p, (const double *)P.dev.p, ctx->opt.fortran_cmplx,
+                                      ftol, ncta, (double *)df.p, (int *)di.p, (int *)ds.p));
     MOED_CHECK_LAUNCH(ctx);
     MOED_CUDA(ctx, cudaMemcpyAsync(x, dx.p, sizeof(double) * (size_t)nbatch * nx, cudaMemcpyDeviceToHost, ctx->stream));
     MOED_CUDA(ctx, cudaMemcpyAsync(fret, df.p, sizeof(double) * nbatch, cudaMemcpyDeviceToHost, ctx->stream));

@@ -208,7 +208,11 @@ __global__ void k_lz_update(const __grid_constant__ LzBatchDev b, int j)
         const T *uc = (const T *)R.u[(j - 1) % 3];
         const T *up = (const T *)R.u[(j + 1) % 3];   // (j-2) mod 3
         T *un = (T *)R.u[j % 3];
+        // ||u_j||^2: partials of 4 squares in T, added to the FP64 sum every
+        // 8 iterations (per-element FP64 work would bound the kernel on GB300)
         double acc = 0.0;
+        T sacc = T(0);
+        int cnt = 0;
         for (long long i = i0 + 4 * threadIdx.x; i < i1; i += 4 * blockDim.x) {
             T wv[4], cv[4], pv[4], v[4];
             vload4(w + i, wv);
@@ -219,12 +223,17 @@ __global__ void k_lz_update(const __grid_constant__ LzBatchDev b, int j)
                 pv[0] = pv[1] = pv[2] = pv[3] = T(0);
             }
 #pragma unroll
-            for (int e = 0; e < 4; ++e) {
+            for (int e = 0; e < 4; ++e)
                 v[e] = (j >= 2) ? s * (wv[e] - a * cv[e]) - c * pv[e] : s * (wv[e] - a * cv[e]);
-                acc += (double)(v[e] * v[e]);
+            sacc += (v[0] * v[0] + v[1] * v[1]) + (v[2] * v[2] + v[3] * v[3]);
+            if (++cnt == 8) {
+                acc += (double)sacc;
+                sacc = T(0);
+                cnt = 0;
             }
             vstore4(un + i, v);
         }
+        acc += (double)sacc;
         double t = block_sum(acc, sred);
         if (threadIdx.x == 0) R.upd_part[it] = t;
     }
@@ -707,7 +716,10 @@ k_multiaxpy(const __grid_constant__ VPtrs<T> V, int nv, const double *__restrict
     __shared__ double sred[32];
     for (int l = threadIdx.x; l < nv + 4; l += blockDim.x) sh[l] = l < nv ? (T)h[l] : T(0);
     __syncthreads();
+    // ||w||^2: partials of 4 squares in T, added in FP64 every 8 iterations
     double acc = 0.0;
+    T sacc = T(0);
+    int cnt = 0;
     for (long long i = 4 * (blockIdx.x * (long long)blockDim.x + threadIdx.x); i < D;
          i += 4 * (long long)gridDim.x * blockDim.x) {
         T s[4] = {T(0), T(0), T(0), T(0)};
@@ -726,12 +738,16 @@ k_multiaxpy(const __grid_constant__ VPtrs<T> V, int nv, const double *__restrict
         T x[4];
         vload4(w + i, x);
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            x[e] -= s[e];
-            acc += (double)(x[e] * x[e]);
+        for (int e = 0; e < 4; ++e) x[e] -= s[e];
+        sacc += (x[0] * x[0] + x[1] * x[1]) + (x[2] * x[2] + x[3] * x[3]);
+        if (++cnt == 8) {
+            acc += (double)sacc;
+            sacc = T(0);
+            cnt = 0;
         }
         vstore4(w + i, x);
     }
+    acc += (double)sacc;
     if (norm_part) {
         double t = block_sum(acc, sred);
         if (threadIdx.x == 0) norm_part[blockIdx.x] = t;
@@ -814,23 +830,34 @@ k_rotate(const __grid_constant__ VPtrs<T> V, int nv, const double *__restrict__ 
         sy[idx] = (c < nc && l < nv) ? (T)Y[(size_t)(c0 + c) * ldy + l] : T(0);
     }
     __syncthreads();
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < D;
-         i += (long long)gridDim.x * blockDim.x) {
-        T acc[KC];
+    // 4 consecutive elements per thread (16-byte accesses; D is a multiple
+    // of 32 and the vectors are 256-byte aligned)
+    for (long long i = 4 * (blockIdx.x * (long long)blockDim.x + threadIdx.x); i < D;
+         i += 4 * (long long)gridDim.x * blockDim.x) {
+        T acc[KC][4];
 #pragma unroll
-        for (int c = 0; c < KC; ++c) acc[c] = T(0);
+        for (int c = 0; c < KC; ++c)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[c][e] = T(0);
         for (int l = 0; l < nv; l += 4) {
-            T v[4];
+            T v[4][4];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) v[q] = (l + q < nv) ? V.p[l + q][i] : T(0);
+            for (int q = 0; q < 4; ++q) {
+                if (l + q < nv) vload4(V.p[l + q] + i, v[q]);
+                else v[q][0] = v[q][1] = v[q][2] = v[q][3] = T(0);
+            }
 #pragma unroll
             for (int q = 0; q < 4; ++q)
 #pragma unroll
-                for (int c = 0; c < KC; ++c) acc[c] += v[q] * sy[(l + q) * KC + c];
+                for (int c = 0; c < KC; ++c) {
+                    const T y = sy[(l + q) * KC + c];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) acc[c][e] += v[q][e] * y;
+                }
         }
 #pragma unroll
         for (int c = 0; c < KC; ++c)
-            if (c < nc) const_cast<T *>(X.p[c])[i] = acc[c];
+            if (c < nc) vstore4(const_cast<T *>(X.p[c]) + i, acc[c]);
     }
 }
 

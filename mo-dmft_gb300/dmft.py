@@ -18,17 +18,24 @@ import time
 
 import numpy as np
 
-from .ed import EDSolver, ev_to_x, matsubara, x_to_ev
+from .ed import EDError, EDSolver, ev_to_x, matsubara, x_to_ev
 
 
 def dmft_loop(solver: EDSolver, inp: dict, nloop: int | None = None, precision: str = "fp32",
-              green_fp64: bool = False, callback=None, trace: list | None = None) -> dict:
+              green_fp64: bool = False, callback=None, trace: list | None = None, fit_starts: int = 1) -> dict:
     """Run the DMFT loop of main.f90 with the parameters of an FDF input.
 
     solver: an open EDSolver (its options, model, sectors and omega are set here).
     inp: configs.read_fdf output.  nloop overrides DMFT.MaxIterations.
     callback(iteration, record) is called after every iteration with its record
     (scf_diff, chi^2, CG iterations, occupations, nev_calc, seconds).
+    fit_starts: 1 (default) is the reference's single minimization from the
+    current bath, which STOPs the run (EDError, MO_ED_ERR_FIT) when frprmn
+    exceeds its iteration limit.  fit_starts > 1 fits the current bath and
+    fit_starts - 1 seeded perturbations of it (every parameter scaled by
+    1 + 0.05 N(0, 1), so zero couplings stay zero) in one batched device fit
+    (mo_ed_fit_batch) and takes the lowest chi^2 of the fits that end within
+    frprmn's limits; the run STOPs only when none does.
     trace: a list that receives, per iteration, the iteration's starting bath
     (ek, vk, ef), the D_ev it starts from, Gr, Gksum, the new D_ev of
     delta_new and the fitted parameters x (copies).
@@ -69,7 +76,18 @@ def dmft_loop(solver: EDSolver, inp: dict, nloop: int | None = None, precision: 
         D_ev, Gksum = solver.delta_new(Gr, D_ev, mu)
         nocc = solver.n_from_gksum(Gksum, beta)
         x = ev_to_x(ek, vk, ef, nsite, nbath)
-        x, fret, it = solver.minimization(x, nw, nsite, nx, omega, D_ev, nbath, norb)
+        if fit_starts <= 1:
+            x, fret, it = solver.minimization(x, nw, nsite, nx, omega, D_ev, nbath, norb)
+        else:
+            rng = np.random.default_rng(1000 + iloop)
+            X0 = np.repeat(x[None, :], fit_starts, axis=0)
+            X0[1:] *= 1.0 + 0.05 * rng.standard_normal((fit_starts - 1, nx))
+            X, F, IT, ST = solver.fit_batch(X0, omega, D_ev, nbath, norb)
+            ok = np.flatnonzero(ST == 0)
+            if ok.size == 0:
+                raise EDError(6, "frprmn: iteration limit exceeded from every start")
+            k = ok[np.argmin(F[ok])]
+            x, fret, it = X[k], float(F[k]), int(IT[k])
         if trace is not None:
             step.update(Gr=Gr.copy(), Gksum=np.array(Gksum), D_ev=D_ev.copy(), x=np.array(x))
             trace.append(step)

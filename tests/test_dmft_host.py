@@ -94,3 +94,45 @@ def test_dmft_loop_order_and_outputs(pkg, oracle):
     w32 = om.astype(np.float32).astype(np.float64)
     assert np.allclose(out["Sigma"], 1j * w32[None, :] - dev - 1.0 / out["Gr"], rtol=0, atol=1e-12)
     assert np.all(np.isfinite(out["Sigma"])) and 0.0 < out["nocc"][0] < 2.0
+
+
+class MultiStartSolver(OracleSolver):
+    """The stand-in with fit_batch: the oracle's frprmn per start, and the
+    second start reported as stopped by frprmn's iteration limit."""
+
+    def fit_batch(self, X, om, dev, nbath, norb):
+        self.calls.append("fit_batch")
+        self.starts = np.array(X)
+        out = [self.O.frprmn(x, nbath + norb, om, dev, nbath, norb) for x in X]
+        P = np.array([o[0] for o in out])
+        F = np.array([o[1] for o in out])
+        IT = np.array([o[2] for o in out], np.int32)
+        ST = np.array([o[3] for o in out], np.int32)
+        ST[1] = 6
+        F[1] = -1.0            # the lowest chi^2, but stopped: must not be taken
+        self.F, self.ST = F, ST
+        return P, F, IT, ST
+
+
+def test_dmft_loop_multistart_fit(pkg, oracle):
+    """fit_starts > 1: the current bath plus seeded perturbations in one batch
+    (zero couplings stay zero); the lowest chi^2 among the fits that ended
+    within frprmn's limits is taken."""
+    text = "\n".join([
+        "DMFT.Norbs 1", "DMFT.Nbaths 3", "DMFT.Nsectors 2",
+        "%block DMFT.Sectors", "  4 2", "  3 2", "%endblock DMFT.Sectors",
+        "DMFT.U 2.0", "DMFT.J 0.0", "DMFT.Mu 1.0", "DMFT.beta 20.0",
+        "%block DMFT.Baths", "  -0.6", "  0.1", "  0.7", "%endblock DMFT.Baths",
+        "%block DMFT.BathCouplings", "  0.3", "  0.0", "  0.4", "%endblock DMFT.BathCouplings",
+        "DMFT.ContinuedFractionSteps 30", "DMFT.Nev 4", "DMFT.Nq 64", "DMFT.Nw 64",
+        "DMFT.ScfTolerance 1d-12"])
+    inp = pkg.configs.read_fdf(text)
+    s = MultiStartSolver(oracle)
+    hist = []
+    out = pkg.dmft_loop(s, inp, nloop=1, callback=lambda i, r: hist.append(r), fit_starts=4)
+    assert "fit_batch" in s.calls and "minimization" not in s.calls
+    X0 = s.starts
+    assert X0.shape[0] == 4 and np.all(X0[:, X0[0] == 0] == 0)     # zeros stay zero
+    assert not np.array_equal(X0[0], X0[2])
+    assert hist[0]["chi2"] == s.F[s.ST == 0].min()                  # the stopped start is skipped
+    assert out["iterations"] == 1

@@ -120,3 +120,48 @@ def test_c4_hv_rows_vs_oracle(solver, oracle, pkg, precision, tol):
         worst = max(worst, rel(y[r0:r0 + 10000], yo[r0:r0 + 10000]))
     print(precision, "max rel error over the sampled rows", worst)
     assert worst < tol
+
+
+@pytest.fixture(scope="module")
+def c5gold():
+    return np.load(os.path.join(HERE, "golden", "c5_oracle.npz"))
+
+
+def test_c5_fits_vs_oracle(solver, pkg, c5gold):
+    """The 256 C5 bath fits (3 orbitals x 4 bath levels, 512 w_n) on the
+    device against the oracle's frprmn from the same starts
+    (tests/golden/c5_oracle.npz, made by tests/golden/make_c5_golden.py;
+    frprmn.f90 driven as func.f90:144-163 drives it).
+
+    frprmn stops on a relative change of chi^2 below FTOL = 1e-7 between CG
+    iterations, so two FP64 codes that sum in different orders follow the
+    same trajectory only as long as their roundings do not steer a line
+    search apart; after that they stop at different points of the same flat
+    valley or in different minima.  Measured on GB300 the parity shows as:
+      * where both end at the same point (final parameters within 1e-4 of
+        each other; 5 to 7 starts with the kernels measured), chi^2 agrees
+        to 1e-6 (measured: 2e-8);
+      * the reference's own limits (itmax 20000, brent ITMAX 100) stop
+        nearly the same starts (measured: 242 of 256 agree);
+      * where both converge, neither is systematically lower (device lower
+        on 48 %), the median relative chi^2 difference is 7e-4 and the
+        median CG iteration counts agree to 20 %."""
+    P = pkg.configs.fit_config(seed=4, nbatch=256)
+    norb, nbath = P["norb"], P["nbath"]
+    solver.set_options(precision="fp64")
+    X, fret, it, st = solver.fit_batch(P["X0"], P["omega"], P["dev"], nbath, norb)
+    fo, io, so, Xo = c5gold["fret"], c5gold["iter"], c5gold["status"], c5gold["X"]
+    both = (st == 0) & (so == 0)
+    d = np.abs(fret - fo) / np.abs(fo)
+    dx = np.abs(X - Xo).max(axis=1)
+    same = both & (dx < 1e-4)
+    print(f"status agree {int((((st == 0) == (so == 0))).sum())}/256, both converged {int(both.sum())}, "
+          f"same end point {int(same.sum())} (max rel dchi2 {d[same].max() if same.any() else 0:.2e}), "
+          f"median rel dchi2 {np.median(d[both]):.2e}, device lower on {int((fret[both] < fo[both]).sum())}, "
+          f"median CG iterations {np.median(it[both]):.0f} vs {np.median(io[both]):.0f}")
+    assert ((st == 0) == (so == 0)).mean() >= 0.9
+    assert same.sum() >= 3
+    assert d[same].max() < 1e-6
+    assert np.median(d[both]) < 1e-2
+    assert 0.3 <= (fret[both] < fo[both]).mean() <= 0.7
+    assert 0.8 <= np.median(it[both]) / np.median(io[both]) <= 1.25
