@@ -40,6 +40,9 @@
 // adds the other terms.  The autotuner picks among all of them per
 // (precision, sector).
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "internal.h"
 
@@ -1245,6 +1248,40 @@ void hv_fill_job(const mo_ed_ctx *ctx, const Sector &s, int R, const void *x, vo
 template void hv_fill_job<float>(const mo_ed_ctx *, const Sector &, int, const void *, void *, HvJobT<float> &);
 template void hv_fill_job<double>(const mo_ed_ctx *, const Sector &, int, const void *, void *, HvJobT<double> &);
 
+// Makes kernel k launchable with smem bytes of dynamic shared memory (and the
+// full carveout) and returns its resident CTAs per SM at nt threads.  The
+// runtime calls cost more than the launch of a small sector's H*v, so they
+// are made once per (device, kernel): the shared-memory limit only ever
+// rises, and the occupancy is kept per (device, kernel, size, threads).
+// Process-wide, under a lock, so contexts on one device agree.
+static std::mutex g_kfit_mu;
+static std::map<std::pair<int, const void *>, size_t> g_kfit_smem;
+static std::map<std::tuple<int, const void *, size_t, int>, int> g_kfit_occ;
+
+template <typename K>
+static int kernel_fit(mo_ed_ctx *ctx, K k, int nt, size_t smem, int *per_sm)
+{
+    std::lock_guard<std::mutex> lock(g_kfit_mu);
+    const void *kp = (const void *)k;
+    auto ins = g_kfit_smem.emplace(std::make_pair(ctx->device, kp), (size_t)0);
+    size_t &set = ins.first->second;
+    if (ins.second)
+        MOED_CUDA(ctx, cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    if (smem > set) {
+        MOED_CUDA(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        set = smem;
+    }
+    const auto key = std::make_tuple(ctx->device, kp, smem, nt);
+    auto it = g_kfit_occ.find(key);
+    if (it == g_kfit_occ.end()) {
+        int n = 0;
+        MOED_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, nt, smem));
+        it = g_kfit_occ.emplace(key, n).first;
+    }
+    *per_sm = it->second;
+    return MO_ED_OK;
+}
+
 template <typename TX, typename TA, typename TY, int R, int NT, int MINB>
 static int launch_batch(mo_ed_ctx *ctx, const HvBatch<TA> &b)
 {
@@ -1256,10 +1293,8 @@ static int launch_batch(mo_ed_ctx *ctx, const HvBatch<TA> &b)
     }
     const size_t smem = dyn_smem_bytes<TX, TA, R>(ldmax, ctx->mdl);
     auto kern = k_hv<TX, TA, TY, R, NT, MINB>;
-    MOED_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    MOED_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     int per_sm = 0;
-    MOED_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem));
+    if (int rc = kernel_fit(ctx, kern, NT, smem, &per_sm)) return rc;
     if (per_sm < 1) return fail(ctx, MO_ED_ERR_ARG, "sector rows too long for the shared-memory stage");
     const int grid = std::min(b.total_items, ctx->num_sms * per_sm);
     kern<<<grid, NT, smem, ctx->stream>>>(b, ctx->d_mdl);
@@ -1280,10 +1315,8 @@ static int launch_batch_async(mo_ed_ctx *ctx, const HvBatch<TA> &b)
     const DescGeom g = desc_geom<TA, R>(ctx->mdl.ncpl, ctx->mdl);
     const size_t smem = dyn_smem_bytes_async<TX, TA, R>(ldmax, ctx->mdl, g);
     auto kern = k_hv_async<TX, TA, TY, R, NT, MINB, SPLIT>;
-    MOED_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    MOED_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     int per_sm = 0;
-    MOED_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem));
+    if (int rc = kernel_fit(ctx, kern, NT, smem, &per_sm)) return rc;
     if (per_sm < 1) return fail(ctx, MO_ED_ERR_ARG, "sector rows too long for the shared-memory stage");
     const int grid = std::min(b.total_items, ctx->num_sms * per_sm);
     kern<<<grid, NT, smem, ctx->stream>>>(b, ctx->d_mdl, g);
@@ -1342,10 +1375,8 @@ static int launch_batch_split(mo_ed_ctx *ctx, const HvBatch<TA> &b0)
     }
     if (smem > kDownSmemMax) return fail(ctx, MO_ED_ERR_ARG, "down-spin blocks too large for the split H*v");
     auto kd = k_hv_down<TX, TA, TY, kDownNT, WB>;
-    MOED_CUDA(ctx, cudaFuncSetAttribute(kd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    MOED_CUDA(ctx, cudaFuncSetAttribute(kd, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     int per_sm = 0;
-    MOED_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kd, kDownNT, smem));
+    if (int rc = kernel_fit(ctx, kd, kDownNT, smem, &per_sm)) return rc;
     if (per_sm < 1) return fail(ctx, MO_ED_ERR_ARG, "down-spin blocks too large for the split H*v");
     const int grid = std::min(tiles, ctx->num_sms * per_sm);
     kd<<<grid, kDownNT, smem, ctx->stream>>>(b, tiles, L, maxrows, dbuf);

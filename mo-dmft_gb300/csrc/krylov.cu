@@ -891,6 +891,25 @@ __global__ void k_jacobi(const double *__restrict__ Hp, int ldh, int m, int kk,
         V[idx] = (i == j) ? 1.0 : 0.0;
     }
     __syncthreads();
+    // Off-diagonal entries below the rounding level of the matrix, 4e-16
+    // ||A||_F, are left alone: rotations keep regenerating entries of that
+    // size, so a smaller threshold never lets a sweep rotate nothing.  An
+    // entry delta left there moves the eigenvalues by delta^2 / gap.
+    __shared__ double s_red[32], s_thr;
+    {
+        double acc = 0.0;
+        for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) acc += A[idx] * A[idx];
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_red[w];
+            s_thr = 4e-16 * sqrt(t);
+        }
+        __syncthreads();
+    }
+    const double thr = s_thr;
     __shared__ int s_rot;
     for (int sweep = 0; sweep < max_sweeps; ++sweep) {
         // threshold Jacobi: a sweep that rotates nothing ends the iteration
@@ -909,7 +928,7 @@ __global__ void k_jacobi(const double *__restrict__ Hp, int ldh, int m, int kk,
                 const double apq = A[(size_t)q * n + p];
                 const double app = A[(size_t)p * n + p], aqq = A[(size_t)q * n + q];
                 double c = 1.0, s = 0.0;
-                if (fabs(apq) > 1e-17 * sqrt(fabs(app) * fabs(aqq)) + 1e-300) {
+                if (fabs(apq) > fmax(1e-17 * sqrt(fabs(app) * fabs(aqq)), thr) + 1e-300) {
                     atomicAdd(&s_rot, 1);
                     const double tau = (aqq - app) / (2.0 * apq);
                     const double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
