@@ -19,6 +19,7 @@
 #include <cstring>
 
 #include "krylov.cuh"
+#include "symeig.h"
 
 namespace moed {
 
@@ -28,6 +29,11 @@ constexpr int kVecThreads = 256;
 // reductions
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double warp_sum(double v)
+{
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    return v;
+}
+__device__ __forceinline__ float warp_sum(float v)
 {
     for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
     return v;
@@ -622,6 +628,7 @@ k_multidot(const __grid_constant__ VPtrs<T> V, int nv, const T *__restrict__ w, 
             sacc[l] = T(0);
         }
         int cnt = 0;
+        bool flushed = false;
         for (long long i = 4 * (blockIdx.x * (long long)blockDim.x + threadIdx.x); i < D;
              i += 4 * (long long)gridDim.x * blockDim.x) {
             T x[4];
@@ -641,12 +648,21 @@ k_multidot(const __grid_constant__ VPtrs<T> V, int nv, const T *__restrict__ w, 
                     sacc[l] = T(0);
                 }
                 cnt = 0;
+                flushed = true;
             }
         }
+        // The warp's partials of the np live columns.  When no lane has moved
+        // a partial to FP64 yet (at most 8 iterations per thread: small
+        // sectors), an FP32 vector's partials are summed in FP32 and widened
+        // once: FP64 shuffle trees of every column would bound the kernel on
+        // GB300's FP64 rate.
+        const bool wide = sizeof(T) == 8 || __any_sync(0xffffffffu, flushed);
 #pragma unroll
         for (int l = 0; l < kDotPass; ++l) {
-            const double v = warp_sum(acc[l] + (double)sacc[l]);
-            if (lane == 0) sred[wid][l] = v;
+            if (l < np) {
+                const double v = wide ? warp_sum(acc[l] + (double)sacc[l]) : (double)warp_sum(sacc[l]);
+                if (lane == 0) sred[wid][l] = v;
+            }
         }
         __syncthreads();
         for (int l = threadIdx.x; l < np; l += blockDim.x) {
@@ -1133,18 +1149,14 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
     std::vector<DevBuf> &sm = ctx->trl_small;   // projected-problem workspace, kept in the context
     if (sm.size() < 12) sm.resize(12);
     DevBuf &dHp = sm[0], &dh1 = sm[1], &dh2 = sm[2], &dpart = sm[3], &dnorm = sm[4], &dbeta = sm[5];
-    DevBuf &dA = sm[6], &dVj = sm[7], &devals = sm[8], &devecs = sm[9], &dtheta = sm[10], &dsc = sm[11];
+    DevBuf &devecs = sm[9], &dsc = sm[11];
     if (int rc = ensure(ctx, dHp, sizeof(double) * (size_t)n2 * n2)) return rc;
     if (int rc = ensure(ctx, dh1, sizeof(double) * n2)) return rc;
     if (int rc = ensure(ctx, dh2, sizeof(double) * n2)) return rc;
     if (int rc = ensure(ctx, dpart, sizeof(double) * (size_t)n2 * ctx->num_sms * 4)) return rc;
     if (int rc = ensure(ctx, dnorm, sizeof(double) * G)) return rc;
     if (int rc = ensure(ctx, dbeta, sizeof(double) * 2)) return rc;
-    if (int rc = ensure(ctx, dA, sizeof(double) * (size_t)n2 * n2)) return rc;
-    if (int rc = ensure(ctx, dVj, sizeof(double) * (size_t)n2 * n2)) return rc;
-    if (int rc = ensure(ctx, devals, sizeof(double) * n2)) return rc;
     if (int rc = ensure(ctx, devecs, sizeof(double) * (size_t)n2 * n2)) return rc;
-    if (int rc = ensure(ctx, dtheta, sizeof(double) * n2)) return rc;
     if (int rc = ensure(ctx, dsc, sizeof(double) * 4)) return rc;
     MOED_CUDA(ctx, cudaMemsetAsync(dHp.p, 0, dHp.bytes, ctx->stream));
     double *Hp = (double *)dHp.p;
@@ -1207,8 +1219,8 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
             }
         }
         bool broke = false;
+        std::vector<double> hc((size_t)ldh * m);
         {
-            std::vector<double> hc((size_t)ldh * m);
             MOED_CUDA(ctx, cudaMemcpyAsync(hc.data(), Hp, sizeof(double) * hc.size(), cudaMemcpyDeviceToHost, ctx->stream));
             MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
             for (int j = k; j < m; ++j) {
@@ -1223,21 +1235,23 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
                 }
             }
         }
-        // Rayleigh-Ritz on span V[0..m-1]
-        MOED_CUDA(ctx, cudaMemcpyAsync(dtheta.p, theta.data(), sizeof(double) * std::max(k, 1),
-                                       cudaMemcpyHostToDevice, ctx->stream));
-        MOED_CUDA(ctx, cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)jacobi_smem(kJacobiSmem)));
-        k_jacobi<<<1, 256, jacobi_smem(m), ctx->stream>>>(Hp, ldh, m, k, (const double *)dtheta.p, (double *)dA.p,
-                                                           (double *)dVj.p, (double *)devals.p, (double *)devecs.p, 60);
-        MOED_CHECK_LAUNCH(ctx);
+        // Rayleigh-Ritz on span V[0..m-1], on the host as PARPACK does: the
+        // projected matrix is diag(theta) on the kept block and the columns
+        // of Hp after it (its entries are on the host already)
         evecs_h.resize((size_t)m * m);
-        double beta_m = 0.0;
-        MOED_CUDA(ctx, cudaMemcpyAsync(theta.data(), devals.p, sizeof(double) * m, cudaMemcpyDeviceToHost, ctx->stream));
-        MOED_CUDA(ctx, cudaMemcpyAsync(evecs_h.data(), devecs.p, sizeof(double) * (size_t)m * m, cudaMemcpyDeviceToHost, ctx->stream));
-        if (m < D)
-            MOED_CUDA(ctx, cudaMemcpyAsync(&beta_m, Hp + (size_t)(m - 1) * ldh + m, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-        MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        {
+            std::vector<double> Am((size_t)m * m);
+            for (int i = 0; i < m; ++i)
+                for (int j = 0; j < m; ++j) {
+                    const int r = std::min(i, j), c = std::max(i, j);
+                    Am[(size_t)i * m + j] = c < k ? (r == c ? theta[r] : 0.0) : hc[(size_t)c * ldh + r];
+                }
+            if (!sym_eig(m, Am, theta.data(), evecs_h.data()))
+                return fail(ctx, MO_ED_ERR_NOCONV, "projected eigenproblem did not converge");
+            MOED_CUDA(ctx, cudaMemcpyAsync(devecs.p, evecs_h.data(), sizeof(double) * (size_t)m * m,
+                                           cudaMemcpyHostToDevice, ctx->stream));
+        }
+        const double beta_m = m < D ? hc[(size_t)(m - 1) * ldh + m] : 0.0;
         int nconv = 0;
         double maxres = 0.0;
         for (int i = 0; i < std::min(nwant, m); ++i) {
@@ -1437,16 +1451,13 @@ int refine_fp64(mo_ed_ctx *ctx, const Sector &s, const float *x, DevBuf &out, do
     DevBuf *W = &buf[m0];
     const int G = (int)std::max(1LL, std::min((Dp + kVecThreads - 1) / kVecThreads, (long long)ctx->num_sms * 4));
     const int n2 = m0 + 2, ldh = n2;
-    DevBuf dHp, dh1, dh2, dpart, dnorm, dbeta, dA, dVj, devals, devecs, dsc;
+    DevBuf dHp, dh1, dh2, dpart, dnorm, dbeta, devecs, dsc;
     if (int rc = dev_alloc(ctx, dHp, sizeof(double) * (size_t)n2 * n2)) return rc;
     if (int rc = dev_alloc(ctx, dh1, sizeof(double) * n2)) return rc;
     if (int rc = dev_alloc(ctx, dh2, sizeof(double) * n2)) return rc;
     if (int rc = dev_alloc(ctx, dpart, sizeof(double) * (size_t)n2 * ctx->num_sms * 4)) return rc;
     if (int rc = dev_alloc(ctx, dnorm, sizeof(double) * G)) return rc;
     if (int rc = dev_alloc(ctx, dbeta, sizeof(double) * 2)) return rc;
-    if (int rc = dev_alloc(ctx, dA, sizeof(double) * (size_t)n2 * n2)) return rc;
-    if (int rc = dev_alloc(ctx, dVj, sizeof(double) * (size_t)n2 * n2)) return rc;
-    if (int rc = dev_alloc(ctx, devals, sizeof(double) * n2)) return rc;
     if (int rc = dev_alloc(ctx, devecs, sizeof(double) * (size_t)n2 * n2)) return rc;
     if (int rc = dev_alloc(ctx, dsc, sizeof(double) * 2)) return rc;
     if (int rc = dev_alloc(ctx, out, vb)) return rc;
@@ -1498,14 +1509,14 @@ int refine_fp64(mo_ed_ctx *ctx, const Sector &s, const float *x, DevBuf &out, do
                 break;
             }
         }
-        MOED_CUDA(ctx, cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)jacobi_smem(kJacobiSmem)));
-        k_jacobi<<<1, 256, jacobi_smem(m), ctx->stream>>>(Hp, ldh, m, 0, (const double *)dh1.p, (double *)dA.p,
-                                                           (double *)dVj.p, (double *)devals.p, (double *)devecs.p, 60);
-        MOED_CHECK_LAUNCH(ctx);
-        std::vector<double> ev((size_t)m * m);
-        MOED_CUDA(ctx, cudaMemcpyAsync(ev.data(), devecs.p, sizeof(double) * ev.size(), cudaMemcpyDeviceToHost, ctx->stream));
-        MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        // the projected tridiagonal problem on the host (symeig.h)
+        std::vector<double> Am((size_t)m * m), w(m), ev((size_t)m * m);
+        for (int i = 0; i < m; ++i)
+            for (int j = 0; j < m; ++j) Am[(size_t)i * m + j] = hc[(size_t)std::max(i, j) * ldh + std::min(i, j)];
+        if (!sym_eig(m, Am, w.data(), ev.data()))
+            return fail(ctx, MO_ED_ERR_NOCONV, "projected eigenproblem did not converge");
+        MOED_CUDA(ctx, cudaMemcpyAsync(devecs.p, ev.data(), sizeof(double) * ev.size(), cudaMemcpyHostToDevice,
+                                       ctx->stream));
         int best = 0;
         for (int i = 1; i < m; ++i)
             if (std::fabs(ev[(size_t)i * m]) > std::fabs(ev[(size_t)best * m])) best = i;
