@@ -131,6 +131,8 @@ int mo_ed_destroy(mo_ed_ctx *ctx)
     if (!ctx) return MO_ED_OK;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    for (mo_ed_ctx *w : ctx->workers) mo_ed_destroy(w);
+    ctx->workers.clear();
     ctx->species.clear();
     ctx->states.clear();
     if (ctx->d_mdl) cudaFree(ctx->d_mdl);
@@ -149,7 +151,8 @@ int mo_ed_set_options(mo_ed_ctx *ctx, const mo_ed_options *o)
     if (!o) return fail(ctx, MO_ED_ERR_ARG, "null options");
     if (o->nstep < 1 || o->nev < 1 || !(o->beta > 0) ||
         (o->precision != MO_ED_FP32 && o->precision != MO_ED_FP64) || o->gs_ncv < 0 ||
-        o->gs_maxcycles < 1 || o->gs_tol < 0 || (o->green_fp64 != 0 && o->green_fp64 != 1))
+        o->gs_maxcycles < 1 || o->gs_tol < 0 || (o->green_fp64 != 0 && o->green_fp64 != 1) ||
+        o->solve_threads < 0 || o->solve_threads > 64)
         return fail(ctx, MO_ED_ERR_ARG, "invalid options");
     if (o->green_reorth != 0)
         return fail(ctx, MO_ED_ERR_ARG, "green_reorth = 1 is not available: the Green's-function "
@@ -183,6 +186,8 @@ int mo_ed_set_model(mo_ed_ctx *ctx, int norb, int nbath, double U, double Jex, c
     ctx->ek.assign(ek, ek + nsite);
     ctx->vk.assign(vk, vk + (size_t)norb * nbath);
     ctx->states.clear();
+    for (mo_ed_ctx *w : ctx->workers) mo_ed_destroy(w);   // they hold the old model
+    ctx->workers.clear();
     ctx->green.clear();
     ctx->have_model = false;
     if (int rc = build_model(ctx)) return rc;

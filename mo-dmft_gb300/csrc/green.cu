@@ -8,9 +8,11 @@
 //                                          the batched reference recurrence;
 //                                          G(i w_n) from one CF kernel)
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <thread>
 
 #include "krylov.cuh"
 
@@ -503,6 +505,96 @@ int calc_green(mo_ed_ctx *ctx, double *Gr)
 
 using namespace moed;
 
+namespace moed {
+
+// The eigensolves of ed_solve's sector list (ed_solver.F90:44-60): eig_all
+// [nsector][nev] and the eigenvectors of each sector.  Sectors are
+// independent, and a small sector's thick-restart Lanczos is a chain of
+// short dependent launches, so lists of many small sectors are spread over
+// host threads, each driving worker contexts of its own (same device, model
+// and options; own stream and workspace) so that the chains overlap on the
+// GPU.  Each sector's eigensolve is the same computation in either case.
+static int solve_sectors(mo_ed_ctx *ctx, int nev, std::vector<double> &eig_all,
+                         std::vector<std::vector<DevBuf>> &vecs)
+{
+    const int nsector = (int)ctx->nelec.size();
+    int nthreads = ctx->opt.solve_threads;
+    if (nthreads == 0) {
+        bool small = nsector >= 8;
+        for (int is = 0; is < nsector && small; ++is) {
+            const int nu = ctx->nup[is], nd = ctx->nelec[is] - nu;
+            small = nu >= 0 && nd >= 0 && nu <= ctx->nsite && nd <= ctx->nsite &&
+                    binom(ctx->nsite, nu) * binom(ctx->nsite, nd) < (1LL << 18);
+        }
+        nthreads = small ? 8 : 1;
+    }
+    nthreads = std::min(nthreads, nsector);
+    if (nthreads <= 1) {
+        for (int is = 0; is < nsector; ++is) {
+            Sector s;
+            if (int rc = get_sector(ctx, ctx->nup[is], ctx->nelec[is] - ctx->nup[is], &s)) return rc;
+            std::vector<double> v;
+            if (int rc = diag_sector(ctx, s, nev, v, &vecs[is])) return rc;
+            for (int i = 0; i < nev; ++i) eig_all[(size_t)is * nev + i] = v[i];
+        }
+        return MO_ED_OK;
+    }
+    // worker contexts, kept until the model changes
+    while ((int)ctx->workers.size() < nthreads) {
+        mo_ed_ctx *w = nullptr;
+        if (int rc = mo_ed_create(&w, ctx->device, nullptr)) return fail(ctx, rc, "worker context");
+        ctx->workers.push_back(w);
+        if (int rc = mo_ed_set_model(w, ctx->norb, ctx->nbath, ctx->U, ctx->J, ctx->ek.data(), ctx->vk.data()))
+            return fail(ctx, rc, std::string("worker context: ") + w->err);
+    }
+    MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    std::atomic<int> next{0}, failed{0};
+    std::vector<int> rcs(nthreads, MO_ED_OK);
+    std::vector<long long> l0(nthreads);
+    std::vector<int> who(nsector, 0);
+    auto work = [&](int t) {
+        mo_ed_ctx *w = ctx->workers[t];
+        cudaSetDevice(w->device);
+        w->opt = ctx->opt;
+        for (;;) {
+            const int is = next.fetch_add(1);
+            if (is >= nsector || failed.load()) break;
+            Sector s;
+            int rc = get_sector(w, ctx->nup[is], ctx->nelec[is] - ctx->nup[is], &s);
+            std::vector<double> v;
+            if (!rc) rc = diag_sector(w, s, nev, v, &vecs[is]);
+            if (rc) {
+                rcs[t] = rc;
+                failed.store(1);
+                break;
+            }
+            for (int i = 0; i < nev; ++i) eig_all[(size_t)is * nev + i] = v[i];
+            who[is] = t;
+        }
+        cudaStreamSynchronize(w->stream);
+    };
+    for (int t = 0; t < nthreads; ++t) l0[t] = ctx->workers[t]->launches;
+    std::vector<std::thread> th;
+    for (int t = 1; t < nthreads; ++t) th.emplace_back(work, t);
+    work(0);
+    for (auto &x : th) x.join();
+    cudaSetDevice(ctx->device);
+    for (int t = 0; t < nthreads; ++t) {
+        mo_ed_ctx *w = ctx->workers[t];
+        ctx->launches += w->launches - l0[t];
+        if (rcs[t]) return fail(ctx, rcs[t], w->err);
+    }
+    // statistics of the last sector, as in one thread
+    const mo_ed_ctx *last = ctx->workers[who[nsector - 1]];
+    ctx->diag_cycles = last->diag_cycles;
+    ctx->diag_matvecs = last->diag_matvecs;
+    ctx->diag_res_est = last->diag_res_est;
+    ctx->diag_res_true = last->diag_res_true;
+    return MO_ED_OK;
+}
+
+}  // namespace moed
+
 extern "C" {
 
 int mo_ed_diag(mo_ed_ctx *ctx, int ne_up, int ne_down, int nev, double *eigval, double *eigvec)
@@ -674,13 +766,7 @@ int mo_ed_solve(mo_ed_ctx *ctx, int *nev_calc, double *val, double *prob, int *s
     std::vector<double> eig_all((size_t)nev * nsector, DBL_MAX);
     std::vector<std::vector<DevBuf>> vecs(nsector);
     ctx->states.clear();
-    for (int is = 0; is < nsector; ++is) {
-        Sector s;
-        if (int rc = get_sector(ctx, ctx->nup[is], ctx->nelec[is] - ctx->nup[is], &s)) return rc;
-        std::vector<double> v;
-        if (int rc = diag_sector(ctx, s, nev, v, &vecs[is])) return rc;
-        for (int i = 0; i < nev; ++i) eig_all[(size_t)is * nev + i] = v[i];
-    }
+    if (int rc = solve_sectors(ctx, nev, eig_all, vecs)) return rc;
     const int ntot = nev * nsector;
     std::vector<int> ind(ntot);
     std::vector<double> pev(ntot);

@@ -268,6 +268,9 @@ struct mo_ed_ctx {
     // every shape measured when it was chosen (negative: did not fit)
     std::map<long long, int> hv_choice;
     std::map<long long, std::vector<float>> hv_times;
+    // worker contexts of mo_ed_solve's threads (same device and model, own
+    // streams and workspace); dropped when the model changes
+    std::vector<mo_ed_ctx *> workers;
 };
 
 namespace moed {

@@ -35,7 +35,8 @@ module mo_ed_bind
         real(c_double) :: gs_tol
         integer(c_int) :: green_reorth
         integer(c_int) :: green_fp64
-        integer(c_int) :: reserved(7)
+        integer(c_int) :: solve_threads
+        integer(c_int) :: reserved(6)
     end type mo_ed_options
 
     interface

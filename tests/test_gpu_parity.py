@@ -375,6 +375,28 @@ def test_ed_solve_green_c2(solver, oracle, pkg, precision, etol, gtol):
 
 
 # ---------------------------------------------------------------- DMFT loop pieces, spectra
+def test_ed_solve_threads_bitexact(solver, pkg):
+    """mo_ed_solve over C2's 81 sectors from 8 host threads (worker contexts
+    with their own streams and workspace) gives bit for bit the kept states
+    and G(i w_n) of one thread, in FP32 and FP64."""
+    cfg = pkg.configs.config("C2")
+    ek, vk = cfg.model()
+    for prec in ("fp32", "fp64"):
+        out = {}
+        for nt in (1, 8):
+            solver.set_options(precision=prec, nstep=cfg.nstep, nev=6, beta=cfg.beta, solve_threads=nt)
+            solver.set_model(cfg.norb, cfg.nbath, cfg.U, cfg.J, ek, vk)
+            solver.set_sectors([n for n, _ in cfg.sectors], [u for _, u in cfg.sectors])
+            solver.set_omega(cfg.omega())
+            st = solver.ed_solve()
+            out[nt] = (st, solver.ed_calc_green_ftn())
+        (s1, g1), (s8, g8) = out[1], out[8]
+        assert [(a["val"], a["prob"], a["sector"], a["level"]) for a in s1] == \
+               [(a["val"], a["prob"], a["sector"], a["level"]) for a in s8]
+        assert np.array_equal(g1, g8)
+    solver.set_options(solve_threads=0)
+
+
 def test_band_delta_new_occupation(solver, oracle, pkg):
     """ed_hamiltonian.F90:29-85 and ed_green.F90:187-253 at the reference's
     default Nq = 10,000 (100 x 100 grid), 3 orbitals, 512 w_n: band average,
@@ -620,6 +642,32 @@ def test_minimization_vs_oracle_and_batch(solver, oracle, pkg):
     # from the hidden bath itself: a short run to the noisy target's optimum
     x1, f1, i1 = solver.minimization(x_true, P["nw"], ns, nx, P["omega"], P["dev"], nbath, norb)
     assert f1 <= oracle.func(x_true, ns, P["omega"], P["dev"], nbath, norb)
+
+
+def test_fit_small_grid_one_cta(solver, oracle, pkg):
+    """Below 256 w_n a fit runs on one CTA of 256 threads (no cluster): FUNC /
+    dfunc on 128 w_n against the oracle, and fits from starts near the hidden
+    bath that reach the oracle's floor, alone and in a batch bit for bit."""
+    P = pkg.configs.fit_config(seed=4, nbatch=3)
+    norb, nbath = P["norb"], P["nbath"]
+    ns, nx = norb + nbath, P["X0"].shape[1]
+    om, dev = P["omega"][:128], P["dev"][:, :128]
+    solver.set_options(precision="fp64")
+    for x in P["X0"][:2]:
+        f = solver.FUNC(x, ns, 128, nx, om, dev, nbath, norb)
+        assert abs(f - oracle.func(x, ns, om, dev, nbath, norb)) < 1e-12 * f
+        g = solver.dfunc(x, 128, ns, nx, om, dev, nbath, norb)
+        assert rel(g, oracle.dfunc(x, ns, om, dev, nbath, norb)) < 1e-12
+    h = P["hidden"]
+    x_true = oracle.ev_to_x(np.concatenate([h["ef"], h["eps"]]), h["vk"], h["ef"], ns, nbath)
+    X0 = x_true[None, :] + 0.02 * np.random.default_rng(3).standard_normal((3, nx)) * (x_true[None, :] != 0)
+    X, fret, it, st = solver.fit_batch(X0, om, dev, nbath, norb)
+    for b in range(3):
+        Xs, fs, its, sts = solver.fit_batch(X0[b:b + 1], om, dev, nbath, norb)
+        assert its[0] == it[b] and fs[0] == fret[b] and np.array_equal(Xs[0], X[b])
+        _, fo, _, rc = oracle.frprmn(X0[b], ns, om, dev, nbath, norb)
+        f0 = oracle.func(X0[b], ns, om, dev, nbath, norb)
+        assert fret[b] < 1e-2 * f0 and fo < 1e-2 * f0
 
 
 def test_calc_dev_vs_oracle(solver, oracle):
