@@ -531,6 +531,44 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def chi2_only(pkg, mode, nbatch=304, reps=200):
+    """k_chi2 alone on device arrays: FUNC (mode "func") or FUNC and dfunc
+    ("grad") of nbatch C5 parameter sets per launch (304 = two CTAs per SM),
+    three warm launches, then `reps` timed with CUDA events on the launching
+    stream (reps = 0: the three launches only, for a profiler).  Returns the
+    microseconds per launch."""
+    import torch
+    P = pkg.configs.fit_config(seed=4, nbatch=nbatch)
+    norb, nbath = P["norb"], P["nbath"]
+    nw, nx = len(P["omega"]), P["X0"].shape[1]
+    st = torch.cuda.Stream()
+    torch.cuda.set_stream(st)
+    s = pkg.EDSolver(torch.cuda.current_device(), st.cuda_stream)
+    om = torch.tensor(P["omega"], dtype=torch.float64, device="cuda")
+    dev = torch.tensor(pkg.ed._dev_f(P["dev"]), dtype=torch.float64, device="cuda")
+    X = torch.tensor(P["X0"], dtype=torch.float64, device="cuda")
+    f = torch.empty(nbatch, dtype=torch.float64, device="cuda")
+    G = torch.empty_like(X)
+
+    def run():
+        s.chi2_grad_dev(nbatch, X.data_ptr(), nw, nx, om.data_ptr(), dev.data_ptr(), nbath, norb, f.data_ptr(),
+                        G.data_ptr() if mode == "grad" else 0)
+    for _ in range(3):
+        run()
+    torch.cuda.synchronize()
+    out = {"kernel": "k_chi2", "mode": mode, "nbatch": nbatch, "nw": nw, "nxsize": nx}
+    if reps:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            run()
+        e1.record(st)
+        torch.cuda.synchronize()
+        out["us_per_launch"] = round(e0.elapsed_time(e1) / reps * 1e3, 2)
+    s.close()
+    return out
+
+
 def parse_loop(spec):
     """CONFIG:ITERATIONS[:PRECISION[:SCF_TOLERANCE[:FIT_STARTS]]] -> (name, nloop, precision, scf_tol,
     fit_starts)."""
@@ -562,6 +600,9 @@ def main():
     ap.add_argument("--dmft-loop", default="C1:20:fp64",
                     help="DMFT-loop runs CONFIG:ITERATIONS[:PRECISION[:SCF_TOLERANCE[:FIT_STARTS]]], "
                          "comma-separated ('' for none)")
+    ap.add_argument("--chi2-only", choices=["func", "grad"], default=None,
+                    help="only k_chi2 on 304 C5 parameter sets (timing; --chi2-reps 0: three launches, for ncu)")
+    ap.add_argument("--chi2-reps", type=int, default=200)
     ap.add_argument("--dmft-loop-only", action="store_true",
                     help="only the DMFT-loop runs (one JSON object per run)")
     args = ap.parse_args()
@@ -575,6 +616,10 @@ def main():
         for c in args.lg_config.split(","):
             print(json.dumps(lanczos_g(pkg, c, args.lg_nev, tuple(args.lg_precisions.split(",")),
                                        None if args.no_cpu else args.lg_cpu)), flush=True)
+        return
+    if args.chi2_only:
+        import __graft_entry__ as g
+        print(json.dumps(chi2_only(g.load_package(), args.chi2_only, reps=args.chi2_reps)), flush=True)
         return
     if args.dmft_loop_only:
         import __graft_entry__ as g
