@@ -73,7 +73,7 @@ typedef struct {
                            1: it runs in FP64 whatever `precision` is (FP32 eigenvectors
                            of ed_solve are widened to FP64 before c / c^dagger) */
     int solve_threads;  /* host threads of mo_ed_solve over the sector list.  0 (default):
-                           automatic -- up to 8 for lists of at least 8 sectors of fewer
+                           automatic -- 4 for lists of at least 8 sectors of fewer
                            than 2^18 elements each (small eigensolves are bound by their
                            chains of short launches), one otherwise; 1: one thread; n: up
                            to n.  Each thread solves its sectors through a worker context

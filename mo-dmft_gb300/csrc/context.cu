@@ -186,8 +186,7 @@ int mo_ed_set_model(mo_ed_ctx *ctx, int norb, int nbath, double U, double Jex, c
     ctx->ek.assign(ek, ek + nsite);
     ctx->vk.assign(vk, vk + (size_t)norb * nbath);
     ctx->states.clear();
-    for (mo_ed_ctx *w : ctx->workers) mo_ed_destroy(w);   // they hold the old model
-    ctx->workers.clear();
+    ++ctx->model_gen;   // worker contexts take the new model at their next use
     ctx->green.clear();
     ctx->have_model = false;
     if (int rc = build_model(ctx)) return rc;

@@ -526,7 +526,7 @@ static int solve_sectors(mo_ed_ctx *ctx, int nev, std::vector<double> &eig_all,
             small = nu >= 0 && nd >= 0 && nu <= ctx->nsite && nd <= ctx->nsite &&
                     binom(ctx->nsite, nu) * binom(ctx->nsite, nd) < (1LL << 18);
         }
-        nthreads = small ? 8 : 1;
+        nthreads = small ? 4 : 1;
     }
     nthreads = std::min(nthreads, nsector);
     if (nthreads <= 1) {
@@ -539,13 +539,20 @@ static int solve_sectors(mo_ed_ctx *ctx, int nev, std::vector<double> &eig_all,
         }
         return MO_ED_OK;
     }
-    // worker contexts, kept until the model changes
+    // worker contexts, kept for the context's lifetime; each takes the
+    // current model when it holds an older one
     while ((int)ctx->workers.size() < nthreads) {
         mo_ed_ctx *w = nullptr;
         if (int rc = mo_ed_create(&w, ctx->device, nullptr)) return fail(ctx, rc, "worker context");
         ctx->workers.push_back(w);
+        ctx->worker_gen.push_back(-1);
+    }
+    for (int t = 0; t < nthreads; ++t) {
+        if (ctx->worker_gen[t] == ctx->model_gen) continue;
+        mo_ed_ctx *w = ctx->workers[t];
         if (int rc = mo_ed_set_model(w, ctx->norb, ctx->nbath, ctx->U, ctx->J, ctx->ek.data(), ctx->vk.data()))
             return fail(ctx, rc, std::string("worker context: ") + w->err);
+        ctx->worker_gen[t] = ctx->model_gen;
     }
     MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     std::atomic<int> next{0}, failed{0};

@@ -269,8 +269,10 @@ struct mo_ed_ctx {
     std::map<long long, int> hv_choice;
     std::map<long long, std::vector<float>> hv_times;
     // worker contexts of mo_ed_solve's threads (same device and model, own
-    // streams and workspace); dropped when the model changes
+    // streams and workspace), with the model generation each one holds
     std::vector<mo_ed_ctx *> workers;
+    std::vector<long long> worker_gen;
+    long long model_gen = 0;   // incremented by every mo_ed_set_model
 };
 
 namespace moed {

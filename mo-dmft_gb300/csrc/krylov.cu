@@ -725,12 +725,19 @@ k_multidot_exact(const __grid_constant__ VPtrs<TV> V, int nv, const TW *__restri
 // per thread, 4 vectors' loads in flight.
 template <typename T>
 __global__ void __launch_bounds__(kVecThreads)
-k_multiaxpy(const __grid_constant__ VPtrs<T> V, int nv, const double *__restrict__ h, T *w,
+k_multiaxpy(const __grid_constant__ VPtrs<T> V, int nv, const double *__restrict__ part, int Gm, T *w,
             long long D, double *norm_part)
 {
     __shared__ T sh[kMaxNcv + 4];
     __shared__ double sred[32];
-    for (int l = threadIdx.x; l < nv + 4; l += blockDim.x) sh[l] = l < nv ? (T)h[l] : T(0);
+    // h_l = sum_b part[b][l] in block order, the sum k_multidot's partials
+    // stand for (each block forms it; no separate reduction launch)
+    for (int l = threadIdx.x; l < nv + 4; l += blockDim.x) {
+        double h = 0.0;
+        if (l < nv)
+            for (int b = 0; b < Gm; ++b) h += part[(size_t)b * nv + l];
+        sh[l] = (T)h;
+    }
     __syncthreads();
     // ||w||^2: partials of 4 squares in T, added in FP64 every 8 iterations
     double acc = 0.0;
@@ -771,11 +778,21 @@ k_multiaxpy(const __grid_constant__ VPtrs<T> V, int nv, const double *__restrict
 }
 
 // column j of the projected matrix, beta, 1/beta
-__global__ void k_cgs_finish(const double *h1, const double *h2, int nv, const double *norm_part,
+// p1, p2: the two CGS passes' coefficients as [Gm][nv] partials (Gm = 1:
+// already reduced); column j of the projected matrix is h1 + h2 with
+// h = sum_b p[b][l] in block order
+__global__ void k_cgs_finish(const double *p1, const double *p2, int Gm, int nv, const double *norm_part,
                              int G, double *Hcol, double *beta_out)
 {
     __shared__ double sred[32];
-    for (int l = threadIdx.x; l < nv; l += blockDim.x) Hcol[l] = h1[l] + h2[l];
+    for (int l = threadIdx.x; l < nv; l += blockDim.x) {
+        double h1 = 0.0, h2 = 0.0;
+        for (int b = 0; b < Gm; ++b) {
+            h1 += p1[(size_t)b * nv + l];
+            h2 += p2[(size_t)b * nv + l];
+        }
+        Hcol[l] = h1 + h2;
+    }
     double acc = 0.0;
     for (int i = threadIdx.x; i < G; i += blockDim.x) acc += norm_part[i];
     double t = block_sum(acc, sred);
@@ -1091,22 +1108,53 @@ static VPtrs<T> make_ptrs(const std::vector<DevBuf *> &v, int n)
     return p;
 }
 
+// blocks of k_multidot over a vector of D elements
+static int multidot_grid(const mo_ed_ctx *ctx, long long D)
+{
+    return (int)std::max(1LL, std::min((D / 4 + kVecThreads - 1) / kVecThreads, (long long)ctx->num_sms * 4));
+}
+
+// part: two passes' partials of ortho_pass_stride(ctx) doubles each, then
+// the two passes' reduced coefficients (kMaxNcv + 2 each)
+static long long ortho_pass_stride(const mo_ed_ctx *ctx) { return (long long)(kMaxNcv + 2) * ctx->num_sms * 4; }
+static size_t ortho_part_doubles(const mo_ed_ctx *ctx) { return 2 * (size_t)ortho_pass_stride(ctx) + 2 * (kMaxNcv + 2); }
+// up to this many multi-dot blocks every multi-axpy block adds the partials
+// itself; beyond, one extra launch reduces them (each of the multi-axpy's
+// blocks redoing Gm x nv FP64 additions would cost more than the launch)
+constexpr int kFuseReduceBlocks = 32;
+
+// Where the coefficients of the two CGS passes of an orthogonalize call are:
+// [Gm][nv] partials, Gm = 1 once reduced.
+struct OrthoCoef {
+    const double *p[2];
+    int Gm;
+};
+
+// classical Gram-Schmidt, twice: w -= V (V^T w).  Each pass is a multi-dot
+// into per-block partials and a multi-axpy, which for small grids adds the
+// partials itself; pass 1 leaves the partials of ||w||^2 in norm_part.
 template <typename T>
 static int orthogonalize(mo_ed_ctx *ctx, const std::vector<DevBuf *> &basis, int nv, T *w,
-                         long long D, double *h1, double *h2, double *part, double *norm_part,
-                         int G)
+                         long long D, double *part, double *norm_part, int G, OrthoCoef *coef = nullptr)
 {
     VPtrs<T> P = make_ptrs<T>(basis, nv);
-    const int Gm = (int)std::max(1LL, std::min((D / 4 + kVecThreads - 1) / kVecThreads, (long long)ctx->num_sms * 4));
+    const int Gm = multidot_grid(ctx, D);
+    const bool fuse = Gm <= kFuseReduceBlocks;
     for (int pass = 0; pass < 2; ++pass) {
-        double *h = pass == 0 ? h1 : h2;
-        k_multidot<T><<<Gm, kVecThreads, 0, ctx->stream>>>(P, nv, w, D, part);
+        double *pp = part + pass * ortho_pass_stride(ctx);
+        double *hp = part + 2 * ortho_pass_stride(ctx) + pass * (kMaxNcv + 2);
+        k_multidot<T><<<Gm, kVecThreads, 0, ctx->stream>>>(P, nv, w, D, pp);
         MOED_CHECK_LAUNCH(ctx);
-        k_reduce_cols<<<1, 256, 0, ctx->stream>>>(part, Gm, nv, h);
+        if (!fuse) {
+            k_reduce_cols<<<1, 256, 0, ctx->stream>>>(pp, Gm, nv, hp);
+            MOED_CHECK_LAUNCH(ctx);
+        }
+        k_multiaxpy<T><<<G, kVecThreads, 0, ctx->stream>>>(P, nv, fuse ? pp : hp, fuse ? Gm : 1, w, D,
+                                                           pass == 1 ? norm_part : nullptr);
         MOED_CHECK_LAUNCH(ctx);
-        k_multiaxpy<T><<<G, kVecThreads, 0, ctx->stream>>>(P, nv, h, w, D, pass == 1 ? norm_part : nullptr);
-        MOED_CHECK_LAUNCH(ctx);
+        if (coef) coef->p[pass] = fuse ? pp : hp;
     }
+    if (coef) coef->Gm = fuse ? Gm : 1;
     return MO_ED_OK;
 }
 
@@ -1153,7 +1201,7 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
     if (int rc = ensure(ctx, dHp, sizeof(double) * (size_t)n2 * n2)) return rc;
     if (int rc = ensure(ctx, dh1, sizeof(double) * n2)) return rc;
     if (int rc = ensure(ctx, dh2, sizeof(double) * n2)) return rc;
-    if (int rc = ensure(ctx, dpart, sizeof(double) * (size_t)n2 * ctx->num_sms * 4)) return rc;
+    if (int rc = ensure(ctx, dpart, sizeof(double) * ortho_part_doubles(ctx))) return rc;
     if (int rc = ensure(ctx, dnorm, sizeof(double) * G)) return rc;
     if (int rc = ensure(ctx, dbeta, sizeof(double) * 2)) return rc;
     if (int rc = ensure(ctx, devecs, sizeof(double) * (size_t)n2 * n2)) return rc;
@@ -1201,12 +1249,11 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
         for (int j = k; j < ncv; ++j) {
             if (int rc = hv(V[j]->p, W->p)) return rc;
             const bool last = j + 1 >= D;   // Krylov space is the whole sector
-            if (int rc = orthogonalize<T>(ctx, V, j + 1, (T *)W->p, Dp, (double *)dh1.p, (double *)dh2.p,
-                                          (double *)dpart.p, (double *)dnorm.p, G))
+            OrthoCoef oc;
+            if (int rc = orthogonalize<T>(ctx, V, j + 1, (T *)W->p, Dp, (double *)dpart.p, (double *)dnorm.p, G, &oc))
                 return rc;
-            k_cgs_finish<<<1, 256, 0, ctx->stream>>>((const double *)dh1.p, (const double *)dh2.p, j + 1,
-                                                     (const double *)dnorm.p, G, Hp + (size_t)j * ldh,
-                                                     (double *)dbeta.p);
+            k_cgs_finish<<<1, 256, 0, ctx->stream>>>(oc.p[0], oc.p[1], oc.Gm, j + 1, (const double *)dnorm.p, G,
+                                                     Hp + (size_t)j * ldh, (double *)dbeta.p);
             MOED_CHECK_LAUNCH(ctx);
             if (!last) {
                 k_scale_copy<T><<<G, kVecThreads, 0, ctx->stream>>>((const T *)W->p, (T *)V[j + 1]->p, Dp,
@@ -1285,8 +1332,7 @@ static int trl_solve(mo_ed_ctx *ctx, const Sector &s, int nev, std::vector<doubl
             k_random<T><<<G, kVecThreads, 0, ctx->stream>>>((T *)W->p, Dp, s.ld(), s.up->n,
                                                             seed + 7919ULL * (cycle + 1) * kMaxNcv);
             MOED_CHECK_LAUNCH(ctx);
-            if (int rc = orthogonalize<T>(ctx, V, kk, (T *)W->p, Dp, (double *)dh1.p, (double *)dh2.p,
-                                          (double *)dpart.p, (double *)dnorm.p, G))
+            if (int rc = orthogonalize<T>(ctx, V, kk, (T *)W->p, Dp, (double *)dpart.p, (double *)dnorm.p, G))
                 return rc;
             if (int rc = normalize_into((T *)W->p, V[kk])) return rc;
         } else {
@@ -1455,7 +1501,7 @@ int refine_fp64(mo_ed_ctx *ctx, const Sector &s, const float *x, DevBuf &out, do
     if (int rc = dev_alloc(ctx, dHp, sizeof(double) * (size_t)n2 * n2)) return rc;
     if (int rc = dev_alloc(ctx, dh1, sizeof(double) * n2)) return rc;
     if (int rc = dev_alloc(ctx, dh2, sizeof(double) * n2)) return rc;
-    if (int rc = dev_alloc(ctx, dpart, sizeof(double) * (size_t)n2 * ctx->num_sms * 4)) return rc;
+    if (int rc = dev_alloc(ctx, dpart, sizeof(double) * ortho_part_doubles(ctx))) return rc;
     if (int rc = dev_alloc(ctx, dnorm, sizeof(double) * G)) return rc;
     if (int rc = dev_alloc(ctx, dbeta, sizeof(double) * 2)) return rc;
     if (int rc = dev_alloc(ctx, devecs, sizeof(double) * (size_t)n2 * n2)) return rc;
@@ -1481,12 +1527,12 @@ int refine_fp64(mo_ed_ctx *ctx, const Sector &s, const float *x, DevBuf &out, do
         // afterwards and ends the Krylov space there (later steps are discarded)
         for (int j = 0; j < m0; ++j) {
             if (int rc = hv_single(ctx, s, HV_F64, V[j]->p, W->p)) return rc;
-            if (int rc = orthogonalize<double>(ctx, V, j + 1, (double *)W->p, Dp, (double *)dh1.p, (double *)dh2.p,
-                                               (double *)dpart.p, (double *)dnorm.p, G))
+            OrthoCoef oc;
+            if (int rc = orthogonalize<double>(ctx, V, j + 1, (double *)W->p, Dp, (double *)dpart.p,
+                                               (double *)dnorm.p, G, &oc))
                 return rc;
-            k_cgs_finish<<<1, 256, 0, ctx->stream>>>((const double *)dh1.p, (const double *)dh2.p, j + 1,
-                                                     (const double *)dnorm.p, G, Hp + (size_t)j * ldh,
-                                                     (double *)dbeta.p);
+            k_cgs_finish<<<1, 256, 0, ctx->stream>>>(oc.p[0], oc.p[1], oc.Gm, j + 1, (const double *)dnorm.p, G,
+                                                     Hp + (size_t)j * ldh, (double *)dbeta.p);
             MOED_CHECK_LAUNCH(ctx);
             if (j + 1 < m0) {
                 k_scale_copy<double><<<G, kVecThreads, 0, ctx->stream>>>((const double *)W->p, (double *)V[j + 1]->p,
