@@ -284,6 +284,17 @@ def test_lanczos_iteration_fp32(setup, oracle):
     n, a, bb = s.lanczos_iteration(4, 5, v)
     n0, a0, b0 = oracle.lanczos_iteration(m, b, v.astype(np.float32).astype(np.float64), 20)
     assert rel(a[:6], a0[:6]) < 1e-5 and rel(bb[1:6], b0[1:6]) < 1e-5
+    # all 20 steps through the continued fraction they define
+    # (ed_green.F90:151-157), at broadening 0.5 over the spectral range
+    assert n == n0
+    z = np.linspace(a0[:n0].min(), a0[:n0].max(), 64) + 0.5j
+
+    def cf(aa, bbb):
+        g = np.zeros_like(z)
+        for j in range(n0 - 1, 0, -1):
+            g = bbb[j] / (z - aa[j] - g)
+        return 1.0 / (z - aa[0] - g)
+    assert rel(cf(a, bb), cf(a0, b0)) < 1e-5
 
 
 # ---------------------------------------------------------------- diag
