@@ -1,5 +1,5 @@
-// fit.cu -- chi^2 bath fit: FUNC / dfunc as one adjoint kernel, frprmn on
-// the host, calc_dev.
+// fit.cu -- chi^2 bath fit: FUNC / dfunc as one adjoint kernel, whole
+// frprmn fits on the device, calc_dev.
 //
 // FUNC (func.f90:1-45) and dfunc (func.f90:47-142) for x = [eps(1:nbath),
 // V(1,1:nbath), ..., V(norb,1:nbath), ef(1:norb)] (x_to_ev, func.f90:193-216):
@@ -9,16 +9,17 @@
 //   d/d eps_k  = sum_{a,n} 2 Re[conj(r) V^2 / (i w_n - eps_k)^2] / w_n / (norb^2 nw)
 //   d/d V_ak   = sum_n     2 Re[2 conj(r) V / (i w_n - eps_k)]  / w_n / (norb^2 nw)
 //   d/d ef_a   = sum_n     2 Re[r] / w_n / (norb^2 nw)
-// The kernel evaluates the forward residual and its adjoint together: one CTA
-// per parameter set, one thread per frequency stripe, per-parameter partials
-// in shared memory summed in a fixed order.  Like the reference, i w_n is
-// formed by CMPLX(0, w_n) -- a single-precision w_n -- when fortran_cmplx is
-// set, while the 1/w_n weights use the double w_n.
+// chi2_sums evaluates the forward residual and its adjoint together over a
+// CTA's share of the w_n, one thread per frequency stripe, per-parameter
+// partials in shared memory summed in a fixed order.  Like the reference,
+// i w_n is formed by CMPLX(0, w_n) -- a single-precision w_n -- when
+// fortran_cmplx is set, while the 1/w_n weights use the double w_n.
 //
 // frprmn / linmin / mnbrak / brent (frprmn.f90) are restated once, with the
-// reference's default-REAL constants, as host/device code.  mo_ed_minimization
-// and mo_ed_fit_batch run them on the device, one CTA per fit (k_fit), each
-// FUNC / dfunc evaluated by that CTA: nbatch fits in one launch.
+// reference's default-REAL constants.  mo_ed_minimization and
+// mo_ed_fit_batch run them on the device (k_fit): one thread-block cluster
+// per fit, which splits each FUNC / dfunc over its CTAs by w_n; nbatch fits
+// in one launch.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
