@@ -143,8 +143,15 @@ def cpu_baseline_sample(cfg, nup, ndn, seconds=3.0):
         done += r1 - r0
         r0 = r1 % b.ntot
     dt = time.perf_counter() - t0
+    # the same rows on one core (the reference is serial within an MPI rank)
+    rows1 = int(min(b.ntot, max(1, done / dt / (os.cpu_count() or 1))))   # about one second
+    t1 = time.perf_counter()
+    O.multiply_H_rows(m, b, x, y, 0, rows1, 1)
+    dt1 = time.perf_counter() - t1
     return dict(value=2.0 * done * 8 / dt / 1e9, unit="GB/s", cores=os.cpu_count(), kind="port",
-                sample=f"{done} of {b.ntot} rows of one FP64 H*v (oracle C port, OpenMP over rows), {dt:.2f} s")
+                value_1core=round(2.0 * rows1 * 8 / dt1 / 1e9, 5),
+                sample=f"{done} of {b.ntot} rows of one FP64 H*v (oracle C port, OpenMP over rows), {dt:.2f} s; "
+                       f"value_1core: {rows1} rows on one core, {dt1:.2f} s")
 
 
 def lanczos_g_cpu(pkg, name, nev, states, matvecs, full=False, seconds=3.0):
@@ -299,11 +306,12 @@ def dmft_bench(pkg, cpu=True):
     return out
 
 
-def fit_bench(pkg, cpu_fits=2):
+def fit_bench(pkg, cpu_fits=2, nbatch=256):
     """C5: 256 random starts of the chi^2 bath fit in one lockstep batch (FP64
     adjoint gradient on the device), next to the oracle's frprmn on one host
     core for a bounded number of the same starts."""
     P = pkg.configs.fit_config(seed=4, nbatch=256)
+    P["X0"] = P["X0"][:nbatch]
     norb, nbath = P["norb"], P["nbath"]
     ns = norb + nbath
     s = pkg.EDSolver(0)
@@ -609,6 +617,8 @@ def main():
     ap.add_argument("--dmft-loop", default="C1:20:fp64",
                     help="DMFT-loop runs CONFIG:ITERATIONS[:PRECISION[:SCF_TOLERANCE[:FIT_STARTS]]], "
                          "comma-separated ('' for none)")
+    ap.add_argument("--fit-only", type=int, default=0,
+                    help="only the C5 bath fit, on the first N starts (no CPU leg)")
     ap.add_argument("--chi2-only", choices=["func", "grad"], default=None,
                     help="only k_chi2 on 304 C5 parameter sets (timing; --chi2-reps 0: three launches, for ncu)")
     ap.add_argument("--chi2-reps", type=int, default=200)
@@ -625,6 +635,10 @@ def main():
         for c in args.lg_config.split(","):
             print(json.dumps(lanczos_g(pkg, c, args.lg_nev, tuple(args.lg_precisions.split(",")),
                                        None if args.no_cpu else args.lg_cpu)), flush=True)
+        return
+    if args.fit_only:
+        import __graft_entry__ as g
+        print(json.dumps(fit_bench(g.load_package(), 0, args.fit_only)), flush=True)
         return
     if args.chi2_only:
         import __graft_entry__ as g
