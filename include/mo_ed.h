@@ -297,12 +297,19 @@ int mo_ed_dfunc(mo_ed_ctx *ctx, const double *x, double *p, int nwloc, int ns, i
 int mo_ed_minimization(mo_ed_ctx *ctx, double *x, int nwloc, int ns, int nxsize,
                        const double *omega, const double *D_ev, int nbath, int norb,
                        double *fret, int *iter);
-/* nbatch independent fits in lockstep; every line-search FUNC call of all
- * active fits is one batched device launch.  x[nbatch][nxsize] in place;
- * fret, iter, status have nbatch entries (status: 0, or MO_ED_ERR_FIT). */
+/* nbatch independent fits (the reference runs one per call) in one launch:
+ * each fit runs on a thread-block cluster that splits every FUNC / dfunc
+ * over its CTAs by w_n; the clusters share the fits out and take turns on
+ * long ones.  Each fit's result equals that of the same fit run alone, bit
+ * for bit.  x[nbatch][nxsize] in place; fret, iter, status have nbatch
+ * entries (status: 0, or MO_ED_ERR_FIT). */
 int mo_ed_fit_batch(mo_ed_ctx *ctx, int nbatch, double *x, int nwloc, int ns, int nxsize,
                     const double *omega, const double *D_ev, int nbath, int norb, double ftol,
                     double *fret, int *iter, int *status);
+/* Statistics of the last mo_ed_fit_batch / mo_ed_minimization (no
+ * counterpart in the reference): how often a fit gave up its cluster to a
+ * waiting fit, and the number of clusters launched. */
+int mo_ed_fit_stats(mo_ed_ctx *ctx, long long *suspensions, int *clusters);
 /* chi^2 and gradient of nbatch parameter sets on device pointers
  * (x[nbatch][nxsize], f[nbatch], g[nbatch][nxsize]); dev is the device copy
  * of D_ev, omega of the grid.  No synchronization. */

@@ -19,18 +19,24 @@
 // reference's default-REAL constants.  mo_ed_minimization and
 // mo_ed_fit_batch run them on the device (k_fit): one thread-block cluster
 // per fit, which splits each FUNC / dfunc over its CTAs by w_n; nbatch fits
-// in one launch.
+// in one launch of persistent clusters that share the fits out among
+// themselves and take turns on long ones.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 
 #include <cooperative_groups.h>
+#include <cuda/atomic>
 
 #include "internal.h"
 
 namespace moed {
 
 constexpr int kFitThreads = 128;
+// Frprmn::run's return value for a fit that gave up its cluster to a
+// waiting fit (not an MO_ED code: k_fit parks such fits and resumes them)
+constexpr int kFitSuspended = -1;
 constexpr int kMaxX = 60;           // nmax of frprmn.f90:12
 
 __device__ __forceinline__ double2 zdiv(double2 a, double2 b)   // Smith (1962)
@@ -366,7 +372,7 @@ struct Evaluator {
 };
 
 // ---------------------------------------------------------------------------
-// frprmn.f90 restated on the host; func(x) / dfunc(x, g) through callbacks
+// frprmn.f90 restated; func(x) / dfunc(x, g) / func.line through functors
 // ---------------------------------------------------------------------------
 template <typename F, typename DF>
 struct Frprmn {
@@ -508,19 +514,40 @@ struct Frprmn {
         return rc;
     }
 
-    __host__ __device__ int run(double *p, double ftol, int &iter, double &fret)
+    // CG state at the top of an iteration: g, h (xi = h there), fp and the
+    // iterations done.  A suspended fit is p plus this state; resumed from
+    // it, the fit takes the same steps as one run without a break.
+    double g[kMaxX], h[kMaxX], fp = 0.0;
+    int its_done = 0;
+
+    // resume: g, h, fp, its_done hold a suspended fit's state.  quantum > 0:
+    // every quantum iterations of this call, ask func.yield() whether other
+    // fits are waiting; if so, return kFitSuspended (*iter = its_done).
+    __host__ __device__ int run(double *p, double ftol, int &iter, double &fret, bool resume = false,
+                                int quantum = 0)
     {
         const int itmax = 20000;
         const double eps = 1.e-10;
-        double g[kMaxX], h[kMaxX], xi[kMaxX], dgg, fp, gam, gg;
-        fp = func(p);
-        dfunc(p, xi);
-        for (int j = 0; j < n; ++j) {
-            g[j] = -xi[j];
-            h[j] = g[j];
-            xi[j] = h[j];
+        double xi[kMaxX], dgg, gam, gg;
+        if (resume) {
+            for (int j = 0; j < n; ++j) xi[j] = h[j];
+        } else {
+            its_done = 0;
+            fp = func(p);
+            dfunc(p, xi);
+            for (int j = 0; j < n; ++j) {
+                g[j] = -xi[j];
+                h[j] = g[j];
+                xi[j] = h[j];
+            }
         }
-        for (int its = 1; its <= itmax; ++its) {
+        const int its0 = its_done + 1;
+        for (int its = its0; its <= itmax; ++its) {
+            if (quantum > 0 && its > its0 && (its - its0) % quantum == 0 && func.yield()) {
+                iter = its_done;
+                fret = fp;
+                return kFitSuspended;
+            }
             iter = its;
             if (int rc = linmin(p, xi, fret)) return rc;
             if (2. * fabs(fret - fp) <= ftol * (fabs(fret) + fabs(fp) + eps)) return 0;
@@ -539,15 +566,19 @@ struct Frprmn {
                 h[j] = g[j] + gam * h[j];
                 xi[j] = h[j];
             }
+            its_done = its;
         }
         return MO_ED_ERR_FIT;
     }
 };
 
 // ---------------------------------------------------------------------------
-// fits on the device: a cluster of C CTAs (C = 1 .. 8) runs one fit to the
-// end.  Every thread of every CTA executes the same frprmn steps on its own
-// copy of the scalars and vectors.  Each FUNC / dfunc is split over the
+// fits on the device: a cluster of C CTAs (C = 1 .. 8) runs one fit.  Warp 0
+// of every CTA executes the same frprmn steps, each lane on its own copy of
+// the scalars and vectors; the other warps of the CTA wait for its commands
+// (evaluate, look for waiting fits, done) and join each evaluation, so the
+// line search's scalar FP64 work runs once per CTA, not once per warp.  Each
+// FUNC / dfunc is split over the
 // cluster by w_n: CTA r of the cluster sums the terms of the w_n with
 // n = r nt + t + k C nt (chi2_sums), writes its sums into its slot, and after
 // one cluster barrier every CTA adds the C slots (read through distributed
@@ -568,17 +599,73 @@ constexpr size_t kFitSmemMax = 220 * 1024;
 
 namespace cg = cooperative_groups;
 
+// Scheduler words of one k_fit launch (global memory, zeroed before it):
+// q[kQFresh] fits handed out from the batch, q[kQParked] fits parked,
+// q[kQSusp] suspensions, q[kQGaveUp] picks that gave up (an internal error);
+// flag[b] = 1 while fit b is parked, its[b] its iterations done.
+constexpr int kQFresh = 0, kQParked = 1, kQSusp = 2, kQGaveUp = 3, kQWords = 4;
+constexpr int kCmdFunc = 0, kCmdGrad = 1, kCmdYield = 2, kCmdDone = 3;
+
+__device__ __forceinline__ int ld_relaxed(int *a)
+{
+    return cuda::atomic_ref<int, cuda::thread_scope_device>(*a).load(cuda::memory_order_relaxed);
+}
+
 struct DevChi2 {
     int nx, nw, norb, nbath, fcmplx;
     const double *omega, *dev;
     double *sm, *sx, *sres, *slots;   // slots: [2][kMaxX + 1] of this CTA
     int rank, ncta, par;
-    // chi^2 (and the gradient into g) at the point sx, already in shared memory
-    __device__ double eval_sx(double *g)
+    int *q, nbatch;                   // scheduler words
+    int *bcast;                       // [2] in this CTA's shared memory
+    int *s_cmd;                       // warp 0's command to the CTA
+    // every thread of every CTA of the cluster passes
+    __device__ void sync_all()
     {
+        if (ncta > 1)
+            cg::this_cluster().sync();
+        else
+            __syncthreads();
+    }
+    // rank 0's thread 0 hands a, b to every CTA of the cluster (read them
+    // after the next sync_all)
+    __device__ void publish(int a, int b)
+    {
+        if (ncta > 1) {
+            cg::cluster_group cl = cg::this_cluster();
+            for (int r = 0; r < ncta; ++r) {
+                int *t = cl.map_shared_rank(bcast, r);
+                t[0] = a;
+                t[1] = b;
+            }
+        } else {
+            bcast[0] = a;
+            bcast[1] = b;
+        }
+    }
+    // Commands of warp 0 (which runs frprmn) to the other warps of its CTA,
+    // which wait in serve(); each starts with a CTA barrier
+    __device__ void command(int cmd)
+    {
+        if (threadIdx.x == 0) *s_cmd = cmd;
         __syncthreads();
+    }
+    // whether fits wait for a cluster: batch fits not yet started or parked
+    // ones.  One thread looks, the cluster follows its answer.
+    __device__ bool yield_body()
+    {
+        if (rank == 0 && threadIdx.x == 0)
+            publish(ld_relaxed(&q[kQFresh]) < nbatch || ld_relaxed(&q[kQParked]) > 0, 0);
+        sync_all();
+        const bool w = bcast[0] != 0;
+        sync_all();   // bcast is written again at the next decision
+        return w;
+    }
+    // chi^2 sums at the point sx by every thread of the CTA, reduced over the
+    // cluster and scaled into sres
+    __device__ void eval_body(bool grad)
+    {
         const int nt = blockDim.x;
-        const bool grad = g != nullptr;
         double *mine = slots + par * (kMaxX + 1);
         chi2_sums(sx, nx, grad, nw, rank * nt, ncta * nt, norb, nbath, omega, dev, fcmplx, sm, mine);
         const int nout = grad ? nx + 1 : 1;
@@ -595,22 +682,47 @@ struct DevChi2 {
             }
         }
         par ^= 1;
-        __syncthreads();
+        __syncthreads();   // sres is complete
+    }
+    // warps 1 .. of the CTA: run the commands of warp 0 until kCmdDone
+    __device__ void serve()
+    {
+        for (;;) {
+            __syncthreads();
+            const int cmd = *s_cmd;
+            if (cmd == kCmdFunc || cmd == kCmdGrad)
+                eval_body(cmd == kCmdGrad);
+            else if (cmd == kCmdYield)
+                yield_body();
+            else
+                return;
+        }
+    }
+    // warp 0 only, from here on.  sx and sres are rewritten only after the
+    // barrier of the next command, which the other warps reach once done.
+    __device__ bool yield()
+    {
+        command(kCmdYield);
+        return yield_body();
+    }
+    // chi^2 (and the gradient into g) at the point sx, already in shared memory
+    __device__ double eval_sx(double *g)
+    {
+        command(g ? kCmdGrad : kCmdFunc);
+        eval_body(g != nullptr);
         if (g)
             for (int j = 0; j < nx; ++j) g[j] = sres[1 + j];
-        const double f = sres[0];
-        __syncthreads();   // sx / sres are reused by the next evaluation
-        return f;
+        return sres[0];
     }
     __device__ double eval(const double *x, double *g)
     {
-        for (int j = threadIdx.x; j < nx; j += blockDim.x) sx[j] = x[j];
+        for (int j = threadIdx.x; j < nx; j += 32) sx[j] = x[j];
         return eval_sx(g);
     }
-    // f1dim's point p + t xi, each element formed once, by one thread
+    // f1dim's point p + t xi, each element formed once, by one lane
     __device__ double line(const double *p, const double *xi, double t)
     {
-        for (int j = threadIdx.x; j < nx; j += blockDim.x) sx[j] = p[j] + t * xi[j];
+        for (int j = threadIdx.x; j < nx; j += 32) sx[j] = p[j] + t * xi[j];
         return eval_sx(nullptr);
     }
 };
@@ -618,49 +730,151 @@ struct DevFunc {
     DevChi2 *c;
     __device__ double operator()(const double *x) const { return c->eval(x, nullptr); }
     __device__ double line(const double *p, const double *xi, double t) const { return c->line(p, xi, t); }
+    __device__ bool yield() const { return c->yield(); }
 };
 struct DevDFunc {
     DevChi2 *c;
     __device__ void operator()(const double *x, double *g) const { c->eval(x, g); }
 };
 
-// grid: nbatch clusters of ncta CTAs (ncta = 1: a plain launch); fit b is
-// cluster b, and CTA rank 0 writes its results
-__global__ void __launch_bounds__(kFitCta, 1)
-k_fit(double *__restrict__ X, int nx, int nw, int norb, int nbath, const double *__restrict__ omega,
-      const double *__restrict__ dev, int fcmplx, double ftol, int ncta, double *fret, int *iter, int *status)
+// A parked fit, taken by one cluster: the one with the fewest iterations
+// done (the waiting fits share the clusters about equally, so the long
+// fits of a batch progress from the start instead of starting last).
+// Called by one thread; returns -1 when no fit is parked.  A fit is parked
+// only by a cluster that picks right after parking it, so a fit that this
+// pick misses is taken by that cluster: no parked fit is left behind when
+// the clusters leave.  Bounded: a failed claim means another cluster took
+// that fit; after 4 nbatch + 4 failed claims the pick gives up (q[kQGaveUp]
+// counts it, and the host reports the fits left unfinished).
+__device__ int take_parked(int *q, int *flag, int *its, int nbatch)
+{
+    for (int attempt = 0; attempt < 4 * nbatch + 4; ++attempt) {
+        int best = -1, fewest = INT_MAX;
+        for (int j = 0; j < nbatch; ++j)
+            if (ld_relaxed(&flag[j]) == 1) {
+                const int d = ld_relaxed(&its[j]);
+                if (d < fewest) {
+                    fewest = d;
+                    best = j;
+                }
+            }
+        if (best < 0) return -1;
+        if (atomicCAS(&flag[best], 1, 0) == 1) {
+            atomicSub(&q[kQParked], 1);
+            __threadfence();   // the parked state is read after this
+            return best;
+        }
+    }
+    atomicAdd(&q[kQGaveUp], 1);
+    return -1;
+}
+
+// grid: persistent clusters of ncta CTAs (ncta = 1: one CTA each).  A
+// cluster takes batch fits in order (q[kQFresh]); every `quantum` CG
+// iterations a running fit yields its cluster if fits are waiting, and is
+// parked: p in X, g, h, fp in state[b][2 nx + 1], its iterations in its[b].
+// When the batch is handed out, clusters resume parked fits.  A resumed fit
+// continues from its state, so every fit takes the same steps as when run
+// alone.  Rank 0's thread 0 makes each decision and hands it to the
+// cluster.  NT threads per CTA, MINB CTAs per SM (the shared memory of the
+// chi^2 partials allows two kFitThreads-thread CTAs per SM for C5's
+// 51 parameters).
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+k_fit(double *__restrict__ X, int nbatch, int nx, int nw, int norb, int nbath, const double *__restrict__ omega,
+      const double *__restrict__ dev, int fcmplx, double ftol, int ncta, int quantum, int *q, int *flag, int *its,
+      double *state, double *fret, int *iter, int *status)
 {
     extern __shared__ double sm[];   // chi2_smem_bytes(nx, nbath, blockDim.x)
     __shared__ double sx[kMaxX], sres[kMaxX + 1], slots[2 * (kMaxX + 1)];
-    const int b = blockIdx.x / ncta, rank = blockIdx.x % ncta;
-    DevChi2 c{nx, nw, norb, nbath, fcmplx, omega, dev, sm, sx, sres, slots, rank, ncta, 0};
+    __shared__ int bcast[2], s_cmd;
+    const int rank = blockIdx.x % ncta;
+    const bool lead = rank == 0 && threadIdx.x == 0;
+    const size_t sw = 2 * (size_t)nx + 1;
+    DevChi2 c{nx, nw, norb, nbath, fcmplx, omega, dev, sm, sx, sres, slots, rank, ncta, 0, q, nbatch, bcast, &s_cmd};
     Frprmn<DevFunc, DevDFunc> fr{DevFunc{&c}, DevDFunc{&c}, nx};
     double p[kMaxX];
-    for (int j = 0; j < nx; ++j) p[j] = X[(size_t)b * nx + j];
-    int it = 0;
-    double f = 0.0;
-    const int rc = fr.run(p, ftol, it, f);
-    if (rank == 0 && threadIdx.x == 0) {
-        for (int j = 0; j < nx; ++j) X[(size_t)b * nx + j] = p[j];
-        fret[b] = f;
-        iter[b] = it;
-        status[b] = rc;
+    c.sync_all();   // every CTA of the cluster runs before its shared memory is written remotely
+    for (;;) {
+        if (lead) {
+            int b = atomicAdd(&q[kQFresh], 1), resume = 0;
+            if (b >= nbatch) {
+                b = take_parked(q, flag, its, nbatch);
+                resume = 1;
+            }
+            c.publish(b, resume);
+        }
+        c.sync_all();
+        const int b = bcast[0];
+        const bool resume = bcast[1] != 0;
+        c.sync_all();   // bcast is written again by yield()
+        if (b < 0) break;
+        if (threadIdx.x >= 32) {
+            c.serve();   // the chi^2 evaluations of warp 0's fit
+            continue;
+        }
+        // L2 loads: a parked fit's words were written by another SM
+        for (int j = 0; j < nx; ++j) p[j] = __ldcg(&X[(size_t)b * nx + j]);
+        if (resume) {
+            const double *st = state + (size_t)b * sw;
+            for (int j = 0; j < nx; ++j) {
+                fr.g[j] = __ldcg(&st[j]);
+                fr.h[j] = __ldcg(&st[nx + j]);
+            }
+            fr.fp = __ldcg(&st[2 * nx]);
+            fr.its_done = __ldcg(&its[b]);
+        }
+        int it = 0;
+        double f = 0.0;
+        const int rc = fr.run(p, ftol, it, f, resume, quantum);
+        c.command(kCmdDone);
+        if (lead) {
+            for (int j = 0; j < nx; ++j) X[(size_t)b * nx + j] = p[j];
+            if (rc == kFitSuspended) {
+                double *st = state + (size_t)b * sw;
+                for (int j = 0; j < nx; ++j) {
+                    st[j] = fr.g[j];
+                    st[nx + j] = fr.h[j];
+                }
+                st[2 * nx] = fr.fp;
+                its[b] = fr.its_done;
+                __threadfence();   // the state is visible before the flag
+                atomicExch(&flag[b], 1);
+                atomicAdd(&q[kQParked], 1);
+                atomicAdd(&q[kQSusp], 1);
+            } else {
+                fret[b] = f;
+                iter[b] = it;
+                status[b] = rc;
+            }
+        }
     }
     // no CTA leaves while another may still read its slots
     if (ncta > 1) cg::this_cluster().sync();
 }
+
+// CG iterations between two looks for waiting fits: short against a long
+// fit (20000 iterations at most), long against a look (two cluster barriers)
+constexpr int kFitQuantum = 256;
 
 // nbatch fits of host parameter sets x[nbatch][nxsize], in place
 static int fit_on_device(mo_ed_ctx *ctx, FitProblem &P, int nbatch, double *x, double ftol, double *fret, int *iter,
                          int *status)
 {
     const int nx = P.nxsize;
-    DevBuf dx, df, di, ds;
+    const size_t sw = 2 * (size_t)nx + 1;
+    DevBuf dx, df, di, ds, dq, dst;
     if (int rc = dev_alloc(ctx, dx, sizeof(double) * (size_t)nbatch * nx)) return rc;
     if (int rc = dev_alloc(ctx, df, sizeof(double) * nbatch)) return rc;
     if (int rc = dev_alloc(ctx, di, sizeof(int) * nbatch)) return rc;
     if (int rc = dev_alloc(ctx, ds, sizeof(int) * nbatch)) return rc;
+    if (int rc = dev_alloc(ctx, dq, sizeof(int) * (kQWords + 2 * (size_t)nbatch))) return rc;
+    if (int rc = dev_alloc(ctx, dst, sizeof(double) * (size_t)nbatch * sw)) return rc;
+    int *q = (int *)dq.p, *flag = q + kQWords, *its = flag + nbatch;
     MOED_CUDA(ctx, cudaMemcpyAsync(dx.p, x, sizeof(double) * (size_t)nbatch * nx, cudaMemcpyHostToDevice, ctx->stream));
+    MOED_CUDA(ctx, cudaMemsetAsync(dq.p, 0, dq.bytes, ctx->stream));
+    // a status the kernel never wrote reads kFitSuspended (all bits set)
+    MOED_CUDA(ctx, cudaMemsetAsync(ds.p, 0xff, ds.bytes, ctx->stream));
     // a cluster of ncta CTAs of kFitThreads per fit for nw >= 256 (about one
     // w_n per thread); else one CTA of kFitCta threads where the partial sums
     // fit in shared memory, or of kFitThreads
@@ -668,7 +882,8 @@ static int fit_on_device(mo_ed_ctx *ctx, FitProblem &P, int nbatch, double *x, d
     while (ncta < kFitMaxCluster && P.nwloc >= 2 * ncta * kFitThreads) ncta *= 2;
     if (P.nwloc < 2 * kFitThreads && chi2_smem_bytes(nx, P.nbath, kFitCta) <= kFitSmemMax) nt = kFitCta;
     size_t smem;
-    if (int rc = chi2_smem(ctx, (const void *)k_fit, nx, P.nbath, nt, &smem)) return rc;
+    auto kern = nt == kFitCta ? k_fit<kFitCta, 1> : k_fit<kFitThreads, 2>;
+    if (int rc = chi2_smem(ctx, (const void *)kern, nx, P.nbath, nt, &smem)) return rc;
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
     cfg.gridDim = dim3((unsigned)(nbatch * ncta));
@@ -681,15 +896,31 @@ static int fit_on_device(mo_ed_ctx *ctx, FitProblem &P, int nbatch, double *x, d
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    MOED_CUDA(ctx, cudaLaunchKernelEx(&cfg, k_fit, (double *)dx.p, nx, P.nwloc, P.norb, P.nbath,
+    // persistent clusters: as many as fit on the GPU at once, at most nbatch
+    // (more would only start when others leave, and find less work)
+    int nclu = nbatch, resident = 0;
+    if (cudaOccupancyMaxActiveClusters(&resident, kern, &cfg) == cudaSuccess && resident > 0)
+        nclu = std::min(nbatch, resident);
+    else
+        (void)cudaGetLastError();
+    cfg.gridDim = dim3((unsigned)(nclu * ncta));
+    MOED_CUDA(ctx, cudaLaunchKernelEx(&cfg, kern, (double *)dx.p, nbatch, nx, P.nwloc, P.norb, P.nbath,
                                       (const double *)P.omega.p, (const double *)P.dev.p, ctx->opt.fortran_cmplx,
-                                      ftol, ncta, (double *)df.p, (int *)di.p, (int *)ds.p));
+                                      ftol, ncta, kFitQuantum, q, flag, its, (double *)dst.p, (double *)df.p,
+                                      (int *)di.p, (int *)ds.p));
     MOED_CHECK_LAUNCH(ctx);
+    int qh[kQWords];
     MOED_CUDA(ctx, cudaMemcpyAsync(x, dx.p, sizeof(double) * (size_t)nbatch * nx, cudaMemcpyDeviceToHost, ctx->stream));
     MOED_CUDA(ctx, cudaMemcpyAsync(fret, df.p, sizeof(double) * nbatch, cudaMemcpyDeviceToHost, ctx->stream));
     MOED_CUDA(ctx, cudaMemcpyAsync(iter, di.p, sizeof(int) * nbatch, cudaMemcpyDeviceToHost, ctx->stream));
     MOED_CUDA(ctx, cudaMemcpyAsync(status, ds.p, sizeof(int) * nbatch, cudaMemcpyDeviceToHost, ctx->stream));
+    MOED_CUDA(ctx, cudaMemcpyAsync(qh, dq.p, sizeof(qh), cudaMemcpyDeviceToHost, ctx->stream));
     MOED_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->fit_suspensions = qh[kQSusp];
+    ctx->fit_clusters = nclu;
+    for (int b = 0; b < nbatch; ++b)
+        if (status[b] == kFitSuspended)
+            return fail(ctx, MO_ED_ERR_CUDA, "k_fit: a fit was left unfinished by the cluster scheduler");
     return MO_ED_OK;
 }
 
@@ -763,6 +994,14 @@ int mo_ed_fit_batch(mo_ed_ctx *ctx, int nbatch, double *x, int nwloc, int ns, in
     FitProblem P;
     if (int rc = fit_problem(ctx, P, omega, D_ev, nwloc, ns, nxsize, nbath, norb)) return rc;
     return fit_on_device(ctx, P, nbatch, x, ftol, fret, iter, status);
+}
+
+int mo_ed_fit_stats(mo_ed_ctx *ctx, long long *suspensions, int *clusters)
+{
+    if (!ctx) return MO_ED_ERR_ARG;
+    if (suspensions) *suspensions = ctx->fit_suspensions;
+    if (clusters) *clusters = ctx->fit_clusters;
+    return MO_ED_OK;
 }
 
 int mo_ed_calc_dev(mo_ed_ctx *ctx, int norb, int nsite, int nwloc, const double *omega, const double *ek,

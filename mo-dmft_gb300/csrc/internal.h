@@ -247,6 +247,9 @@ struct mo_ed_ctx {
     long long diag_matvecs = 0;
     double diag_res_est = 0.0, diag_res_true = 0.0;
     double refine_res = 0.0;   // largest Ritz residual of the last FP64 refinement (green_fp64)
+    // the last bath fit (mo_ed_fit_stats): suspensions, persistent clusters
+    long long fit_suspensions = 0;
+    int fit_clusters = 0;
 
     // sectors / omega
     std::vector<int> nelec, nup;

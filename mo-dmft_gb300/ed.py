@@ -109,6 +109,7 @@ SIGNATURES = [
                                      _dp, _ip]),
     ("mo_ed_fit_batch", C.c_int, [C.c_void_p, C.c_int, _dp, C.c_int, C.c_int, C.c_int, _dp, _dp, C.c_int,
                                   C.c_int, C.c_double, _dp, _ip, _ip]),
+    ("mo_ed_fit_stats", C.c_int, [C.c_void_p, _llp, _ip]),
     ("mo_ed_chi2_grad_dev", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p,
                                       C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     ("mo_ed_calc_dev", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp]),
@@ -478,6 +479,13 @@ class EDSolver:
         self._chk(lib().mo_ed_fit_batch(self._ctx, nb, _d(X), len(om), Nbath + Norb, nx, _d(om), _d(_dev_f(D_ev)),
                                         Nbath, Norb, ftol, _d(fret), it.ctypes.data_as(_ip), st.ctypes.data_as(_ip)))
         return X, fret, it, st
+
+    def fit_stats(self):
+        """Suspensions (a fit giving up its cluster to a waiting fit) and
+        clusters launched, of the last fit_batch / minimization."""
+        n, c = C.c_longlong(), C.c_int()
+        self._chk(lib().mo_ed_fit_stats(self._ctx, C.byref(n), C.byref(c)))
+        return dict(suspensions=n.value, clusters=c.value)
 
     def chi2_grad_dev(self, nbatch, dx, nwloc, nxsize, domega, ddev, Nbath, Norb, df, dg):
         self._chk(lib().mo_ed_chi2_grad_dev(self._ctx, nbatch, C.c_void_p(dx), nwloc, Nbath + Norb, nxsize,

@@ -165,3 +165,11 @@ def test_c5_fits_vs_oracle(solver, pkg, c5gold):
     assert np.median(d[both]) < 1e-2
     assert 0.3 <= (fret[both] < fo[both]).mean() <= 0.7
     assert 0.8 <= np.median(it[both]) / np.median(io[both]) <= 1.25
+    # the clusters took turns: fits were parked and resumed, and a parked
+    # fit ends where it ends when run alone, bit for bit
+    stats = solver.fit_stats()
+    print("fit scheduler", stats)
+    assert 1 <= stats["clusters"] < 256 and stats["suspensions"] > 0
+    for b in np.flatnonzero(it > 600)[np.argsort(it[it > 600])][:3]:
+        Xs, fs, its, sts = solver.fit_batch(P["X0"][b:b + 1], P["omega"], P["dev"], nbath, norb)
+        assert sts[0] == st[b] and its[0] == it[b] and fs[0] == fret[b] and np.array_equal(Xs[0], X[b]), b
