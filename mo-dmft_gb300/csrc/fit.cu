@@ -124,11 +124,12 @@ __device__ __forceinline__ bool finite_bits(double x)
 // Per-thread partials are summed in a fixed order.  out[0] = sum_n,a
 // |r|^2 / w_n (thread 0); with grad out[1 + i] = the unscaled sum of
 // gradient row i (chi2_scale turns the sums into FUNC / dfunc).  Every
-// thread returns after a final barrier, so out may be shared memory read by
-// all next.
+// thread returns after a final barrier (unless final_sync is false: the
+// caller's next step is a barrier), so out may be shared memory read by all
+// next.
 __device__ void chi2_sums(const double *__restrict__ xb, int nx, bool grad, int nw, int n_first, int n_step,
                           int norb, int nbath, const double *__restrict__ omega, const double *__restrict__ dev,
-                          int fcmplx, double *sm, double *out)
+                          int fcmplx, double *sm, double *out, bool final_sync = true)
 {
     const int tid = threadIdx.x, nt = blockDim.x;
     double *sz = sm + (size_t)nx * nt;                 // [nbath][2][nt]
@@ -140,18 +141,23 @@ __device__ void chi2_sums(const double *__restrict__ xb, int nx, bool grad, int 
     const double *eps = xb;                            // eps_k
     const double *V = xb + nbath;                      // V[a*nbath + k]
     const double *ef = xb + nx - norb;                 // ef_a
-    if (tid < norb) {
-        int c = 0;
-        for (int k = 0; k < nbath; ++k) {
-            const double v = V[tid * nbath + k];
-            if ((__double_as_longlong(v) << 1) != 0 || !finite_bits(eps[k])) {
-                lk[tid * kListMax + c] = k;
-                lv[tid * kListMax + c] = v;
-                lv2[tid * kListMax + c] = v * v;
-                ++c;
+    if (tid < 32) {
+        // warp 0, lane k = bath level k (nbath < 32): per orbital, a ballot
+        // of the kept levels and each kept level's place among them
+        const int k = tid;
+        const bool eps_ok = k < nbath && finite_bits(eps[k]);
+        for (int a = 0; a < norb; ++a) {
+            const double v = k < nbath ? V[a * nbath + k] : 0.0;
+            const bool keep = k < nbath && ((__double_as_longlong(v) << 1) != 0 || !eps_ok);
+            const unsigned m = __ballot_sync(0xffffffffu, keep);
+            if (keep) {
+                const int c = __popc(m & ((1u << k) - 1u));
+                lk[a * kListMax + c] = k;
+                lv[a * kListMax + c] = v;
+                lv2[a * kListMax + c] = v * v;
             }
+            if (k == 0) lcnt[a] = __popc(m);
         }
-        lcnt[tid] = c;
     }
     if (grad)
         for (int i = 0; i < nx - norb; ++i) sm[(size_t)i * nt + tid] = 0.0;
@@ -236,7 +242,7 @@ __device__ void chi2_sums(const double *__restrict__ xb, int nx, bool grad, int 
         for (int i = tid; i < nx; i += nt)
             out[1 + i] = ((red[4 * i] + red[4 * i + 1]) + red[4 * i + 2]) + red[4 * i + 3];
     }
-    __syncthreads();
+    if (final_sync) __syncthreads();
 }
 
 // FUNC = sum / (norb^2 nw) (func.f90:40-43) from out[0] of chi2_sums over
@@ -667,7 +673,8 @@ struct DevChi2 {
     {
         const int nt = blockDim.x;
         double *mine = slots + par * (kMaxX + 1);
-        chi2_sums(sx, nx, grad, nw, rank * nt, ncta * nt, norb, nbath, omega, dev, fcmplx, sm, mine);
+        // with a cluster, its barrier right after the sums stands for their final CTA barrier
+        chi2_sums(sx, nx, grad, nw, rank * nt, ncta * nt, norb, nbath, omega, dev, fcmplx, sm, mine, ncta == 1);
         const int nout = grad ? nx + 1 : 1;
         if (ncta == 1) {
             for (int i = threadIdx.x; i < nout; i += nt)
