@@ -79,7 +79,11 @@ typedef struct {
                            to n.  Each thread solves its sectors through a worker context
                            of its own (stream and workspace); every sector's result is
                            the same as in one thread. */
-    int reserved[6];
+    int fit_quantum;    /* bath fits (mo_ed_fit_batch, mo_ed_minimization): CG
+                           iterations between a fit's looks for waiting fits, to which
+                           it then gives up its thread-block cluster (0: 256).  Results
+                           do not depend on it. */
+    int reserved[5];
 } mo_ed_options;
 
 /* ---- context ----------------------------------------------------------- */

@@ -152,7 +152,7 @@ int mo_ed_set_options(mo_ed_ctx *ctx, const mo_ed_options *o)
     if (o->nstep < 1 || o->nev < 1 || !(o->beta > 0) ||
         (o->precision != MO_ED_FP32 && o->precision != MO_ED_FP64) || o->gs_ncv < 0 ||
         o->gs_maxcycles < 1 || o->gs_tol < 0 || (o->green_fp64 != 0 && o->green_fp64 != 1) ||
-        o->solve_threads < 0 || o->solve_threads > 64)
+        o->solve_threads < 0 || o->solve_threads > 64 || o->fit_quantum < 0)
         return fail(ctx, MO_ED_ERR_ARG, "invalid options");
     if (o->green_reorth != 0)
         return fail(ctx, MO_ED_ERR_ARG, "green_reorth = 1 is not available: the Green's-function "

@@ -860,8 +860,9 @@ k_fit(double *__restrict__ X, int nbatch, int nx, int nw, int norb, int nbath, c
     if (ncta > 1) cg::this_cluster().sync();
 }
 
-// CG iterations between two looks for waiting fits: short against a long
-// fit (20000 iterations at most), long against a look (two cluster barriers)
+// CG iterations between two looks for waiting fits (mo_ed_options.fit_quantum
+// = 0): short against a long fit (20000 iterations at most), long against a
+// look (two cluster barriers)
 constexpr int kFitQuantum = 256;
 
 // nbatch fits of host parameter sets x[nbatch][nxsize], in place
@@ -913,7 +914,8 @@ static int fit_on_device(mo_ed_ctx *ctx, FitProblem &P, int nbatch, double *x, d
     cfg.gridDim = dim3((unsigned)(nclu * ncta));
     MOED_CUDA(ctx, cudaLaunchKernelEx(&cfg, kern, (double *)dx.p, nbatch, nx, P.nwloc, P.norb, P.nbath,
                                       (const double *)P.omega.p, (const double *)P.dev.p, ctx->opt.fortran_cmplx,
-                                      ftol, ncta, kFitQuantum, q, flag, its, (double *)dst.p, (double *)df.p,
+                                      ftol, ncta, ctx->opt.fit_quantum > 0 ? ctx->opt.fit_quantum : kFitQuantum, q,
+                                      flag, its, (double *)dst.p, (double *)df.p,
                                       (int *)di.p, (int *)ds.p));
     MOED_CHECK_LAUNCH(ctx);
     int qh[kQWords];

@@ -50,7 +50,8 @@ class Options(C.Structure):
     _fields_ = [("nstep", C.c_int), ("nev", C.c_int), ("beta", C.c_double), ("precision", C.c_int),
                 ("fortran_cmplx", C.c_int), ("gs_ncv", C.c_int), ("gs_maxcycles", C.c_int),
                 ("gs_tol", C.c_double), ("green_reorth", C.c_int),
-                ("green_fp64", C.c_int), ("solve_threads", C.c_int), ("reserved", C.c_int * 6)]
+                ("green_fp64", C.c_int), ("solve_threads", C.c_int), ("fit_quantum", C.c_int),
+                ("reserved", C.c_int * 5)]
 
 
 class EDError(RuntimeError):

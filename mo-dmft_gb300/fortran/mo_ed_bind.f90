@@ -36,7 +36,8 @@ module mo_ed_bind
         integer(c_int) :: green_reorth
         integer(c_int) :: green_fp64
         integer(c_int) :: solve_threads
-        integer(c_int) :: reserved(6)
+        integer(c_int) :: fit_quantum
+        integer(c_int) :: reserved(5)
     end type mo_ed_options
 
     interface

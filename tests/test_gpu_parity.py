@@ -681,6 +681,41 @@ def test_fit_small_grid_one_cta(solver, oracle, pkg):
         assert fret[b] < 1e-2 * f0 and fo < 1e-2 * f0
 
 
+def test_fit_parking_does_not_change_results(solver, oracle, pkg):
+    """A fit that gives up its cluster to a waiting fit, and is resumed later,
+    ends where it ends without a break, bit for bit.  The batches hold more
+    fits than the GPU runs at once, and fits look for waiting fits every 3 CG
+    iterations (fit_quantum).  They are compared with the same batches at the
+    default 256 and with fits run alone, on the one-CTA shape (128 w_n) and
+    on 4-CTA clusters (512 w_n).  ftol = 1e-5 keeps the fits short."""
+    P = pkg.configs.fit_config(seed=4, nbatch=3)
+    norb, nbath = P["norb"], P["nbath"]
+    ns, nx = norb + nbath, P["X0"].shape[1]
+    h = P["hidden"]
+    x_true = oracle.ev_to_x(np.concatenate([h["ef"], h["eps"]]), h["vk"], h["ef"], ns, nbath)
+    rng = np.random.default_rng(21)
+    solver.set_options(precision="fp64")
+    try:
+        for nw, nb in ((128, 160), (512, 80)):
+            om, dev = P["omega"][:nw], P["dev"][:, :nw]
+            X0 = x_true[None, :] + 0.05 * rng.standard_normal((nb, nx)) * (x_true[None, :] != 0)
+            solver.set_options(fit_quantum=3)
+            Xa, fa, ia, sa = solver.fit_batch(X0, om, dev, nbath, norb, ftol=1e-5)
+            stats = solver.fit_stats()
+            print(nw, stats, "CG iterations", int(ia.min()), int(np.median(ia)), int(ia.max()))
+            assert stats["suspensions"] > 0 and stats["clusters"] < nb
+            solver.set_options(fit_quantum=0)
+            Xb, fb, ib, sb = solver.fit_batch(X0, om, dev, nbath, norb, ftol=1e-5)
+            assert np.array_equal(Xa, Xb) and np.array_equal(fa, fb)
+            assert np.array_equal(ia, ib) and np.array_equal(sa, sb)
+            order = np.argsort(ia, kind="stable")
+            for b in order[[nb // 2, (3 * nb) // 4]]:
+                Xs, fs, its, sts = solver.fit_batch(X0[b:b + 1], om, dev, nbath, norb, ftol=1e-5)
+                assert sts[0] == sa[b] and its[0] == ia[b] and fs[0] == fa[b] and np.array_equal(Xs[0], Xa[b])
+    finally:
+        solver.set_options(fit_quantum=0)
+
+
 def test_calc_dev_vs_oracle(solver, oracle):
     rng = np.random.default_rng(10)
     norb, nbath = 3, 12
