@@ -472,7 +472,8 @@ class EDSolver:
         return x, fret.value, it.value
 
     def fit_batch(self, X, omega, D_ev, Nbath, Norb, ftol=1.0e-7):
-        """Many fits (rows of X) in lockstep -> (X_min, fret, iter, status)."""
+        """Many fits (rows of X) in one launch -> (X_min, fret, iter, status);
+        each row's result equals that of the same fit run alone."""
         X = np.array(X, dtype=np.float64, order="C")
         nb, nx = X.shape
         fret, it, st = np.zeros(nb), np.zeros(nb, np.int32), np.zeros(nb, np.int32)
