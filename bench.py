@@ -202,7 +202,8 @@ def lanczos_g_cpu(pkg, name, nev, states, matvecs, full=False, seconds=3.0):
 
 # H*v kernel of each tile-shape variant kind (hv_tuning's fourth field)
 KERNEL_NAMES = {0: "k_hv", 1: "k_hv_async", 2: "k_hv_down (128-byte slices) + k_hv_async<split>",
-                3: "k_hv_down (64-byte slices) + k_hv_async<split>"}
+                3: "k_hv_down (64-byte slices) + k_hv_async<split>",
+                4: "k_hv_down_rows (row AXPYs from L2) + k_hv_async<split>"}
 
 
 def lanczos_g(pkg, name, nev, precisions=("fp32", "fp32+g64", "fp64"), cpu=None):

@@ -40,6 +40,7 @@
 // adds the other terms.  The autotuner picks among all of them per
 // (precision, sector).
 #include <algorithm>
+#include <climits>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -1153,6 +1154,47 @@ k_hv_down(const __grid_constant__ HvBatch<TA> batch, int total, const DownLayout
     asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
+// ---------------------------------------------------------------------------
+// k_hv_down_rows: the same down-spin term as k_hv_down, as row AXPYs,
+//   y[d][c] = sum over moves (d -> d', t) of t * x[d'][c],
+// straight from the species' per-row move tables (dn_info / dn_tgt /
+// dn_val), with no staging.  A tile is one row d times 4 NT columns, each
+// thread four consecutive columns (16-byte loads and stores; rows are padded
+// to a multiple of 32 elements).  Tiles run column-tile-major: the CTAs in
+// flight share one column tile of x (C4: 6,435 rows x 512 columns, 13 MB),
+// which stays in L2 while each source segment is read by the rows that move
+// to it, so x comes from memory once per H*v.
+// ---------------------------------------------------------------------------
+template <typename TX, typename TA, typename TY, int NT>
+__global__ void __launch_bounds__(NT)
+k_hv_down_rows(const __grid_constant__ HvBatch<TA> batch, int total)
+{
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+        const int jid = hv_tile_job(batch, t);
+        const HvJobT<TA> &jb = batch.job[jid];
+        if (jb.active && *jb.active == 0) continue;
+        const int lt = t - jb.tile0;
+        const int ct = lt / jb.nd, d = lt - ct * jb.nd;
+        const int c = ct * 4 * NT + 4 * (int)threadIdx.x;
+        if (c >= jb.ld) continue;   // ld is a multiple of 4: c + 3 < ld
+        const int cnt = __ldg(&jb.dn_info[d]) & 0xff;
+        const TX *x = (const TX *)jb.x;
+        TA a[4] = {TA(0), TA(0), TA(0), TA(0)};
+#pragma unroll 4
+        for (int h = 0; h < cnt; ++h) {
+            const int dt = __ldg(&jb.dn_tgt[(size_t)h * jb.nd + d]);
+            const TA v = __ldg(&jb.dn_val[(size_t)h * jb.nd + d]);
+            const Vec4<TX> xv = ldg4(x + (size_t)dt * jb.ld + c);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) a[q] += v * (TA)xv.v[q];
+        }
+        TY o[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) o[q] = (TY)a[q];
+        stg4((TY *)jb.y + (size_t)d * jb.ld + c, o);
+    }
+}
+
 template <typename TX, typename TA, int R>
 static size_t dyn_smem_bytes_async(int ld, const ModelDev &m, const DescGeom &g)
 {
@@ -1173,14 +1215,16 @@ static size_t dyn_smem_bytes_async(int ld, const ModelDev &m, const DescGeom &g)
 struct HvVariant {
     int R, NT, MINB;
     // 0: k_hv; 1: k_hv_async (double-buffered asynchronous stage);
-    // 2 / 3: split, k_hv_down on 128- / 64-byte row slices + k_hv_async<SPLIT>
+    // 2 / 3: split, k_hv_down on 128- / 64-byte row slices + k_hv_async<SPLIT>;
+    // 4: split, k_hv_down_rows (row AXPYs from L2) + k_hv_async<SPLIT>
     int staged;
 };
 static const HvVariant kVarF32[] = {{3, 512, 2, 0}, {4, 256, 2, 0}, {6, 512, 1, 0}, {3, 256, 3, 0},
                                     {8, 512, 1, 0}, {4, 512, 1, 1}, {3, 512, 1, 1}, {2, 512, 2, 1},
-                                    {2, 256, 2, 1}, {3, 512, 1, 2}, {4, 512, 1, 2}, {3, 512, 1, 3}};
+                                    {2, 256, 2, 1}, {3, 512, 1, 2}, {4, 512, 1, 2}, {3, 512, 1, 3},
+                                    {3, 512, 1, 4}, {4, 512, 1, 4}};
 static const HvVariant kVarF64[] = {{2, 256, 2, 0}, {3, 256, 1, 0}, {2, 512, 1, 0}, {2, 512, 1, 1},
-                                    {4, 512, 1, 1}, {2, 512, 1, 2}, {2, 512, 1, 3}};
+                                    {4, 512, 1, 1}, {2, 512, 1, 2}, {2, 512, 1, 3}, {2, 512, 1, 4}};
 static const int kNVarF32 = sizeof(kVarF32) / sizeof(kVarF32[0]);
 static const int kNVarF64 = sizeof(kVarF64) / sizeof(kVarF64[0]);
 
@@ -1384,6 +1428,35 @@ static int launch_batch_split(mo_ed_ctx *ctx, const HvBatch<TA> &b0)
     return launch_batch_async<TX, TA, TY, R, NT, MINB, true>(ctx, b);
 }
 
+// Split H*v with the row-AXPY down pass: k_hv_down_rows writes the
+// down-spin hybridisation into y, then k_hv_async<SPLIT> adds the rest.
+constexpr int kRowsNT = 128;   // 512 columns per tile
+template <typename TX, typename TA, typename TY, int R, int NT, int MINB>
+static int launch_batch_rows(mo_ed_ctx *ctx, const HvBatch<TA> &b0)
+{
+    if (b0.total_items <= 0) return MO_ED_OK;
+    HvBatch<TA> b = b0;
+    long long tiles = 0;
+    for (int i = 0; i < b.njobs; ++i) {
+        HvJobT<TA> &j = b.job[i];
+        if (!j.dn_info || !j.dn_tgt || !j.dn_val || j.ld % 4 != 0)
+            return fail(ctx, MO_ED_ERR_STATE, "H*v down-spin move tables missing");
+        j.tile0 = (int)tiles;
+        j.ntiles = j.nd * ((j.ld + 4 * kRowsNT - 1) / (4 * kRowsNT));
+        tiles += j.ntiles;
+    }
+    if (tiles > INT_MAX) return fail(ctx, MO_ED_ERR_ARG, "too many row tiles for the row-AXPY H*v");
+    auto kd = k_hv_down_rows<TX, TA, TY, kRowsNT>;
+    int per_sm = 0;
+    if (int rc = kernel_fit(ctx, kd, kRowsNT, 0, &per_sm)) return rc;
+    const int grid = (int)std::min<long long>(tiles, (long long)ctx->num_sms * std::max(per_sm, 1));
+    if (grid > 0) {
+        kd<<<grid, kRowsNT, 0, ctx->stream>>>(b, (int)tiles);
+        MOED_CHECK_LAUNCH(ctx);
+    }
+    return launch_batch_async<TX, TA, TY, R, NT, MINB, true>(ctx, b);
+}
+
 // Whether the split kernel fits every down-spin block of the model (any
 // electron count: at most dblk_bound rows and dblk_mv_bound moves).
 static bool split_fits(const mo_ed_ctx *ctx, size_t wb, size_t ent_bytes)
@@ -1443,7 +1516,9 @@ static int launch_variant(mo_ed_ctx *ctx, int kind, int v, const HvBatch<TA> &b)
         case 8: return launch_batch_async<float, float, float, 2, 256, 2>(ctx, b);
         case 9: return launch_batch_split<float, float, float, 3, 512, 1, 128>(ctx, b);
         case 10: return launch_batch_split<float, float, float, 4, 512, 1, 128>(ctx, b);
-        default: return launch_batch_split<float, float, float, 3, 512, 1, 64>(ctx, b);
+        case 11: return launch_batch_split<float, float, float, 3, 512, 1, 64>(ctx, b);
+        case 12: return launch_batch_rows<float, float, float, 3, 512, 1>(ctx, b);
+        default: return launch_batch_rows<float, float, float, 4, 512, 1>(ctx, b);
         }
     } else if (kind == HV_F64) {
         switch (v) {
@@ -1453,7 +1528,8 @@ static int launch_variant(mo_ed_ctx *ctx, int kind, int v, const HvBatch<TA> &b)
         case 3: return launch_batch_async<double, double, double, 2, 512>(ctx, b);
         case 4: return launch_batch_async<double, double, double, 4, 512>(ctx, b);
         case 5: return launch_batch_split<double, double, double, 2, 512, 1, 128>(ctx, b);
-        default: return launch_batch_split<double, double, double, 2, 512, 1, 64>(ctx, b);
+        case 6: return launch_batch_split<double, double, double, 2, 512, 1, 64>(ctx, b);
+        default: return launch_batch_rows<double, double, double, 2, 512, 1>(ctx, b);
         }
     } else {
         switch (v) {
@@ -1463,7 +1539,8 @@ static int launch_variant(mo_ed_ctx *ctx, int kind, int v, const HvBatch<TA> &b)
         case 3: return launch_batch_async<float, double, double, 2, 512>(ctx, b);
         case 4: return launch_batch_async<float, double, double, 4, 512>(ctx, b);
         case 5: return launch_batch_split<float, double, double, 2, 512, 1, 128>(ctx, b);
-        default: return launch_batch_split<float, double, double, 2, 512, 1, 64>(ctx, b);
+        case 6: return launch_batch_split<float, double, double, 2, 512, 1, 64>(ctx, b);
+        default: return launch_batch_rows<float, double, double, 2, 512, 1>(ctx, b);
         }
     }
 }
@@ -1520,7 +1597,7 @@ static int prepare_variant(mo_ed_ctx *ctx, const Sector &s, int kind, int v)
     int n;
     if (int rc = species_items(ctx, s.dn, h.R, &items, &n)) return rc;
     if (!h.staged) return MO_ED_OK;
-    if (h.staged >= 2) {
+    if (h.staged == 2 || h.staged == 3) {
         // the split kernel stages whole down-spin blocks: the largest block of
         // the model (any electron count) must fit one CTA's shared memory
         const size_t wb = h.staged == 2 ? 128 : 64;
@@ -1636,7 +1713,8 @@ int hv_lookup(mo_ed_ctx *ctx, const Sector &s, int kind, int *v_out, int *R_out)
     bool ready = s.dn->items.count(R) != 0;
     if (h.staged)
         ready = ready && s.up->sched_rf.count(R) && s.dn->desc.count(R * 2 + (kind == HV_F32 ? 0 : 1));
-    if (h.staged >= 2) ready = ready && s.dn->dblk_ptr != nullptr && s.dn->dblk_chunks.count(s.ld());
+    if (h.staged == 2 || h.staged == 3)
+        ready = ready && s.dn->dblk_ptr != nullptr && s.dn->dblk_chunks.count(s.ld());
     if (!ready) return fail(ctx, MO_ED_ERR_STATE, "H*v item table of this sector not built yet");
     if (v_out) *v_out = it->second;
     if (R_out) *R_out = R;

@@ -122,11 +122,12 @@ def test_multiply_h_fp32(setup, oracle, name):
 @pytest.mark.parametrize("name", ["3x6_block", "4x4_mixed", "5x2_dense"])
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-13), ("fp32", 2e-6)])
 def test_multiply_h_every_variant(setup, oracle, pkg, name, precision, tol):
-    """Each tile-shape variant (k_hv, the double-buffered staged k_hv_async and the
-    split k_hv_down + k_hv_async), pinned in turn, against the oracle on several
-    sectors.  The split variants need every down-spin block of the model in one
-    CTA's shared memory: the dense-V model has one block per sector and rejects
-    them with MO_ED_ERR_ARG."""
+    """Each tile-shape variant (k_hv, the double-buffered staged k_hv_async, the
+    split k_hv_down + k_hv_async and the split k_hv_down_rows + k_hv_async),
+    pinned in turn, against the oracle on several sectors.  The k_hv_down split
+    variants need every down-spin block of the model in one CTA's shared
+    memory: the dense-V model has one block per sector and rejects them with
+    MO_ED_ERR_ARG."""
     s, m = setup(name, precision=precision)
     dt = pkg.FP32 if precision == "fp32" else pkg.FP64
     ns = m.nsite
@@ -195,8 +196,8 @@ def test_multiply_h_symmetric_c3(setup, oracle):
 def test_multiply_h_c4_full_size(solver, pkg):
     """C4 ground sector at full size (D = 41,409,225): FP64 symmetry <x|Hy> =
     <y|Hx>, linearity, and every FP32 tile-shape variant (previous, staged and
-    split kernels) against the FP64 product of the same FP32 input; the FP64
-    split variants against the FP64 product."""
+    both split kernels) against the FP64 product of the same FP32 input; the
+    FP64 split variants against the FP64 product."""
     cfg = pkg.configs.config("C4")
     ek, vk = cfg.model()
     solver.set_options(precision="fp64")
@@ -220,7 +221,7 @@ def test_multiply_h_c4_full_size(solver, pkg):
         solver.hv_set_variant(nu, nd, v, pkg.FP32)
         assert rel(solver.multiply_H(nu, nd, x32), h64) < 2e-6, (v, shape)
         kinds.add(shape[3])
-    assert kinds == {0, 1, 2, 3}
+    assert kinds == {0, 1, 2, 3, 4}
     variants, chosen = solver.hv_tuning(nu, nd, pkg.FP64)
     for v, (shape, ms) in enumerate(variants):
         if shape[3] >= 2:
