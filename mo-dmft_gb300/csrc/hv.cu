@@ -36,9 +36,9 @@
 // scheduled up-spin gathers, precomputed item descriptors.
 //
 // Split (below): k_hv_down computes the down-spin hybridisation over
-// down-spin blocks x column slices from shared memory, then k_hv_async<SPLIT>
-// adds the other terms.  The autotuner picks among all of them per
-// (precision, sector).
+// down-spin blocks x column slices from shared memory, or k_hv_down_rows as
+// row AXPYs from L2; then k_hv_async<SPLIT> adds the other terms.  The
+// autotuner picks among all of them per (precision, sector).
 #include <algorithm>
 #include <climits>
 #include <map>
