@@ -1158,14 +1158,16 @@ k_hv_down(const __grid_constant__ HvBatch<TA> batch, int total, const DownLayout
 // k_hv_down_rows: the same down-spin term as k_hv_down, as row AXPYs,
 //   y[d][c] = sum over moves (d -> d', t) of t * x[d'][c],
 // straight from the species' per-row move tables (dn_info / dn_tgt /
-// dn_val), with no staging.  A tile is one row d times 4 NT columns, each
-// thread four consecutive columns (16-byte loads and stores; rows are padded
-// to a multiple of 32 elements).  Tiles run column-tile-major: the CTAs in
-// flight share one column tile of x (C4: 6,435 rows x 512 columns, 13 MB),
-// which stays in L2 while each source segment is read by the rows that move
-// to it, so x comes from memory once per H*v.
+// dn_val), with no staging.  A tile is one row d times 4 NT CPT columns,
+// each thread CPT chunks of four consecutive columns, 4 NT apart (16-byte
+// loads and stores; rows are padded to a multiple of 32 elements): one load
+// of a move's target row serves CPT independent loads of x.  Tiles run
+// column-tile-major: the CTAs in flight share one column tile of x (C4 with
+// CPT = 2: 6,435 rows x 1,024 columns, 26 MB), which stays in L2 while each
+// source segment is read by the rows that move to it, so x comes from memory
+// about once per H*v.
 // ---------------------------------------------------------------------------
-template <typename TX, typename TA, typename TY, int NT>
+template <typename TX, typename TA, typename TY, int NT, int CPT>
 __global__ void __launch_bounds__(NT)
 k_hv_down_rows(const __grid_constant__ HvBatch<TA> batch, int total)
 {
@@ -1175,23 +1177,37 @@ k_hv_down_rows(const __grid_constant__ HvBatch<TA> batch, int total)
         if (jb.active && *jb.active == 0) continue;
         const int lt = t - jb.tile0;
         const int ct = lt / jb.nd, d = lt - ct * jb.nd;
-        const int c = ct * 4 * NT + 4 * (int)threadIdx.x;
-        if (c >= jb.ld) continue;   // ld is a multiple of 4: c + 3 < ld
+        const int c0 = ct * 4 * NT * CPT + 4 * (int)threadIdx.x;
+        if (c0 >= jb.ld) continue;   // ld is a multiple of 4: a chunk at c < ld ends before ld
         const int cnt = __ldg(&jb.dn_info[d]) & 0xff;
         const TX *x = (const TX *)jb.x;
-        TA a[4] = {TA(0), TA(0), TA(0), TA(0)};
+        TA a[CPT][4];
+#pragma unroll
+        for (int k = 0; k < CPT; ++k)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) a[k][q] = TA(0);
 #pragma unroll 4
         for (int h = 0; h < cnt; ++h) {
             const int dt = __ldg(&jb.dn_tgt[(size_t)h * jb.nd + d]);
             const TA v = __ldg(&jb.dn_val[(size_t)h * jb.nd + d]);
-            const Vec4<TX> xv = ldg4(x + (size_t)dt * jb.ld + c);
+            const TX *xr = x + (size_t)dt * jb.ld;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) a[q] += v * (TA)xv.v[q];
+            for (int k = 0; k < CPT; ++k)
+                if (k == 0 || c0 + k * 4 * NT < jb.ld) {   // chunk 0 is in range (checked above)
+                    const Vec4<TX> xv = ldg4(xr + c0 + k * 4 * NT);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) a[k][q] += v * (TA)xv.v[q];
+                }
         }
-        TY o[4];
+        TY *yr = (TY *)jb.y + (size_t)d * jb.ld;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) o[q] = (TY)a[q];
-        stg4((TY *)jb.y + (size_t)d * jb.ld + c, o);
+        for (int k = 0; k < CPT; ++k)
+            if (k == 0 || c0 + k * 4 * NT < jb.ld) {
+                TY o[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) o[q] = (TY)a[k][q];
+                stg4(yr + c0 + k * 4 * NT, o);
+            }
     }
 }
 
@@ -1222,7 +1238,7 @@ struct HvVariant {
 static const HvVariant kVarF32[] = {{3, 512, 2, 0}, {4, 256, 2, 0}, {6, 512, 1, 0}, {3, 256, 3, 0},
                                     {8, 512, 1, 0}, {4, 512, 1, 1}, {3, 512, 1, 1}, {2, 512, 2, 1},
                                     {2, 256, 2, 1}, {3, 512, 1, 2}, {4, 512, 1, 2}, {3, 512, 1, 3},
-                                    {3, 512, 1, 4}, {4, 512, 1, 4}};
+                                    {3, 512, 1, 4}, {4, 512, 1, 4}, {4, 512, 1, 4}};
 static const HvVariant kVarF64[] = {{2, 256, 2, 0}, {3, 256, 1, 0}, {2, 512, 1, 0}, {2, 512, 1, 1},
                                     {4, 512, 1, 1}, {2, 512, 1, 2}, {2, 512, 1, 3}, {2, 512, 1, 4}};
 static const int kNVarF32 = sizeof(kVarF32) / sizeof(kVarF32[0]);
@@ -1430,8 +1446,8 @@ static int launch_batch_split(mo_ed_ctx *ctx, const HvBatch<TA> &b0)
 
 // Split H*v with the row-AXPY down pass: k_hv_down_rows writes the
 // down-spin hybridisation into y, then k_hv_async<SPLIT> adds the rest.
-constexpr int kRowsNT = 128;   // 512 columns per tile
-template <typename TX, typename TA, typename TY, int R, int NT, int MINB>
+constexpr int kRowsNT = 128;   // 512 CPT columns per tile
+template <typename TX, typename TA, typename TY, int R, int NT, int MINB, int CPT = 2>
 static int launch_batch_rows(mo_ed_ctx *ctx, const HvBatch<TA> &b0)
 {
     if (b0.total_items <= 0) return MO_ED_OK;
@@ -1442,11 +1458,11 @@ static int launch_batch_rows(mo_ed_ctx *ctx, const HvBatch<TA> &b0)
         if (!j.dn_info || !j.dn_tgt || !j.dn_val || j.ld % 4 != 0)
             return fail(ctx, MO_ED_ERR_STATE, "H*v down-spin move tables missing");
         j.tile0 = (int)tiles;
-        j.ntiles = j.nd * ((j.ld + 4 * kRowsNT - 1) / (4 * kRowsNT));
+        j.ntiles = j.nd * ((j.ld + 4 * kRowsNT * CPT - 1) / (4 * kRowsNT * CPT));
         tiles += j.ntiles;
     }
     if (tiles > INT_MAX) return fail(ctx, MO_ED_ERR_ARG, "too many row tiles for the row-AXPY H*v");
-    auto kd = k_hv_down_rows<TX, TA, TY, kRowsNT>;
+    auto kd = k_hv_down_rows<TX, TA, TY, kRowsNT, CPT>;
     int per_sm = 0;
     if (int rc = kernel_fit(ctx, kd, kRowsNT, 0, &per_sm)) return rc;
     const int grid = (int)std::min<long long>(tiles, (long long)ctx->num_sms * std::max(per_sm, 1));
@@ -1518,7 +1534,8 @@ static int launch_variant(mo_ed_ctx *ctx, int kind, int v, const HvBatch<TA> &b)
         case 10: return launch_batch_split<float, float, float, 4, 512, 1, 128>(ctx, b);
         case 11: return launch_batch_split<float, float, float, 3, 512, 1, 64>(ctx, b);
         case 12: return launch_batch_rows<float, float, float, 3, 512, 1>(ctx, b);
-        default: return launch_batch_rows<float, float, float, 4, 512, 1>(ctx, b);
+        case 13: return launch_batch_rows<float, float, float, 4, 512, 1>(ctx, b);
+        default: return launch_batch_rows<float, float, float, 4, 512, 1, 4>(ctx, b);   // 2,048-column tiles
         }
     } else if (kind == HV_F64) {
         switch (v) {
