@@ -112,3 +112,49 @@ def test_header_compiles_standalone(tmp_path, lang, std):
                         "-I", os.path.join(ROOT, "include"), "-c", str(src), "-o", str(tmp_path / "u.o")],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_options_layout_matches_header(tmp_path, pkg):
+    """mo_ed_options has three copies: the C header, the ctypes mirror
+    (ed.Options) and the Fortran bind(C) type (mo_ed_bind.f90).  The same
+    fields in the same order with the same kinds, and the ctypes offsets and
+    size equal the C compiler's."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc")
+    if cc is None:
+        pytest.skip("no host compiler")
+    txt = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    body = re.search(r"typedef struct\s*\{(.*?)\}\s*mo_ed_options;", txt, re.S).group(1)
+    cfields = []   # (name, C type, array length)
+    for m in re.finditer(r"\b(int|double)\s+(\w+)(?:\[(\d+)\])?\s*;", body):
+        cfields.append((m.group(2), m.group(1), int(m.group(3) or 0)))
+    names = [f[0] for f in cfields]
+    prog = ['#include <stddef.h>', '#include <stdio.h>', '#include "mo_ed.h"', 'int main(void) {',
+            '  printf("%zu\\n", sizeof(mo_ed_options));']
+    prog += [f'  printf("%zu\\n", offsetof(mo_ed_options, {n}));' for n in names]
+    prog += ['  return 0;', '}']
+    src, exe = tmp_path / "layout.c", tmp_path / "layout"
+    src.write_text("\n".join(prog) + "\n")
+    subprocess.run([cc, "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    vals = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    size, offs = vals[0], vals[1:]
+    # ctypes mirror
+    O = pkg.Options
+    assert [f[0] for f in O._fields_] == names
+    assert C.sizeof(O) == size
+    for (n, _), off in zip(O._fields_, offs):
+        assert getattr(O, n).offset == off, n
+    for (n, ct), (_, ctype, arr) in zip(O._fields_, cfields):
+        base = ct._type_ if arr else ct
+        assert base == (C.c_int if ctype == "int" else C.c_double), n
+        if arr:
+            assert ct._length_ == arr, n
+    # Fortran bind(C) type: same names, kinds and array lengths, in order
+    f90 = open(os.path.join(ROOT, "mo-dmft_gb300", "fortran", "mo_ed_bind.f90")).read()
+    tbody = re.search(r"type, bind\(C\) :: mo_ed_options(.*?)end type mo_ed_options", f90, re.S | re.I).group(1)
+    ffields = [(m.group(3), m.group(1), int(m.group(4) or 0))
+               for m in re.finditer(r"(integer|real)\((c_int|c_double)\)\s*::\s*(\w+)(?:\((\d+)\))?", tbody)]
+    assert [f[0] for f in ffields] == names
+    for (n, kind, arr), (_, ctype, carr) in zip(ffields, cfields):
+        assert (kind == "integer") == (ctype == "int") and arr == carr, n
