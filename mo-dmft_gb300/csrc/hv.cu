@@ -1160,26 +1160,37 @@ k_hv_down(const __grid_constant__ HvBatch<TA> batch, int total, const DownLayout
 // straight from the species' per-row move tables (dn_info / dn_tgt /
 // dn_val), with no staging.  A tile is one row d times 4 NT CPT columns,
 // each thread CPT chunks of four consecutive columns, 4 NT apart (16-byte
-// loads and stores; rows are padded to a multiple of 32 elements): one load
-// of a move's target row serves CPT independent loads of x.  Tiles run
+// loads and stores; rows are padded to a multiple of 32 elements).  The
+// row's move targets and couplings are staged in shared memory first, one
+// per thread, so the x loads of all its moves can be in flight at once.
+// Tiles run
 // column-tile-major: the CTAs in flight share one column tile of x (C4 with
 // CPT = 2: 6,435 rows x 1,024 columns, 26 MB), which stays in L2 while each
 // source segment is read by the rows that move to it, so x comes from memory
 // about once per H*v.
 // ---------------------------------------------------------------------------
+// The host guarantees dn_maxcnt <= NT (launch_batch_rows).
 template <typename TX, typename TA, typename TY, int NT, int CPT>
 __global__ void __launch_bounds__(NT)
 k_hv_down_rows(const __grid_constant__ HvBatch<TA> batch, int total)
 {
-    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    __shared__ int s_tgt[NT];
+    __shared__ TA s_val[NT];
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {   // t is uniform over the CTA
         const int jid = hv_tile_job(batch, t);
         const HvJobT<TA> &jb = batch.job[jid];
         if (jb.active && *jb.active == 0) continue;
         const int lt = t - jb.tile0;
         const int ct = lt / jb.nd, d = lt - ct * jb.nd;
+        const int cnt = min(__ldg(&jb.dn_info[d]) & 0xff, NT);
+        __syncthreads();   // the previous tile is done with s_tgt / s_val
+        if ((int)threadIdx.x < cnt) {
+            s_tgt[threadIdx.x] = __ldg(&jb.dn_tgt[(size_t)threadIdx.x * jb.nd + d]);
+            s_val[threadIdx.x] = __ldg(&jb.dn_val[(size_t)threadIdx.x * jb.nd + d]);
+        }
+        __syncthreads();
         const int c0 = ct * 4 * NT * CPT + 4 * (int)threadIdx.x;
         if (c0 >= jb.ld) continue;   // ld is a multiple of 4: a chunk at c < ld ends before ld
-        const int cnt = __ldg(&jb.dn_info[d]) & 0xff;
         const TX *x = (const TX *)jb.x;
         TA a[CPT][4];
 #pragma unroll
@@ -1188,9 +1199,8 @@ k_hv_down_rows(const __grid_constant__ HvBatch<TA> batch, int total)
             for (int q = 0; q < 4; ++q) a[k][q] = TA(0);
 #pragma unroll 4
         for (int h = 0; h < cnt; ++h) {
-            const int dt = __ldg(&jb.dn_tgt[(size_t)h * jb.nd + d]);
-            const TA v = __ldg(&jb.dn_val[(size_t)h * jb.nd + d]);
-            const TX *xr = x + (size_t)dt * jb.ld;
+            const TA v = s_val[h];
+            const TX *xr = x + (size_t)s_tgt[h] * jb.ld;
 #pragma unroll
             for (int k = 0; k < CPT; ++k)
                 if (k == 0 || c0 + k * 4 * NT < jb.ld) {   // chunk 0 is in range (checked above)
@@ -1457,6 +1467,7 @@ static int launch_batch_rows(mo_ed_ctx *ctx, const HvBatch<TA> &b0)
         HvJobT<TA> &j = b.job[i];
         if (!j.dn_info || !j.dn_tgt || !j.dn_val || j.ld % 4 != 0)
             return fail(ctx, MO_ED_ERR_STATE, "H*v down-spin move tables missing");
+        if (j.dn_maxcnt > kRowsNT) return fail(ctx, MO_ED_ERR_ARG, "more down-spin moves per row than the row-AXPY CTA stages");
         j.tile0 = (int)tiles;
         j.ntiles = j.nd * ((j.ld + 4 * kRowsNT * CPT - 1) / (4 * kRowsNT * CPT));
         tiles += j.ntiles;
